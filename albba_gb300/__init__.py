@@ -1,0 +1,359 @@
+"""albba_gb300: GB300-native linear-algebra BFS (Python binding over the C ABI).
+
+The native library ``libalbba_gb300.so`` (built in-tree by
+``albba_gb300.build.build_library``) does all the work; this module only
+marshals arguments through ctypes. There is no Python or CPU fallback: if the
+library is missing, importing this package raises ImportError.
+
+Reference mapping (scalbba/albba):
+  run_custom_bfs_test (bfs/src/bfs.h:13-24)  ->  Graph.sell_build + Graph.bfs
+  run_bfs_ref's per-level frontier counts     ->  Stats / Graph.level_trace
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libalbba_gb300.so"
+
+if not LIB_PATH.exists():
+    raise ImportError(
+        f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+        "(there is no CPU fallback)")
+
+_lib = C.CDLL(str(LIB_PATH), mode=C.RTLD_GLOBAL)
+
+# ----------------------------------------------------------------- constants
+OK = 0
+ERR_INVALID, ERR_OOM, ERR_CUDA, ERR_TIMEOUT = -1, -2, -3, -4
+ERR_STATE, ERR_IO, ERR_UNSUPPORTED, ERR_DEVICE = -5, -6, -7, -8
+
+CSR_OUT, CSR_IN, CSR_SYMMETRIC, CSR_SORTED = 0, 1, 2, 4
+
+POLICY_BEAMER, POLICY_REF004, POLICY_LEARNED = 0, 1, 2
+POLICY_TOPDOWN, POLICY_BOTTOMUP, POLICY_BOTTOMUP_NOBYPASS = 3, 4, 5
+POLICIES = {"beamer": 0, "ref004": 1, "learned": 2, "topdown": 3, "bottomup": 4,
+            "bottomup_nobypass": 5}
+
+LOOP_HOST, LOOP_GRAPH, LOOP_PERSISTENT = 0, 1, 2
+LOOPS = {"host": 0, "graph": 1, "persistent": 2}
+
+DIR_TOPDOWN, DIR_BOTTOMUP, DIR_BOTTOMUP_NOBYPASS = 0, 1, 2
+
+EXPORTED = [
+    "alb_last_error", "alb_version", "alb_graph_create", "alb_graph_create32",
+    "alb_graph_destroy", "alb_graph_info", "alb_sell_opts_default", "alb_sell_build",
+    "alb_sell_export", "alb_bfs_opts_default", "alb_bfs", "alb_bfs_device",
+    "alb_level_trace", "alb_debug_fail_alloc_after", "alb_gen_rmat", "alb_gen_grid",
+    "alb_gen_er", "alb_csr_from_edges", "alb_pick_roots", "alb_host_csr_free",
+    "alb_cbd_write", "alb_cbd_read", "alb_selector_load", "alb_selector_clear",
+]
+
+
+class AlbError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"albba_gb300 error {code}: {msg}")
+        self.code = code
+
+
+# ------------------------------------------------------------------- structs
+class SellOpts(C.Structure):
+    _fields_ = [("C", C.c_int32), ("sigma", C.c_int32)]
+
+
+class BfsOpts(C.Structure):
+    _fields_ = [("policy", C.c_int32), ("loop", C.c_int32), ("alpha", C.c_float),
+                ("beta", C.c_float), ("block", C.c_int32), ("trace", C.c_int32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("num_levels", C.c_int32), ("levels_topdown", C.c_int32),
+                ("levels_bottomup", C.c_int32), ("pad_", C.c_int32), ("reached", C.c_int64),
+                ("edges", C.c_int64), ("ms", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad_"}
+
+
+class LevelRec(C.Structure):
+    _fields_ = [("dir", C.c_int32), ("level", C.c_int32), ("nf", C.c_int64), ("mf", C.c_int64),
+                ("nu", C.c_int64), ("mu", C.c_int64), ("active_slices", C.c_int64),
+                ("t_ns", C.c_int64)]
+
+
+class HostCsr(C.Structure):
+    _fields_ = [("n", C.c_int64), ("nnz", C.c_int64), ("rowptr", C.POINTER(C.c_int64)),
+                ("col", C.POINTER(C.c_int32))]
+
+
+_P = C.c_void_p
+_i32p = C.POINTER(C.c_int32)
+_i64p = C.POINTER(C.c_int64)
+
+_sigs = {
+    "alb_last_error": (C.c_char_p, []),
+    "alb_version": (C.c_char_p, []),
+    "alb_graph_create": (C.c_int32, [C.c_int64, _P, _P, C.c_uint32, C.POINTER(_P)]),
+    "alb_graph_create32": (C.c_int32, [C.c_int32, _P, _P, C.c_uint32, C.POINTER(_P)]),
+    "alb_graph_destroy": (None, [_P]),
+    "alb_graph_info": (C.c_int32, [_P, _i64p, _i64p]),
+    "alb_sell_opts_default": (None, [C.POINTER(SellOpts)]),
+    "alb_sell_build": (C.c_int32, [_P, C.POINTER(SellOpts), C.POINTER(C.c_double)]),
+    "alb_sell_export": (C.c_int32, [_P, _i64p, _P, _P, _P, _P]),
+    "alb_bfs_opts_default": (None, [C.POINTER(BfsOpts)]),
+    "alb_bfs": (C.c_int32, [_P, C.c_int32, C.POINTER(BfsOpts), _P, _P, C.POINTER(Stats)]),
+    "alb_bfs_device": (C.c_int32, [_P, C.c_int32, C.POINTER(BfsOpts), _P, _P, C.POINTER(Stats)]),
+    "alb_level_trace": (C.c_int32, [_P, C.c_int32, C.POINTER(LevelRec), _i32p]),
+    "alb_debug_fail_alloc_after": (None, [C.c_int32]),
+    "alb_gen_rmat": (C.c_int32, [C.c_int32, C.c_int32, C.c_uint64, C.c_double, C.c_double,
+                                 C.c_double, C.c_int32, C.POINTER(HostCsr)]),
+    "alb_gen_grid": (C.c_int32, [C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_uint64,
+                                 C.POINTER(HostCsr)]),
+    "alb_gen_er": (C.c_int32, [C.c_int64, C.c_double, C.c_uint64, C.POINTER(HostCsr)]),
+    "alb_csr_from_edges": (C.c_int32, [C.c_int64, C.c_int64, _P, _P, C.POINTER(HostCsr)]),
+    "alb_pick_roots": (C.c_int32, [C.POINTER(HostCsr), C.c_int32, C.c_uint64, _P]),
+    "alb_host_csr_free": (None, [C.POINTER(HostCsr)]),
+    "alb_cbd_write": (C.c_int32, [C.c_char_p, C.POINTER(HostCsr)]),
+    "alb_cbd_read": (C.c_int32, [C.c_char_p, C.POINTER(HostCsr)]),
+    "alb_selector_load": (C.c_int32, [C.c_int32, _P]),
+    "alb_selector_clear": (C.c_int32, [C.c_int32]),
+}
+for _name, (_res, _args) in _sigs.items():
+    _f = getattr(_lib, _name)
+    _f.restype = _res
+    _f.argtypes = _args
+
+
+def lib() -> C.CDLL:
+    return _lib
+
+
+def last_error() -> str:
+    return _lib.alb_last_error().decode()
+
+
+def version() -> str:
+    return _lib.alb_version().decode()
+
+
+def check(code: int) -> None:
+    if code != OK:
+        raise AlbError(code, last_error())
+
+
+def _ptr(a) -> int | None:
+    """Address of a numpy array or a torch tensor (None passes through)."""
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return a.ctypes.data
+
+
+# ---------------------------------------------------------------- host CSR
+class Csr:
+    """Host CSR: int64 row offsets, int32 columns (numpy)."""
+
+    def __init__(self, rowptr: np.ndarray, col: np.ndarray, _owner: HostCsr | None = None):
+        self.rowptr = rowptr
+        self.col = col
+        self._owner = _owner
+
+    @property
+    def n(self) -> int:
+        return int(self.rowptr.shape[0] - 1)
+
+    @property
+    def nnz(self) -> int:
+        return int(self.rowptr[-1])
+
+    def degrees(self) -> np.ndarray:
+        return np.diff(self.rowptr)
+
+    def _as_host(self) -> HostCsr:
+        h = HostCsr()
+        h.n = self.n
+        h.nnz = self.nnz
+        h.rowptr = self.rowptr.ctypes.data_as(_i64p)
+        h.col = self.col.ctypes.data_as(_i32p)
+        return h
+
+    def __del__(self):
+        if self._owner is not None:
+            _lib.alb_host_csr_free(C.byref(self._owner))
+            self._owner = None
+
+    def pick_roots(self, count: int, seed: int) -> np.ndarray:
+        roots = np.empty(count, dtype=np.int32)
+        h = self._as_host()
+        check(_lib.alb_pick_roots(C.byref(h), count, seed, roots.ctypes.data))
+        return roots
+
+    def write_cbd(self, path: str | os.PathLike) -> None:
+        h = self._as_host()
+        check(_lib.alb_cbd_write(str(path).encode(), C.byref(h)))
+
+
+def _wrap(h: HostCsr) -> Csr:
+    n, nnz = h.n, h.nnz
+    rp = np.ctypeslib.as_array(h.rowptr, shape=(n + 1,))
+    col = np.ctypeslib.as_array(h.col, shape=(max(nnz, 1),))[:nnz]
+    return Csr(rp, col, _owner=h)
+
+
+def gen_rmat(scale: int, edgefactor: int = 16, seed: int = 1, a: float = 0.57, b: float = 0.19,
+             c: float = 0.19, permute: bool = True) -> Csr:
+    h = HostCsr()
+    check(_lib.alb_gen_rmat(scale, edgefactor, seed, a, b, c, 1 if permute else 0, C.byref(h)))
+    return _wrap(h)
+
+
+def gen_grid(rows: int, cols: int, drop: float = 0.1, shortcut_frac: float = 1e-4,
+             seed: int = 1) -> Csr:
+    h = HostCsr()
+    check(_lib.alb_gen_grid(rows, cols, drop, shortcut_frac, seed, C.byref(h)))
+    return _wrap(h)
+
+
+def gen_er(n: int, mean_degree: float = 8.0, seed: int = 1) -> Csr:
+    h = HostCsr()
+    check(_lib.alb_gen_er(n, mean_degree, seed, C.byref(h)))
+    return _wrap(h)
+
+
+def csr_from_edges(n: int, u: np.ndarray, v: np.ndarray) -> Csr:
+    u = np.ascontiguousarray(u, dtype=np.int32)
+    v = np.ascontiguousarray(v, dtype=np.int32)
+    h = HostCsr()
+    check(_lib.alb_csr_from_edges(n, u.shape[0], u.ctypes.data, v.ctypes.data, C.byref(h)))
+    return _wrap(h)
+
+
+def read_cbd(path: str | os.PathLike) -> Csr:
+    h = HostCsr()
+    check(_lib.alb_cbd_read(str(path).encode(), C.byref(h)))
+    return _wrap(h)
+
+
+# -------------------------------------------------------------- device graph
+def bfs_opts(policy: str | int = "beamer", loop: str | int = "graph", alpha: float = 14.0,
+             beta: float = 24.0, block: int = 256, trace: bool = False) -> BfsOpts:
+    o = BfsOpts()
+    _lib.alb_bfs_opts_default(C.byref(o))
+    o.policy = POLICIES[policy] if isinstance(policy, str) else int(policy)
+    o.loop = LOOPS[loop] if isinstance(loop, str) else int(loop)
+    o.alpha, o.beta, o.block, o.trace = alpha, beta, block, 1 if trace else 0
+    return o
+
+
+@dataclass
+class SellExport:
+    nslices: int
+    perm: np.ndarray
+    width: np.ndarray
+    slice_off: np.ndarray
+    col: np.ndarray
+
+
+class Graph:
+    """A graph resident on the current CUDA device."""
+
+    def __init__(self, csr: Csr, flags: int = CSR_SYMMETRIC):
+        self._h = _P()
+        rp = np.ascontiguousarray(csr.rowptr, dtype=np.int64)
+        col = np.ascontiguousarray(csr.col, dtype=np.int32)
+        check(_lib.alb_graph_create(csr.n, rp.ctypes.data, col.ctypes.data, flags,
+                                    C.byref(self._h)))
+        self.n = csr.n
+        self.nnz = csr.nnz
+
+    @classmethod
+    def from_int32(cls, n: int, rowptr: np.ndarray, col: np.ndarray, flags: int) -> "Graph":
+        g = cls.__new__(cls)
+        g._h = _P()
+        rp = np.ascontiguousarray(rowptr, dtype=np.int32)
+        cc = np.ascontiguousarray(col, dtype=np.int32)
+        check(_lib.alb_graph_create32(n, rp.ctypes.data, cc.ctypes.data, flags, C.byref(g._h)))
+        g.n, g.nnz = n, int(rp[-1])
+        return g
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            _lib.alb_graph_destroy(self._h)
+            self._h = _P()
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def sell_build(self, C_: int = 32, sigma: int = 1024) -> float:
+        o = SellOpts(C_, sigma)
+        ms = C.c_double()
+        check(_lib.alb_sell_build(self._h, C.byref(o), C.byref(ms)))
+        return ms.value
+
+    def sell_export(self) -> SellExport:
+        ns = C.c_int64()
+        check(_lib.alb_sell_export(self._h, C.byref(ns), None, None, None, None))
+        perm = np.empty(self.n, np.int32)
+        width = np.empty(ns.value, np.int32)
+        off = np.empty(ns.value + 1, np.int64)
+        check(_lib.alb_sell_export(self._h, None, None, None, off.ctypes.data, None))
+        col = np.empty(int(off[-1]), np.int32)
+        check(_lib.alb_sell_export(self._h, None, perm.ctypes.data, width.ctypes.data, None,
+                                   col.ctypes.data))
+        return SellExport(ns.value, perm, width, off, col)
+
+    def bfs(self, root: int, opts: BfsOpts | None = None, want_level: bool = True,
+            want_parent: bool = True) -> tuple[np.ndarray | None, np.ndarray | None, Stats]:
+        lv = np.empty(self.n, np.int32) if want_level else None
+        pa = np.empty(self.n, np.int32) if want_parent else None
+        st = Stats()
+        o = opts or bfs_opts()
+        check(_lib.alb_bfs(self._h, int(root), C.byref(o), _ptr(lv), _ptr(pa), C.byref(st)))
+        return lv, pa, st
+
+    def bfs_device(self, root: int, d_level=None, d_parent=None,
+                   opts: BfsOpts | None = None) -> Stats:
+        st = Stats()
+        o = opts or bfs_opts()
+        check(_lib.alb_bfs_device(self._h, int(root), C.byref(o), _ptr(d_level), _ptr(d_parent),
+                                  C.byref(st)))
+        return st
+
+    def level_trace(self) -> list[LevelRec]:
+        cnt = C.c_int32()
+        check(_lib.alb_level_trace(self._h, 0, None, C.byref(cnt)))
+        buf = (LevelRec * max(cnt.value, 1))()
+        check(_lib.alb_level_trace(self._h, cnt.value, buf, C.byref(cnt)))
+        return list(buf[: cnt.value])
+
+
+def selector_load(which: int, params: np.ndarray) -> None:
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    assert p.size == 1443
+    check(_lib.alb_selector_load(which, p.ctypes.data))
+
+
+def selector_clear(which: int) -> None:
+    check(_lib.alb_selector_clear(which))
+
+
+def debug_fail_alloc_after(k: int) -> None:
+    _lib.alb_debug_fail_alloc_after(k)

@@ -1,0 +1,945 @@
+// Single-root direction-optimising BFS over SELL-C-sigma (position space).
+//
+// Reference: the level loop of run_custom_bfs_test (bfs/src/bfs_SELLCSv2.c:
+// 296-762) with its pull kernel (bfs/src/bfs_par_kernels.c:128-198), its
+// sparse-frontier kernel (:566-656) and the frontier representation changes
+// (:696-797). GB300 design:
+//
+//  * bottom-up pull (k_bu): one warp per 32-row bitmap word. The visited word
+//    is the slice bypass test (a full word is skipped), each unvisited lane
+//    walks its row with 16-byte int4 loads, tests frontier bits, and stops at
+//    the first hit (the smallest original id, rows being ascending) or at the
+//    padding (its own position). __ballot_sync drops the warp out as soon as
+//    no lane is active, and one ballot writes the next-frontier word: no
+//    atomics on the pull side.
+//  * top-down push (k_td): warp-cooperative over the frontier queue; the 32
+//    rows a warp holds are flattened by a warp prefix sum so every lane
+//    processes one edge per step regardless of degree skew. Unvisited targets
+//    get atomicMin(parent) (so the parent is the smallest original id) and an
+//    atomicOr claim on the next-frontier word; claimers append to the next
+//    queue with one atomicAdd per warp.
+//  * bitmap -> queue compaction (k_prep): ballot/popc warp prefix sums.
+//  * the level loop runs host-driven, as a CUDA graph whose while node is
+//    driven by a device-side decision, or as one persistent cooperative
+//    kernel with a bounded grid barrier.
+#include <algorithm>
+#include <cstring>
+#include <new>
+
+#include "graph.h"
+#include "selector.cuh"
+
+namespace alb {
+
+constexpr int kMaxBlock = 1024;
+constexpr uint64_t kBarrierTimeoutNs = 4ull * 1000 * 1000 * 1000;
+
+// Loads of bitmaps/queues: .nc is safe in standalone kernels (the data was
+// written by an earlier launch); the persistent kernel needs ordinary loads.
+template <bool kPersist, class T>
+__device__ __forceinline__ T ld_state(const T *p) {
+    if constexpr (kPersist)
+        return *(const volatile T *)p;
+    else
+        return __ldg(p);
+}
+template <bool kPersist>
+__device__ __forceinline__ uint32_t ld_bits(const uint32_t *p) {
+    if constexpr (kPersist)
+        return __ldcg(p);
+    else
+        return __ldg(p);
+}
+
+struct Range {
+    int bid, nblk;
+};
+
+// ------------------------------------------------------------ level phases
+
+// Decision (one warp). forced >= 0 overrides the policy (host-driven loop).
+__device__ int decide_warp(const BfsArgs &a, const BfsCtl &c, int forced) {
+    int dir;
+    if (forced >= 0) {
+        dir = forced;
+    } else if (c.policy == ALB_POLICY_LEARNED && a.mlp && a.mlp[kMlpParams] != 0.0f) {
+        float f[kMlpIn];
+        level_features(c, f);
+        dir = mlp_select_warp(a.mlp, f);
+    } else {
+        dir = rule_dir(c);
+    }
+    return dir;
+}
+
+__device__ void record_trace(const BfsArgs &a, const BfsCtl &c, int dir) {
+    if (a.trace && c.level < c.trace_cap) {
+        alb_level_rec r;
+        r.dir = dir;
+        r.level = c.level;
+        r.nf = c.nf;
+        r.mf = c.mf;
+        r.nu = c.nu;
+        r.mu = c.mu;
+        r.active_slices = c.active_words;
+        r.t_ns = (int64_t)globaltimer_ns();
+        a.trace[c.level] = r;
+    }
+}
+
+// F -> queue compaction and/or clearing of the next bitmap.
+template <bool kPersist>
+__device__ void prep_phase(const BfsArgs &a, int L, bool compact, bool zero_next, Range r) {
+    const uint32_t *F = (L & 1) ? a.bm1 : a.bm0;
+    uint32_t *N = (L & 1) ? a.bm0 : a.bm1;
+    int32_t *Q = (L & 1) ? a.q1 : a.q0;
+    unsigned long long *slot = &a.ctl->qn[L % 3];
+    const int lane = threadIdx.x & 31;
+    const int64_t wpb = blockDim.x >> 5;
+    const int64_t gw = (int64_t)r.bid * wpb + (threadIdx.x >> 5);
+    const int64_t stride = (int64_t)r.nblk * wpb * 32;
+    for (int64_t wb = gw * 32; wb < a.nwords; wb += stride) {
+        const int64_t w = wb + lane;
+        uint32_t word = 0;
+        if (w < a.nwords) {
+            if (compact) word = ld_bits<kPersist>(F + w);
+            if (zero_next) N[w] = 0;
+        }
+        if (!compact) continue;
+        const int cnt = __popc(word);
+        const int inc = warp_inclusive_scan(cnt);
+        const int tot = __shfl_sync(kFull, inc, 31);
+        unsigned long long base = 0;
+        if (lane == 31 && tot) base = atomicAdd(slot, (unsigned long long)tot);
+        base = __shfl_sync(kFull, base, 31);
+        int64_t pos = (int64_t)base + inc - cnt;
+        while (word) {
+            int b = __ffs(word) - 1;
+            word &= word - 1;
+            Q[pos++] = (int32_t)(w * 32 + b);
+        }
+    }
+}
+
+template <bool kPersist>
+__device__ void td_phase(const BfsArgs &a, int L, Range r) {
+    const int32_t *Q = (L & 1) ? a.q1 : a.q0;
+    int32_t *NQ = (L & 1) ? a.q0 : a.q1;
+    uint32_t *N = (L & 1) ? a.bm0 : a.bm1;
+    const int64_t qlen = (int64_t)ld_state<kPersist>(&a.ctl->qn[L % 3]);
+    unsigned long long *nq_slot = &a.ctl->qn[(L + 1) % 3];
+    __shared__ int64_t s_ex[kMaxBlock / 32][32];
+    __shared__ int64_t s_st[kMaxBlock / 32][32];
+    __shared__ int32_t s_ou[kMaxBlock / 32][32];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t wpb = blockDim.x >> 5;
+    const int64_t gw = (int64_t)r.bid * wpb + wib;
+    const int64_t stride = (int64_t)r.nblk * wpb * 32;
+    unsigned long long cn = 0, cmo = 0, cmi = 0;
+    const uint32_t lvl = (uint32_t)(L + 1);
+    for (int64_t cb = gw * 32; cb < qlen; cb += stride) {
+        const int64_t i = cb + lane;
+        int32_t u = i < qlen ? ld_state<kPersist>(Q + i) : -1;
+        int64_t st = 0, d = 0;
+        int32_t ou = 0;
+        if (u >= 0) {
+            st = __ldg(a.prow + u);
+            d = __ldg(a.prow + u + 1) - st;
+            ou = __ldg(a.perm + u);
+        }
+        const int64_t inc = warp_inclusive_scan(d);
+        const int64_t T = __shfl_sync(kFull, inc, 31);
+        s_ex[wib][lane] = inc - d;
+        s_st[wib][lane] = st;
+        s_ou[wib][lane] = ou;
+        __syncwarp();
+        for (int64_t eb = 0; eb < T; eb += 32) {
+            const int64_t e = eb + lane;
+            bool claimed = false;
+            int32_t v = 0;
+            if (e < T) {
+                int j = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1)
+                    if (s_ex[wib][j + step] <= e) j += step;
+                v = __ldg(a.pcol + s_st[wib][j] + (e - s_ex[wib][j]));
+                const uint32_t bit = 1u << (v & 31);
+                const uint32_t w = ld_bits<kPersist>(a.vis + (v >> 5));
+                if (!(w & bit)) {
+                    atomicMin(a.parent_pos + v, (uint32_t)s_ou[wib][j]);
+                    claimed = !(atomicOr(N + (v >> 5), bit) & bit);
+                }
+            }
+            const unsigned cm = __ballot_sync(kFull, claimed);
+            if (cm) {
+                const int leader = __ffs(cm) - 1;
+                unsigned long long base = 0;
+                if (lane == leader) base = atomicAdd(nq_slot, (unsigned long long)__popc(cm));
+                base = __shfl_sync(kFull, base, leader);
+                if (claimed) {
+                    NQ[base + __popc(cm & lanemask_lt())] = v;
+                    a.level_pos[v] = (int32_t)lvl;
+                    cn++;
+                    cmo += (unsigned long long)__ldg(a.odeg + v);
+                    cmi += (unsigned long long)__ldg(a.ideg + v);
+                }
+            }
+        }
+        __syncwarp();
+    }
+    cn = warp_sum(cn);
+    cmo = warp_sum(cmo);
+    cmi = warp_sum(cmi);
+    if (lane == 0 && cn) {
+        const int k = (L + 1) % 3;
+        atomicAdd(&a.ctl->acc_n[k], cn);
+        atomicAdd(&a.ctl->acc_mo[k], cmo);
+        atomicAdd(&a.ctl->acc_mi[k], cmi);
+    }
+}
+
+// After a top-down level: mark the new frontier visited, clear the old one.
+template <bool kPersist>
+__device__ void td_finish_phase(const BfsArgs &a, int L, Range r) {
+    const int32_t *Q = (L & 1) ? a.q1 : a.q0;
+    const int32_t *NQ = (L & 1) ? a.q0 : a.q1;
+    uint32_t *F = (L & 1) ? a.bm1 : a.bm0;
+    const int64_t qlen = (int64_t)ld_state<kPersist>(&a.ctl->qn[L % 3]);
+    const int64_t nqlen = (int64_t)ld_state<kPersist>(&a.ctl->qn[(L + 1) % 3]);
+    const int64_t m = qlen > nqlen ? qlen : nqlen;
+    unsigned long long full = 0;
+    for (int64_t i = (int64_t)r.bid * blockDim.x + threadIdx.x; i < m;
+         i += (int64_t)r.nblk * blockDim.x) {
+        if (i < nqlen) {
+            const int32_t v = ld_state<kPersist>(NQ + i);
+            const uint32_t bit = 1u << (v & 31);
+            const uint32_t old = atomicOr(a.vis + (v >> 5), bit);
+            full += (old != kFull && (old | bit) == kFull);
+        }
+        if (i < qlen) F[ld_state<kPersist>(Q + i) >> 5] = 0;
+    }
+    full = warp_sum(full);
+    if ((threadIdx.x & 31) == 0 && full) atomicAdd(&a.ctl->acc_full[(L + 1) % 3], full);
+}
+
+// Bottom-up pull. kBypass: skip words whose rows are all visited.
+// kEarly: stop each row at its first frontier source or its padding.
+template <bool kPersist, bool kBypass, bool kEarly>
+__device__ void bu_phase(const BfsArgs &a, int L, Range r) {
+    const uint32_t *F = (L & 1) ? a.bm1 : a.bm0;
+    uint32_t *N = (L & 1) ? a.bm0 : a.bm1;
+    const int lane = threadIdx.x & 31;
+    const int64_t wpb = blockDim.x >> 5;
+    const int64_t gw = (int64_t)r.bid * wpb + (threadIdx.x >> 5);
+    const int64_t stride = (int64_t)r.nblk * wpb;
+    const int32_t C = a.C, log2C = a.log2C;
+    const int32_t lvl = L + 1;
+    unsigned long long cn = 0, cmo = 0, cmi = 0, full = 0;
+    for (int64_t w = gw; w < a.nwords; w += stride) {
+        const uint32_t vis = ld_bits<kPersist>(a.vis + w);
+        if (kBypass && vis == kFull) {
+            if (lane == 0) N[w] = 0;
+            continue;
+        }
+        const int32_t p = (int32_t)(w * 32 + lane);
+        const int64_t s = (int64_t)p >> log2C;
+        bool active = !((vis >> lane) & 1u);
+        int32_t ng = 0;
+        const int4 *cp = nullptr;
+        if (active) {
+            ng = (__ldg(a.width + s) + 3) >> 2;
+            cp = a.col4 + (__ldg(a.slice_off + s) >> 2) + (p & (C - 1));
+        }
+        int32_t found = -1;
+        for (int32_t j = 0;; j++) {
+            active = active && (j < ng);
+            if (!__any_sync(kFull, active)) break;
+            if (!active) continue;
+            const int4 c = ld_nc(cp + (int64_t)j * C);
+            const uint32_t f0 = ld_bits<kPersist>(F + (c.x >> 5));
+            const uint32_t f1 = ld_bits<kPersist>(F + (c.y >> 5));
+            const uint32_t f2 = ld_bits<kPersist>(F + (c.z >> 5));
+            const uint32_t f3 = ld_bits<kPersist>(F + (c.w >> 5));
+            const int32_t cc[4] = {c.x, c.y, c.z, c.w};
+            const uint32_t ff[4] = {f0, f1, f2, f3};
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                if (!active) break;
+                if (kEarly && cc[k] == p) {
+                    active = false;  // padding: end of row
+                } else if ((ff[k] >> (cc[k] & 31)) & 1u) {
+                    if (found < 0) found = cc[k];
+                    if (kEarly) active = false;
+                }
+            }
+        }
+        const unsigned nm = __ballot_sync(kFull, found >= 0);
+        if (lane == 0) {
+            N[w] = nm;
+            if (nm) {
+                a.vis[w] = vis | nm;
+                full += (vis != kFull && (vis | nm) == kFull);
+            }
+        }
+        if (found >= 0) {
+            a.level_pos[p] = lvl;
+            a.parent_pos[p] = (uint32_t)__ldg(a.perm + found);
+            cn++;
+            cmo += (unsigned long long)__ldg(a.odeg + p);
+            cmi += (unsigned long long)__ldg(a.ideg + p);
+        }
+    }
+    cn = warp_sum(cn);
+    cmo = warp_sum(cmo);
+    cmi = warp_sum(cmi);
+    if (lane == 0 && (cn || full)) {
+        const int k = (L + 1) % 3;
+        if (cn) {
+            atomicAdd(&a.ctl->acc_n[k], cn);
+            atomicAdd(&a.ctl->acc_mo[k], cmo);
+            atomicAdd(&a.ctl->acc_mi[k], cmi);
+        }
+        if (full) atomicAdd(&a.ctl->acc_full[k], full);
+    }
+}
+
+// Level rollover from the accumulators of slot (L+1)%3 (values read with
+// coherent loads by the caller).
+__host__ __device__ inline void roll(BfsCtl &c, int dir, unsigned long long nn,
+                                     unsigned long long mo, unsigned long long mi,
+                                     unsigned long long fl) {
+    c.prev_nf = c.nf;
+    c.nf = (int64_t)nn;
+    c.mf = (int64_t)mo;
+    c.nu -= (int64_t)nn;
+    c.mu -= (int64_t)mi;
+    c.active_words -= (int64_t)fl;
+    c.reached += (int64_t)nn;
+    c.edges += (int64_t)mo;
+    c.q_valid = dir == ALB_DIR_TOPDOWN;
+    c.n_dirty = dir != ALB_DIR_TOPDOWN;
+    c.prev_dir = dir;
+    if (dir == ALB_DIR_TOPDOWN)
+        c.levels_td++;
+    else
+        c.levels_bu++;
+    c.level++;
+    if (nn == 0 || c.level >= c.level_cap) c.done = 1;
+}
+
+// ---------------------------------------------------- standalone kernels
+
+__global__ void k_init_bulk(BfsArgs a) {
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t str = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t p = tid; p < a.n; p += str) {
+        a.level_pos[p] = -1;
+        a.parent_pos[p] = 0xFFFFFFFFu;
+    }
+    for (int64_t w = tid; w < a.nwords; w += str) {
+        a.vis[w] = a.vinit[w];
+        a.bm0[w] = 0;
+        a.bm1[w] = 0;
+    }
+}
+
+struct InitParams {
+    int32_t root, policy, trace_cap, level_cap;
+    float alpha, beta, mean_deg, skew;
+    int64_t n_live, m_in, active0;
+};
+
+__global__ void k_init_root(BfsArgs a, InitParams ip) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int32_t rp = a.inv[ip.root];
+    const uint32_t bit = 1u << (rp & 31);
+    const uint32_t old = a.vis[rp >> 5];
+    a.vis[rp >> 5] = old | bit;
+    a.bm0[rp >> 5] |= bit;
+    a.q0[0] = rp;
+    a.level_pos[rp] = 0;
+    a.parent_pos[rp] = (uint32_t)ip.root;
+    BfsCtl c;
+    memset(&c, 0, sizeof(c));
+    c.level = 0;
+    c.dir = -1;
+    c.prev_dir = -1;
+    c.q_valid = 1;
+    c.n_dirty = 0;
+    c.policy = ip.policy;
+    c.alpha = ip.alpha;
+    c.beta = ip.beta;
+    c.n = a.n;
+    c.nwords = a.nwords;
+    c.nf = 1;
+    c.mf = a.odeg[rp];
+    c.prev_nf = 0;
+    const bool live = a.ideg[rp] > 0;  // discoverable by a pull
+    c.nu = ip.n_live - (live ? 1 : 0);
+    c.mu = ip.m_in - a.ideg[rp];
+    c.active_words = ip.active0 - ((old != kFull && (old | bit) == kFull) ? 1 : 0);
+    c.reached = 1;
+    c.edges = a.odeg[rp];
+    c.qn[0] = 1;
+    c.trace_cap = ip.trace_cap;
+    c.level_cap = ip.level_cap;
+    c.feat_mean_deg = ip.mean_deg;
+    c.feat_skew = ip.skew;
+    *a.ctl = c;
+}
+
+__global__ void k_decide(BfsArgs a, int forced, cudaGraphConditionalHandle sw) {
+    if (threadIdx.x >= 32) return;
+    const BfsCtl c = *a.ctl;
+    const int dir = decide_warp(a, c, forced);
+    if (threadIdx.x == 0) {
+        a.ctl->dir = dir;
+        record_trace(a, c, dir);
+        // zero the slots the next level will accumulate into
+        const int k = (c.level + 2) % 3;
+        a.ctl->acc_n[k] = 0;
+        a.ctl->acc_mo[k] = 0;
+        a.ctl->acc_mi[k] = 0;
+        a.ctl->acc_full[k] = 0;
+        a.ctl->qn[k] = 0;
+        if (sw) {
+            unsigned branch;
+            if (dir == ALB_DIR_TOPDOWN)
+                branch = (!c.q_valid || c.n_dirty) ? 1u : 0u;
+            else
+                branch = dir == ALB_DIR_BOTTOMUP ? 2u : 3u;
+            cudaGraphSetConditional(sw, branch);
+        }
+    }
+}
+
+__global__ void k_prep(BfsArgs a) {
+    const BfsCtl *c = a.ctl;
+    const int L = c->level;
+    prep_phase<false>(a, L, !c->q_valid, c->n_dirty != 0, Range{(int)blockIdx.x, (int)gridDim.x});
+}
+
+__global__ void k_td(BfsArgs a) {
+    td_phase<false>(a, a.ctl->level, Range{(int)blockIdx.x, (int)gridDim.x});
+}
+
+__global__ void k_td_finish(BfsArgs a) {
+    td_finish_phase<false>(a, a.ctl->level, Range{(int)blockIdx.x, (int)gridDim.x});
+}
+
+template <bool kBypass, bool kEarly>
+__global__ void k_bu(BfsArgs a) {
+    bu_phase<false, kBypass, kEarly>(a, a.ctl->level, Range{(int)blockIdx.x, (int)gridDim.x});
+}
+
+__global__ void k_end(BfsArgs a, cudaGraphConditionalHandle wh) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    BfsCtl c = *a.ctl;
+    const int k = (c.level + 1) % 3;
+    roll(c, c.dir, c.acc_n[k], c.acc_mo[k], c.acc_mi[k], c.acc_full[k]);
+    if (c.level < c.trace_cap) c.trace_len = c.level;
+    else c.trace_len = c.trace_cap;
+    *a.ctl = c;
+    if (wh) cudaGraphSetConditional(wh, c.done ? 0u : 1u);
+}
+
+__global__ void k_scatter(BfsArgs a, int32_t *level, int32_t *parent) {
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t str = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t p = tid; p < a.n; p += str) {
+        const int32_t v = a.perm[p];
+        if (level) level[v] = a.level_pos[p];
+        if (parent) parent[v] = (int32_t)a.parent_pos[p];
+    }
+}
+
+// ------------------------------------------------------ persistent kernel
+
+__device__ bool grid_sync(BfsCtl *ctl, unsigned nblocks) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *gen = &ctl->bar_gen;
+        const unsigned g0 = *gen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(&ctl->bar_count, 1u);
+        if (arrived == nblocks - 1) {
+            atomicExch(&ctl->bar_count, 0u);
+            __threadfence();
+            atomicAdd(&ctl->bar_gen, 1u);
+        } else {
+            const uint64_t t0 = globaltimer_ns();
+            while (*gen == g0) {
+                if (globaltimer_ns() - t0 > kBarrierTimeoutNs) {
+                    atomicExch(&ctl->err, ALB_ERR_TIMEOUT);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *(volatile int32_t *)&ctl->err == 0;
+}
+
+__global__ void __launch_bounds__(256) k_persistent(BfsArgs a) {
+    __shared__ BfsCtl c;
+    __shared__ int s_dir;
+    const unsigned nb = gridDim.x;
+    const Range r{(int)blockIdx.x, (int)gridDim.x};
+    if (threadIdx.x == 0) c = *a.ctl;  // written by an earlier launch
+    __syncthreads();
+    while (true) {
+        if (threadIdx.x < 32) {
+            const int dir = decide_warp(a, c, -1);
+            if (threadIdx.x == 0) {
+                s_dir = dir;
+                if (blockIdx.x == 0) {
+                    record_trace(a, c, dir);
+                    const int k = (c.level + 2) % 3;
+                    a.ctl->acc_n[k] = 0;
+                    a.ctl->acc_mo[k] = 0;
+                    a.ctl->acc_mi[k] = 0;
+                    a.ctl->acc_full[k] = 0;
+                    a.ctl->qn[k] = 0;
+                }
+            }
+        }
+        __syncthreads();
+        const int dir = s_dir;
+        const int L = c.level;
+        bool ok = true;
+        if (dir == ALB_DIR_TOPDOWN) {
+            if (!c.q_valid || c.n_dirty) {
+                prep_phase<true>(a, L, !c.q_valid, c.n_dirty != 0, r);
+                ok = grid_sync(a.ctl, nb);
+            }
+            if (ok) {
+                td_phase<true>(a, L, r);
+                ok = grid_sync(a.ctl, nb);
+            }
+            if (ok) {
+                td_finish_phase<true>(a, L, r);
+                ok = grid_sync(a.ctl, nb);
+            }
+        } else if (dir == ALB_DIR_BOTTOMUP) {
+            bu_phase<true, true, true>(a, L, r);
+            ok = grid_sync(a.ctl, nb);
+        } else {
+            bu_phase<true, false, false>(a, L, r);
+            ok = grid_sync(a.ctl, nb);
+        }
+        if (!ok) break;
+        if (threadIdx.x == 0) {
+            const int k = (L + 1) % 3;
+            volatile BfsCtl *g = a.ctl;
+            roll(c, dir, g->acc_n[k], g->acc_mo[k], g->acc_mi[k], g->acc_full[k]);
+            c.dir = dir;
+        }
+        __syncthreads();
+        if (c.done) break;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        // publish the rolling fields (accumulators and barrier stay as they are)
+        BfsCtl *g = a.ctl;
+        g->level = c.level;
+        g->dir = c.dir;
+        g->prev_dir = c.prev_dir;
+        g->q_valid = c.q_valid;
+        g->n_dirty = c.n_dirty;
+        g->done = c.done;
+        g->levels_td = c.levels_td;
+        g->levels_bu = c.levels_bu;
+        g->nf = c.nf;
+        g->mf = c.mf;
+        g->prev_nf = c.prev_nf;
+        g->nu = c.nu;
+        g->mu = c.mu;
+        g->active_words = c.active_words;
+        g->reached = c.reached;
+        g->edges = c.edges;
+        g->trace_len = c.level < c.trace_cap ? c.level : c.trace_cap;
+    }
+}
+
+// ------------------------------------------------------------- host side
+
+}  // namespace alb
+
+struct alb::CachedLoop {
+    int block = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace alb {
+
+alb_status bfs_scratch_alloc(alb_graph *g) {
+    BfsScratch &b = g->bfs;
+    if (b.ready) return ALB_OK;
+    const int64_t n = g->n, nw = g->sell.nwords;
+    ALB_TRY(dmalloc((void **)&b.bm0, sizeof(uint32_t) * nw, "frontier bitmap"));
+    ALB_TRY(dmalloc((void **)&b.bm1, sizeof(uint32_t) * nw, "frontier bitmap"));
+    ALB_TRY(dmalloc((void **)&b.vis, sizeof(uint32_t) * nw, "visited bitmap"));
+    ALB_TRY(dmalloc((void **)&b.q0, sizeof(int32_t) * n, "frontier queue"));
+    ALB_TRY(dmalloc((void **)&b.q1, sizeof(int32_t) * n, "frontier queue"));
+    ALB_TRY(dmalloc((void **)&b.level_pos, sizeof(int32_t) * n, "levels"));
+    ALB_TRY(dmalloc((void **)&b.parent_pos, sizeof(uint32_t) * n, "parents"));
+    ALB_TRY(dmalloc((void **)&b.ctl, sizeof(BfsCtl), "level control"));
+    b.trace_cap = (int32_t)std::min<int64_t>(n + 2, 1 << 16);
+    ALB_TRY(dmalloc((void **)&b.trace, sizeof(alb_level_rec) * b.trace_cap, "level trace"));
+    ALB_CK(cudaMallocHost((void **)&b.h_ctl, sizeof(BfsCtl)));
+    b.ready = true;
+    return ALB_OK;
+}
+
+void bfs_scratch_free(alb_graph *g) {
+    BfsScratch &b = g->bfs;
+    dfree(b.bm0);
+    dfree(b.bm1);
+    dfree(b.vis);
+    dfree(b.q0);
+    dfree(b.q1);
+    dfree(b.level_pos);
+    dfree(b.parent_pos);
+    dfree(b.out_level);
+    dfree(b.out_parent);
+    dfree(b.ctl);
+    dfree(b.trace);
+    if (b.h_ctl) cudaFreeHost(b.h_ctl);
+    b = BfsScratch();
+}
+
+void loop_cache_free(alb_graph *g) {
+    if (!g->loop) return;
+    if (g->loop->exec) cudaGraphExecDestroy(g->loop->exec);
+    if (g->loop->graph) cudaGraphDestroy(g->loop->graph);
+    delete g->loop;
+    g->loop = nullptr;
+}
+
+extern const float *selector_device_params(int which);
+extern bool selector_host_params(int which, float *out);
+
+BfsArgs make_args(alb_graph *g) {
+    const Sell &s = g->sell;
+    const BfsScratch &b = g->bfs;
+    BfsArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.n = g->n;
+    a.nslices = s.nslices;
+    a.nwords = s.nwords;
+    a.C = s.C;
+    a.log2C = s.log2C;
+    a.perm = s.perm;
+    a.inv = s.inv;
+    a.ideg = s.ideg;
+    a.odeg = s.odeg;
+    a.width = s.width;
+    a.slice_off = s.slice_off;
+    a.col4 = (const int4 *)s.col;
+    a.prow = s.prow;
+    a.pcol = s.pcol;
+    a.vinit = s.vinit;
+    a.bm0 = b.bm0;
+    a.bm1 = b.bm1;
+    a.vis = b.vis;
+    a.q0 = b.q0;
+    a.q1 = b.q1;
+    a.level_pos = b.level_pos;
+    a.parent_pos = b.parent_pos;
+    a.ctl = b.ctl;
+    a.trace = b.trace;
+    a.mlp = selector_device_params(0);
+    return a;
+}
+
+namespace {
+
+struct Launch {
+    unsigned grid;
+    unsigned block;
+};
+
+Launch level_launch(const alb_graph *g, int block) {
+    // every level kernel is a grid-stride loop: fill the GPU once
+    const int per_sm = std::max(1, 2048 / block);
+    return Launch{(unsigned)(g->num_sms * per_sm), (unsigned)block};
+}
+
+alb_status add_kernel_node(cudaGraph_t graph, cudaGraphNode_t *node, const cudaGraphNode_t *deps,
+                           size_t ndeps, void *func, Launch l, void **args) {
+    cudaKernelNodeParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.func = func;
+    p.gridDim = dim3(l.grid);
+    p.blockDim = dim3(l.block);
+    p.sharedMemBytes = 0;
+    p.kernelParams = args;
+    ALB_CK(cudaGraphAddKernelNode(node, graph, deps, ndeps, &p));
+    return ALB_OK;
+}
+
+// while (!done) { decide; switch { td | prep+td | bu | bu-nobypass }; end }
+alb_status build_loop_graph(alb_graph *g, int block) {
+    loop_cache_free(g);
+    CachedLoop *cl = new CachedLoop();
+    g->loop = cl;
+    cl->block = block;
+    BfsArgs a = make_args(g);
+    const Launch wide = level_launch(g, block);
+    const Launch one{1, 32};
+    ALB_CK(cudaGraphCreate(&cl->graph, 0));
+    cudaGraphConditionalHandle wh;
+    ALB_CK(cudaGraphConditionalHandleCreate(&wh, cl->graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams wp = {cudaGraphNodeTypeConditional};
+    wp.conditional.handle = wh;
+    wp.conditional.type = cudaGraphCondTypeWhile;
+    wp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    ALB_CK(cudaGraphAddNode(&wnode, cl->graph, nullptr, nullptr, 0, &wp));
+    cudaGraph_t body = wp.conditional.phGraph_out[0];
+
+    cudaGraphConditionalHandle sh;
+    ALB_CK(cudaGraphConditionalHandleCreate(&sh, body, 0, cudaGraphCondAssignDefault));
+    int forced = -1;
+    void *dargs[] = {&a, &forced, &sh};
+    cudaGraphNode_t ndecide;
+    ALB_TRY(add_kernel_node(body, &ndecide, nullptr, 0, (void *)k_decide, one, dargs));
+    cudaGraphNodeParams sp = {cudaGraphNodeTypeConditional};
+    sp.conditional.handle = sh;
+    sp.conditional.type = cudaGraphCondTypeSwitch;
+    sp.conditional.size = 4;
+    cudaGraphNode_t nswitch;
+    ALB_CK(cudaGraphAddNode(&nswitch, body, &ndecide, nullptr, 1, &sp));
+    void *aargs[] = {&a};
+    {  // 0: top-down, queue ready
+        cudaGraph_t b0 = sp.conditional.phGraph_out[0];
+        cudaGraphNode_t t, f;
+        ALB_TRY(add_kernel_node(b0, &t, nullptr, 0, (void *)k_td, wide, aargs));
+        ALB_TRY(add_kernel_node(b0, &f, &t, 1, (void *)k_td_finish, wide, aargs));
+    }
+    {  // 1: compaction / clear, then top-down
+        cudaGraph_t b1 = sp.conditional.phGraph_out[1];
+        cudaGraphNode_t pr, t, f;
+        ALB_TRY(add_kernel_node(b1, &pr, nullptr, 0, (void *)k_prep, wide, aargs));
+        ALB_TRY(add_kernel_node(b1, &t, &pr, 1, (void *)k_td, wide, aargs));
+        ALB_TRY(add_kernel_node(b1, &f, &t, 1, (void *)k_td_finish, wide, aargs));
+    }
+    {  // 2: bottom-up with bypass
+        cudaGraphNode_t b;
+        ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[2], &b, nullptr, 0,
+                                (void *)k_bu<true, true>, wide, aargs));
+    }
+    {  // 3: bottom-up without bypass
+        cudaGraphNode_t b;
+        ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[3], &b, nullptr, 0,
+                                (void *)k_bu<false, false>, wide, aargs));
+    }
+    void *eargs[] = {&a, &wh};
+    cudaGraphNode_t nend;
+    ALB_TRY(add_kernel_node(body, &nend, &nswitch, 1, (void *)k_end, one, eargs));
+    ALB_CK(cudaGraphInstantiate(&cl->exec, cl->graph, 0));
+    return ALB_OK;
+}
+
+alb_status run_host_loop(alb_graph *g, const BfsArgs &a, const alb_bfs_opts &o) {
+    const Launch wide = level_launch(g, o.block);
+    cudaStream_t st = g->stream;
+    BfsCtl *h = g->bfs.h_ctl;
+    float mlp[kMlpParams];
+    const bool have_mlp = o.policy == ALB_POLICY_LEARNED && selector_host_params(0, mlp);
+    (void)a;
+    ALB_CK(cudaMemcpyAsync(h, a.ctl, sizeof(BfsCtl), cudaMemcpyDeviceToHost, st));
+    ALB_CK(cudaStreamSynchronize(st));
+    while (!h->done) {
+        int dir;
+        if (have_mlp) {
+            float f[kMlpIn], out[kMlpOut];
+            level_features(*h, f);
+            mlp_forward_host(mlp, f, out);
+            dir = argmin3(out);
+        } else {
+            dir = rule_dir(*h);
+        }
+        k_decide<<<1, 32, 0, st>>>(a, dir, 0);
+        if (dir == ALB_DIR_TOPDOWN) {
+            if (!h->q_valid || h->n_dirty) k_prep<<<wide.grid, wide.block, 0, st>>>(a);
+            k_td<<<wide.grid, wide.block, 0, st>>>(a);
+            k_td_finish<<<wide.grid, wide.block, 0, st>>>(a);
+        } else if (dir == ALB_DIR_BOTTOMUP) {
+            k_bu<true, true><<<wide.grid, wide.block, 0, st>>>(a);
+        } else {
+            k_bu<false, false><<<wide.grid, wide.block, 0, st>>>(a);
+        }
+        k_end<<<1, 32, 0, st>>>(a, 0);
+        ALB_CK(cudaGetLastError());
+        ALB_CK(cudaMemcpyAsync(h, a.ctl, sizeof(BfsCtl), cudaMemcpyDeviceToHost, st));
+        ALB_CK(cudaStreamSynchronize(st));
+    }
+    return ALB_OK;
+}
+
+alb_status run_persistent(alb_graph *g, const BfsArgs &a) {
+    int per_sm = 0;
+    ALB_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persistent, 256, 0));
+    if (per_sm < 1) return fail(ALB_ERR_CUDA, "persistent kernel does not fit on an SM");
+    const unsigned grid = (unsigned)(per_sm * g->num_sms);
+    BfsArgs args = a;
+    void *kargs[] = {&args};
+    ALB_CK(cudaLaunchCooperativeKernel((void *)k_persistent, dim3(grid), dim3(256), kargs, 0,
+                                       g->stream));
+    return ALB_OK;
+}
+
+float skew_feature(const Sell &s, int64_t n) {
+    const double mean = n > 0 ? (double)s.m_in / (double)n : 0.0;
+    return mean > 0 ? (float)std::log2(1.0 + (double)s.max_deg / mean) : 0.0f;
+}
+
+alb_status bfs_impl(alb_graph *g, int32_t root, const alb_bfs_opts &o, int32_t *d_level,
+                    int32_t *d_parent, alb_stats *st) {
+    ALB_TRY(bfs_scratch_alloc(g));
+    const BfsArgs a = make_args(g);
+    const Sell &s = g->sell;
+    cudaStream_t stream = g->stream;
+    InitParams ip;
+    ip.root = root;
+    ip.policy = o.policy;
+    ip.trace_cap = o.trace ? g->bfs.trace_cap : 0;
+    ip.level_cap = (int32_t)std::min<int64_t>(g->n + 1, INT32_MAX - 1);
+    ip.alpha = o.alpha;
+    ip.beta = o.beta;
+    ip.mean_deg = g->n > 0 ? (float)((double)s.m_in / (double)g->n) : 0.f;
+    ip.skew = skew_feature(s, g->n);
+    ip.n_live = g->n - s.zero_in;
+    ip.m_in = s.m_in;
+    ip.active0 = s.active0;
+    const Launch wide = level_launch(g, 256);
+    ALB_CK(cudaEventRecord(g->ev0, stream));
+    k_init_bulk<<<wide.grid, wide.block, 0, stream>>>(a);
+    k_init_root<<<1, 32, 0, stream>>>(a, ip);
+    ALB_CK(cudaGetLastError());
+    if (o.loop == ALB_LOOP_HOST) {
+        ALB_TRY(run_host_loop(g, a, o));
+    } else if (o.loop == ALB_LOOP_PERSISTENT) {
+        ALB_TRY(run_persistent(g, a));
+    } else {
+        if (!g->loop || g->loop->block != o.block) ALB_TRY(build_loop_graph(g, o.block));
+        ALB_CK(cudaGraphLaunch(g->loop->exec, stream));
+    }
+    if (d_level || d_parent) k_scatter<<<wide.grid, wide.block, 0, stream>>>(a, d_level, d_parent);
+    ALB_CK(cudaGetLastError());
+    ALB_CK(cudaEventRecord(g->ev1, stream));
+    ALB_CK(cudaMemcpyAsync(g->bfs.h_ctl, a.ctl, sizeof(BfsCtl), cudaMemcpyDeviceToHost, stream));
+    ALB_CK(cudaStreamSynchronize(stream));
+    const BfsCtl &c = *g->bfs.h_ctl;
+    if (c.err) return fail(c.err, "BFS aborted on the device (code %d)", c.err);
+    if (!c.done) return fail(ALB_ERR_DEVICE, "BFS level loop ended without finishing");
+    float ms = 0;
+    ALB_CK(cudaEventElapsedTime(&ms, g->ev0, g->ev1));
+    g->last_trace_valid = false;
+    if (o.trace) {
+        const int32_t cnt = std::min(c.trace_len, g->bfs.trace_cap);
+        g->last_trace.resize((size_t)cnt);
+        if (cnt)
+            ALB_CK(cudaMemcpy(g->last_trace.data(), g->bfs.trace, sizeof(alb_level_rec) * cnt,
+                              cudaMemcpyDeviceToHost));
+        g->last_trace_valid = true;
+    }
+    if (st) {
+        st->num_levels = c.level;
+        st->levels_topdown = c.levels_td;
+        st->levels_bottomup = c.levels_bu;
+        st->pad_ = 0;
+        st->reached = c.reached;
+        st->edges = c.edges;
+        st->ms = ms;
+    }
+    return ALB_OK;
+}
+
+alb_status check_bfs_args(alb_graph *g, int32_t root, const alb_bfs_opts *o, alb_bfs_opts &out) {
+    if (!g) return fail(ALB_ERR_INVALID, "BFS: graph is NULL");
+    if (!g->sell.built) return fail(ALB_ERR_STATE, "BFS: call alb_sell_build first");
+    if (root < 0 || root >= g->n)
+        return fail(ALB_ERR_INVALID, "BFS: root %d outside [0, %lld)", root, (long long)g->n);
+    alb_bfs_opts_default(&out);
+    if (o) out = *o;
+    if (out.policy < ALB_POLICY_BEAMER || out.policy > ALB_POLICY_BOTTOMUP_NOBYPASS)
+        return fail(ALB_ERR_INVALID, "BFS: unknown policy %d", out.policy);
+    if (out.loop < ALB_LOOP_HOST || out.loop > ALB_LOOP_PERSISTENT)
+        return fail(ALB_ERR_INVALID, "BFS: unknown loop mode %d", out.loop);
+    if (!(out.block == 128 || out.block == 256 || out.block == 512 || out.block == 1024))
+        return fail(ALB_ERR_UNSUPPORTED, "BFS: block must be 128, 256, 512 or 1024");
+    if (!(out.alpha > 0) || !(out.beta > 0))
+        return fail(ALB_ERR_INVALID, "BFS: alpha and beta must be positive");
+    return ALB_OK;
+}
+
+}  // namespace
+}  // namespace alb
+
+using namespace alb;
+
+extern "C" {
+
+void alb_bfs_opts_default(alb_bfs_opts *o) {
+    if (!o) return;
+    o->policy = ALB_POLICY_BEAMER;
+    o->loop = ALB_LOOP_GRAPH;
+    o->alpha = 14.0f;
+    o->beta = 24.0f;
+    o->block = 256;
+    o->trace = 0;
+}
+
+alb_status alb_bfs_device(alb_graph *g, int32_t root, const alb_bfs_opts *o, int32_t *d_level,
+                          int32_t *d_parent, alb_stats *st) {
+    alb_bfs_opts oo;
+    ALB_TRY(check_bfs_args(g, root, o, oo));
+    ALB_CK(cudaSetDevice(g->device));
+    try {
+        return bfs_impl(g, root, oo, d_level, d_parent, st);
+    } catch (const std::bad_alloc &) {
+        return fail(ALB_ERR_OOM, "alb_bfs_device: host allocation failed");
+    }
+}
+
+alb_status alb_bfs(alb_graph *g, int32_t root, const alb_bfs_opts *o, int32_t *level,
+                   int32_t *parent, alb_stats *st) {
+    alb_bfs_opts oo;
+    ALB_TRY(check_bfs_args(g, root, o, oo));
+    ALB_CK(cudaSetDevice(g->device));
+    BfsScratch &b = g->bfs;
+    ALB_TRY(bfs_scratch_alloc(g));
+    if (level && !b.out_level) ALB_TRY(dmalloc((void **)&b.out_level, sizeof(int32_t) * g->n, "level output"));
+    if (parent && !b.out_parent)
+        ALB_TRY(dmalloc((void **)&b.out_parent, sizeof(int32_t) * g->n, "parent output"));
+    alb_status rc;
+    try {
+        rc = bfs_impl(g, root, oo, level ? b.out_level : nullptr, parent ? b.out_parent : nullptr, st);
+    } catch (const std::bad_alloc &) {
+        rc = fail(ALB_ERR_OOM, "alb_bfs: host allocation failed");
+    }
+    if (rc != ALB_OK) return rc;
+    if (level)
+        ALB_CK(cudaMemcpyAsync(level, b.out_level, sizeof(int32_t) * g->n, cudaMemcpyDeviceToHost, g->stream));
+    if (parent)
+        ALB_CK(cudaMemcpyAsync(parent, b.out_parent, sizeof(int32_t) * g->n, cudaMemcpyDeviceToHost,
+                               g->stream));
+    ALB_CK(cudaStreamSynchronize(g->stream));
+    return ALB_OK;
+}
+
+alb_status alb_level_trace(const alb_graph *g, int32_t cap, alb_level_rec *out, int32_t *count) {
+    if (!g || !count || (cap > 0 && !out)) return fail(ALB_ERR_INVALID, "alb_level_trace: bad arguments");
+    if (!g->last_trace_valid) return fail(ALB_ERR_STATE, "alb_level_trace: last BFS ran without trace");
+    const int32_t n = (int32_t)g->last_trace.size();
+    *count = n;
+    const int32_t k = std::min(n, std::max(cap, 0));
+    if (k) std::memcpy(out, g->last_trace.data(), sizeof(alb_level_rec) * k);
+    return ALB_OK;
+}
+
+}  // extern "C"

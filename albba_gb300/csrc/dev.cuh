@@ -1,0 +1,143 @@
+// Device-side types and helpers shared by the CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "albba.h"
+
+namespace alb {
+
+constexpr uint32_t kFull = 0xFFFFFFFFu;
+
+// ---------------------------------------------------------------- loads
+// Column and structure arrays are read-only for a whole traversal: read them
+// through the non-coherent path. Bitmaps and queues are rewritten between
+// levels; inside the persistent kernel they must be read with ordinary
+// (L1-coherent after the grid barrier's fence) loads, never .nc.
+__device__ __forceinline__ int4 ld_nc(const int4 *p) {
+    int4 r;
+    asm volatile("ld.global.nc.L1::no_allocate.v4.s32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+                 : "l"(p));
+    return r;
+}
+template <class T>
+__device__ __forceinline__ T ld_ro(const T *p) { return __ldg(p); }
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    return v;
+}
+
+template <class T>
+__device__ __forceinline__ T warp_inclusive_scan(T v) {
+    const unsigned lane = lane_id();
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        T t = __shfl_up_sync(kFull, v, o);
+        if (lane >= (unsigned)o) v += t;
+    }
+    return v;
+}
+
+// ----------------------------------------------------------- level control
+// Counters produced while traversing level L (they describe level L+1) live
+// in slot (L+1) % 3. All readers of slot k finish before slot k is zeroed
+// again two levels later, so the persistent kernel needs no extra barrier
+// for the rollover.
+struct BfsCtl {
+    int32_t level;    // depth of the current frontier
+    int32_t dir;      // ALB_DIR_* chosen for the current level
+    int32_t prev_dir; // direction of the previous level (-1 at level 0)
+    int32_t q_valid;  // queue[level & 1] lists the current frontier
+    int32_t n_dirty;  // bitmap[(level + 1) & 1] may hold stale bits
+    int32_t done;
+    int32_t err;      // ALB_ERR_* raised on the device (0 = none)
+    int32_t policy;
+    float alpha, beta;
+    int32_t levels_td, levels_bu;
+    int64_t n;               // vertices
+    int64_t nwords;          // 32-bit words per bitmap
+    int64_t nf, mf;          // current frontier: vertices, push-side entries
+    int64_t prev_nf;
+    int64_t nu, mu;          // unvisited vertices / pull-side entries
+    int64_t active_words;    // bitmap words with an unvisited row
+    int64_t reached, edges;  // running totals
+    unsigned long long acc_n[3], acc_mo[3], acc_mi[3], acc_full[3], qn[3];
+    unsigned int bar_count, bar_gen;  // persistent-kernel grid barrier
+    int32_t trace_cap, trace_len;
+    int32_t level_cap;       // safety bound on the number of levels
+    int32_t pad_;
+    float feat_mean_deg, feat_skew;  // static selector features
+};
+
+// Per-traversal device arguments (passed by value to every kernel).
+struct BfsArgs {
+    int64_t n, nslices, nwords;
+    int32_t C, log2C;
+    const int32_t *perm;       // position -> original id
+    const int32_t *inv;        // original id -> position
+    const int32_t *ideg;       // pull-side row length by position
+    const int32_t *odeg;       // push-side row length by position
+    const int32_t *width;      // slice width (max row length)
+    const int64_t *slice_off;  // slice start, int32 entries
+    const int4 *col4;          // SELL columns, 4-interleaved
+    const int64_t *prow;       // push CSR (position space)
+    const int32_t *pcol;
+    const uint32_t *vinit;     // initial visited mask
+    uint32_t *bm0, *bm1;       // frontier bitmaps (by level parity)
+    uint32_t *vis;             // visited bitmap
+    int32_t *q0, *q1;          // frontier queues (by level parity)
+    int32_t *level_pos;        // depth by position
+    uint32_t *parent_pos;      // parent original id by position
+    BfsCtl *ctl;
+    alb_level_rec *trace;
+    const float *mlp;          // selector parameters or null
+};
+
+// Shared by host and device: pick the direction for the current level.
+__host__ __device__ inline int beamer_dir(const BfsCtl &c) {
+    if (c.prev_dir < 0 || c.prev_dir == ALB_DIR_TOPDOWN) {
+        // top-down -> bottom-up when the frontier's edges exceed m_u / alpha
+        return ((double)c.mf > (double)c.mu / (double)c.alpha) ? ALB_DIR_BOTTOMUP
+                                                               : ALB_DIR_TOPDOWN;
+    }
+    // stay bottom-up while the frontier grows or is large
+    bool stay = (c.nf >= c.prev_nf) || ((double)c.nf > (double)c.n / (double)c.beta);
+    return stay ? ALB_DIR_BOTTOMUP : ALB_DIR_TOPDOWN;
+}
+
+__host__ __device__ inline int rule_dir(const BfsCtl &c) {
+    switch (c.policy) {
+        case ALB_POLICY_TOPDOWN:
+            return ALB_DIR_TOPDOWN;
+        case ALB_POLICY_BOTTOMUP:
+            return c.level == 0 ? ALB_DIR_TOPDOWN : ALB_DIR_BOTTOMUP;
+        case ALB_POLICY_BOTTOMUP_NOBYPASS:
+            return c.level == 0 ? ALB_DIR_TOPDOWN : ALB_DIR_BOTTOMUP_NOBYPASS;
+        case ALB_POLICY_REF004: {
+            // SWITCH = (int)(nrows * 0.04); pull when nnzx > SWITCH
+            int64_t thr = (int64_t)((double)c.n * 0.04);
+            return c.nf > thr ? ALB_DIR_BOTTOMUP : ALB_DIR_TOPDOWN;
+        }
+        default:
+            return beamer_dir(c);
+    }
+}
+
+}  // namespace alb

@@ -1,0 +1,605 @@
+// Graph upload and the device SELL-C-sigma builder.
+//
+// Reference counterparts: the CSR container and its int32 limits
+// (bfs/src/sparse_matrix.h:18-29), the transpose done before the BFS
+// (bfs/src/main.c:117-126, bfs/src/sparse_matrix.c:230-290), and the SELL
+// pre-processing (bfs/src/bfs_SELLCSv2.c:34-59): row lengths
+// (bfs/src/utils.c:111-124), stable descending sort inside sigma windows
+// (bfs/src/sorting_utils.c:173-253), slice widths and the padded fill
+// (bfs/src/sparse_matrix.c:435-521).
+//
+// GB300 layout, all in sorted-position space (position p holds original row
+// perm[p]; neighbour ids are stored as positions):
+//   slice s = rows [s*C, s*C+C); width[s] = longest row; w4 = width rounded
+//   up to 4; col[slice_off[s] + (k/4)*4*C + r*4 + k%4] = k-th neighbour of
+//   row s*C+r, padded with the row's own position. A warp reading group
+//   k/4 of a C=32 slice issues one fully coalesced 512-byte int4 load.
+//   Self-loops are dropped, so the padding value doubles as an end marker.
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "graph.h"
+#include "scan.cuh"
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace alb {
+
+alb_status dmalloc(void **p, size_t bytes, const char *what) {
+    *p = nullptr;
+    if (injected_alloc_failure())
+        return fail(ALB_ERR_OOM, "device allocation of %zu bytes for %s failed (injected)", bytes,
+                    what);
+    cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        if (e == cudaErrorMemoryAllocation)
+            return fail(ALB_ERR_OOM, "device allocation of %zu bytes for %s failed", bytes, what);
+        return fail(ALB_ERR_CUDA, "cudaMalloc for %s: %s", what, cudaGetErrorString(e));
+    }
+    return ALB_OK;
+}
+
+void dfree(void *p) {
+    if (p) cudaFree(p);
+}
+
+namespace {
+
+// ------------------------------------------------------------ host prep
+
+bool rows_sorted(int64_t n, const int64_t *rp, const int32_t *col) {
+    int bad = 0;
+#pragma omp parallel for schedule(dynamic, 4096) reduction(| : bad)
+    for (int64_t r = 0; r < n; r++)
+        for (int64_t e = rp[r] + 1; e < rp[r + 1]; e++)
+            if (col[e - 1] > col[e]) {
+                bad = 1;
+                break;
+            }
+    return !bad;
+}
+
+alb_status validate_csr(int64_t n, const int64_t *rp, const int32_t *col) {
+    if (rp[0] != 0) return fail(ALB_ERR_INVALID, "rowptr[0] must be 0");
+    int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+    for (int64_t r = 0; r < n; r++)
+        if (rp[r + 1] < rp[r]) bad |= 1;
+    if (bad) return fail(ALB_ERR_INVALID, "rowptr must be non-decreasing");
+    const int64_t nnz = rp[n];
+#pragma omp parallel for schedule(static) reduction(| : bad)
+    for (int64_t e = 0; e < nnz; e++)
+        if (col[e] < 0 || col[e] >= n) bad |= 1;
+    if (bad) return fail(ALB_ERR_INVALID, "column index outside [0, n)");
+    return ALB_OK;
+}
+
+// Copy of a CSR with every row sorted ascending.
+void sorted_copy(int64_t n, const int64_t *rp, const int32_t *col, std::vector<int32_t> &out) {
+    out.assign(col, col + rp[n]);
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t r = 0; r < n; r++) std::sort(out.begin() + rp[r], out.begin() + rp[r + 1]);
+}
+
+// Transpose by counting; iterating source rows in order leaves every
+// transposed row ascending.
+void transpose(int64_t n, const int64_t *rp, const int32_t *col, std::vector<int64_t> &trp,
+               std::vector<int32_t> &tcol) {
+    const int64_t nnz = rp[n];
+    trp.assign((size_t)n + 1, 0);
+    for (int64_t e = 0; e < nnz; e++) trp[(size_t)col[e] + 1]++;
+    for (int64_t i = 0; i < n; i++) trp[i + 1] += trp[i];
+    std::vector<int64_t> cur(trp.begin(), trp.end() - 1);
+    tcol.resize((size_t)nnz);
+    for (int64_t r = 0; r < n; r++)
+        for (int64_t e = rp[r]; e < rp[r + 1]; e++) tcol[cur[col[e]]++] = (int32_t)r;
+}
+
+alb_status upload(int64_t n, const int64_t *rp, const int32_t *col, int64_t **d_rp,
+                  int32_t **d_col, cudaStream_t st) {
+    ALB_TRY(dmalloc((void **)d_rp, sizeof(int64_t) * (size_t)(n + 1), "row offsets"));
+    ALB_TRY(dmalloc((void **)d_col, sizeof(int32_t) * (size_t)rp[n], "columns"));
+    ALB_CK(cudaMemcpyAsync(*d_rp, rp, sizeof(int64_t) * (size_t)(n + 1), cudaMemcpyHostToDevice, st));
+    ALB_CK(cudaMemcpyAsync(*d_col, col, sizeof(int32_t) * (size_t)rp[n], cudaMemcpyHostToDevice, st));
+    return ALB_OK;
+}
+
+void free_sell(Sell &s) {
+    dfree(s.perm);
+    dfree(s.inv);
+    dfree(s.ideg);
+    dfree(s.odeg);
+    dfree(s.width);
+    dfree(s.slice_off);
+    dfree(s.col);
+    dfree(s.prow);
+    dfree(s.pcol);
+    dfree(s.vinit);
+    s = Sell();
+}
+
+alb_status create_impl(int64_t n, const int64_t *rowptr, const int32_t *col, uint32_t flags,
+                       alb_graph **out) {
+    ALB_TRY(validate_csr(n, rowptr, col));
+    int dev = 0;
+    ALB_CK(cudaGetDevice(&dev));
+    alb_graph *g = new alb_graph();
+    g->device = dev;
+    g->n = n;
+    auto cleanup = [&](alb_status s) {
+        alb_graph_destroy(g);
+        return s;
+    };
+    cudaError_t e = cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&g->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&g->ev1);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return cleanup(fail(ALB_ERR_CUDA, "stream/event setup: %s", cudaGetErrorString(e)));
+    }
+    const bool sorted = (flags & ALB_CSR_SORTED) || rows_sorted(n, rowptr, col);
+    std::vector<int32_t> scol;
+    const int32_t *given = col;
+    if (!sorted) {
+        sorted_copy(n, rowptr, col, scol);
+        given = scol.data();
+    }
+    alb_status st = ALB_OK;
+    if (flags & ALB_CSR_SYMMETRIC) {
+        g->symmetric = true;
+        st = upload(n, rowptr, given, &g->rp_in, &g->col_in, g->stream);
+        g->rp_out = g->rp_in;
+        g->col_out = g->col_in;
+        g->nnz_in = g->nnz_out = rowptr[n];
+    } else {
+        std::vector<int64_t> trp;
+        std::vector<int32_t> tcol;
+        transpose(n, rowptr, given, trp, tcol);
+        const bool given_is_in = (flags & ALB_CSR_IN) != 0;
+        const int64_t *rin = given_is_in ? rowptr : trp.data();
+        const int32_t *cin = given_is_in ? given : tcol.data();
+        const int64_t *rout = given_is_in ? trp.data() : rowptr;
+        const int32_t *cout = given_is_in ? tcol.data() : given;
+        st = upload(n, rin, cin, &g->rp_in, &g->col_in, g->stream);
+        if (st == ALB_OK) st = upload(n, rout, cout, &g->rp_out, &g->col_out, g->stream);
+        g->nnz_in = g->nnz_out = rowptr[n];
+        if (st == ALB_OK) {
+            // host vectors die at scope exit: finish the copies first
+            cudaError_t se = cudaStreamSynchronize(g->stream);
+            if (se != cudaSuccess)
+                st = fail(ALB_ERR_CUDA, "upload: %s", cudaGetErrorString(se));
+        }
+    }
+    if (st == ALB_OK) {
+        cudaError_t se = cudaStreamSynchronize(g->stream);
+        if (se != cudaSuccess) st = fail(ALB_ERR_CUDA, "upload: %s", cudaGetErrorString(se));
+    }
+    if (st != ALB_OK) return cleanup(st);
+    *out = g;
+    return ALB_OK;
+}
+
+// --------------------------------------------------------- device kernels
+
+// Row lengths without self-loops, for both sides.
+__global__ void k_row_lengths(int64_t n, const int64_t *rp, const int32_t *col, int32_t *len,
+                              int32_t *max_len) {
+    int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int32_t l = 0;
+    if (v < n) {
+        int64_t b = rp[v], e = rp[v + 1];
+        int32_t self = 0;
+        for (int64_t i = b; i < e; i++) self += (col[i] == (int32_t)v);
+        l = (int32_t)(e - b) - self;
+        len[v] = l;
+    }
+    l = __reduce_max_sync(kFull, l);
+    if ((threadIdx.x & 31) == 0 && l > 0) atomicMax(max_len, l);
+}
+
+// Stable descending sort of row lengths inside one sigma window per CTA:
+// LSD radix sort with 4-bit digits (the digit size of
+// bfs/src/sorting_utils.c:26-28), each pass a counting sort over
+// (digit, thread) buckets so equal digits keep their order.
+// Shared memory: key[sigma] int32, idx[2][sigma] uint16, cnt[16*TPB] int32.
+__global__ void k_window_sort(int64_t n, int32_t sigma, int32_t items, const int32_t *len,
+                              int32_t *perm) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int tpb = blockDim.x, t = threadIdx.x;
+    int32_t *key = (int32_t *)smem;
+    int32_t *cnt = key + sigma;
+    uint16_t *ia = (uint16_t *)(cnt + 16 * tpb);
+    uint16_t *ib = ia + sigma;
+    __shared__ int32_t s_max, s_wsum[32];
+    const int64_t wbase = (int64_t)blockIdx.x * sigma;
+    const int32_t wlen = (int32_t)min((int64_t)sigma, n - wbase);
+    if (t == 0) s_max = 0;
+    __syncthreads();
+    int32_t lmax = 0;
+    for (int32_t i = t; i < wlen; i += tpb) {
+        int32_t k = len[wbase + i];
+        key[i] = k;
+        ia[i] = (uint16_t)i;
+        lmax = max(lmax, k);
+    }
+    atomicMax(&s_max, lmax);
+    __syncthreads();
+    int32_t passes = 0;
+    for (uint32_t m = (uint32_t)s_max; m; m >>= 4) passes++;
+    const int32_t lo = t * items, hi = min(lo + items, wlen);
+    for (int32_t pass = 0; pass < passes; pass++) {
+        const int shift = 4 * pass;
+        int32_t c[16];
+#pragma unroll
+        for (int b = 0; b < 16; b++) c[b] = 0;
+        for (int32_t i = lo; i < hi; i++) {
+            int d = 15 - ((key[ia[i]] >> shift) & 15);  // descending
+#pragma unroll
+            for (int b = 0; b < 16; b++) c[b] += (b == d);
+        }
+#pragma unroll
+        for (int b = 0; b < 16; b++) cnt[b * tpb + t] = c[b];
+        __syncthreads();
+        // exclusive scan of cnt[0 .. 16*tpb): thread t owns entries [16t, 16t+16)
+        int32_t run = 0;
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+            int32_t v = cnt[16 * t + j];
+            cnt[16 * t + j] = run;
+            run += v;
+        }
+        int32_t inc = warp_inclusive_scan(run);
+        if ((t & 31) == 31) s_wsum[t >> 5] = inc;
+        __syncthreads();
+        if (t < 32) {
+            int32_t v = (t < (tpb >> 5)) ? s_wsum[t] : 0;
+            int32_t vi = warp_inclusive_scan(v);
+            if (t < (tpb >> 5)) s_wsum[t] = vi - v;
+        }
+        __syncthreads();
+        const int32_t add = s_wsum[t >> 5] + inc - run;
+#pragma unroll
+        for (int j = 0; j < 16; j++) cnt[16 * t + j] += add;
+        __syncthreads();
+#pragma unroll
+        for (int b = 0; b < 16; b++) c[b] = cnt[b * tpb + t];
+        for (int32_t i = lo; i < hi; i++) {
+            uint16_t id = ia[i];
+            int d = 15 - ((key[id] >> shift) & 15);
+            int32_t at = 0;
+#pragma unroll
+            for (int b = 0; b < 16; b++)
+                if (b == d) at = c[b]++;
+            ib[at] = id;
+        }
+        __syncthreads();
+        uint16_t *tmp = ia;
+        ia = ib;
+        ib = tmp;
+    }
+    for (int32_t i = t; i < wlen; i += tpb) perm[wbase + i] = (int32_t)(wbase + ia[i]);
+}
+
+__global__ void k_identity(int64_t n, int32_t *perm) {
+    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p < n) perm[p] = (int32_t)p;
+}
+
+// inv, and per-position degrees.
+__global__ void k_positions(int64_t n, const int32_t *perm, const int32_t *ilen,
+                            const int32_t *olen, int32_t *inv, int32_t *ideg, int32_t *odeg) {
+    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    int32_t v = perm[p];
+    inv[v] = (int32_t)p;
+    ideg[p] = ilen[v];
+    odeg[p] = olen[v];
+}
+
+// width[s] and the padded slice size C * w4 (int64) for the scan.
+__global__ void k_widths(int64_t n, int64_t nslices, int32_t C, const int32_t *ideg,
+                         int32_t *width, int64_t *ssize) {
+    int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= nslices) return;
+    int32_t w = 0;
+    for (int32_t r = 0; r < C; r++) {
+        int64_t p = s * C + r;
+        if (p < n) w = max(w, ideg[p]);
+    }
+    width[s] = w;
+    ssize[s] = (int64_t)C * ((w + 3) & ~3);
+}
+
+// Fill the 4-interleaved SELL columns, one thread per (padded) row.
+__global__ void k_fill_sell(int64_t n, int64_t npad, int32_t C, int32_t log2C,
+                            const int32_t *perm, const int32_t *inv, const int32_t *width,
+                            const int64_t *slice_off, const int64_t *rp, const int32_t *col,
+                            int32_t *scol) {
+    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= npad) return;
+    const int64_t s = p >> log2C;
+    const int32_t r = (int32_t)(p & (C - 1));
+    const int32_t w4 = (width[s] + 3) & ~3;
+    int32_t *base = scol + slice_off[s] + r * 4;
+    int32_t k = 0;
+    if (p < n) {
+        const int32_t v = perm[p];
+        for (int64_t e = rp[v]; e < rp[v + 1]; e++) {
+            int32_t c = col[e];
+            if (c == v) continue;
+            base[(int64_t)(k >> 2) * 4 * C + (k & 3)] = inv[c];
+            k++;
+        }
+    }
+    const int32_t pad = p < n ? (int32_t)p : 0;
+    for (; k < w4; k++) base[(int64_t)(k >> 2) * 4 * C + (k & 3)] = pad;
+}
+
+// Push-side CSR in position space.
+__global__ void k_fill_push(int64_t n, const int32_t *perm, const int32_t *inv,
+                            const int64_t *prow, const int64_t *rp, const int32_t *col,
+                            int32_t *pcol) {
+    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int32_t v = perm[p];
+    int64_t at = prow[p];
+    for (int64_t e = rp[v]; e < rp[v + 1]; e++) {
+        int32_t c = col[e];
+        if (c != v) pcol[at++] = inv[c];
+    }
+}
+
+// Initial visited mask: padded tail rows and rows without sources can never
+// be discovered by a pull, so they start visited (their level stays -1).
+__global__ void k_vinit(int64_t n, int64_t nwords, const int32_t *ideg, uint32_t *vinit,
+                        unsigned long long *counters) {
+    int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (w >= nwords) return;
+    uint32_t m = 0;
+    int32_t z = 0;
+    unsigned long long sum = 0;
+    for (int b = 0; b < 32; b++) {
+        int64_t p = w * 32 + b;
+        if (p >= n) {
+            m |= 1u << b;
+        } else {
+            int32_t d = ideg[p];
+            sum += (unsigned long long)d;
+            if (d == 0) {
+                m |= 1u << b;
+                z++;
+            }
+        }
+    }
+    vinit[w] = m;
+    if (m != kFull) atomicAdd(&counters[0], 1ull);  // active words
+    if (z) atomicAdd(&counters[1], (unsigned long long)z);  // rows without sources
+    if (sum) atomicAdd(&counters[2], sum);  // pull-side entries
+}
+
+inline unsigned grid_for(int64_t count, int tpb) { return (unsigned)((count + tpb - 1) / tpb); }
+
+alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma) {
+    const int64_t n = g->n;
+    cudaStream_t st = g->stream;
+    free_sell(g->sell);
+    loop_cache_free(g);
+    bfs_scratch_free(g);  // bitmap sizes depend on C
+    Sell &s = g->sell;
+    s.C = C;
+    s.log2C = C == 8 ? 3 : C == 16 ? 4 : C == 32 ? 5 : 6;
+    s.sigma = sigma;
+    s.nslices = (n + C - 1) / C;
+    const int64_t npad = s.nslices * C;
+    s.nwords = (npad + 31) / 32;
+    int32_t *ilen = nullptr, *olen = nullptr, *dmax = nullptr;
+    int64_t *ssize = nullptr;
+    unsigned long long *dcnt = nullptr;
+    auto tmp_free = [&]() {
+        dfree(ilen);
+        dfree(olen);
+        dfree(dmax);
+        dfree(ssize);
+        dfree(dcnt);
+    };
+    alb_status rc = [&]() -> alb_status {
+        ALB_TRY(dmalloc((void **)&ilen, sizeof(int32_t) * n, "row lengths"));
+        ALB_TRY(dmalloc((void **)&olen, sizeof(int32_t) * n, "row lengths"));
+        ALB_TRY(dmalloc((void **)&dmax, sizeof(int32_t) * 2, "max length"));
+        ALB_TRY(dmalloc((void **)&dcnt, sizeof(unsigned long long) * 3, "counters"));
+        ALB_TRY(dmalloc((void **)&s.perm, sizeof(int32_t) * n, "perm"));
+        ALB_TRY(dmalloc((void **)&s.inv, sizeof(int32_t) * n, "inv"));
+        ALB_TRY(dmalloc((void **)&s.ideg, sizeof(int32_t) * n, "ideg"));
+        ALB_TRY(dmalloc((void **)&s.odeg, sizeof(int32_t) * n, "odeg"));
+        ALB_TRY(dmalloc((void **)&s.width, sizeof(int32_t) * s.nslices, "width"));
+        ALB_TRY(dmalloc((void **)&s.slice_off, sizeof(int64_t) * (s.nslices + 1), "slice_off"));
+        ALB_TRY(dmalloc((void **)&ssize, sizeof(int64_t) * (s.nslices + 1), "slice sizes"));
+        ALB_TRY(dmalloc((void **)&s.prow, sizeof(int64_t) * (n + 1), "push offsets"));
+        ALB_TRY(dmalloc((void **)&s.vinit, sizeof(uint32_t) * s.nwords, "vinit"));
+        ALB_CK(cudaMemsetAsync(dmax, 0, sizeof(int32_t) * 2, st));
+        ALB_CK(cudaMemsetAsync(dcnt, 0, sizeof(unsigned long long) * 3, st));
+        const int T = 256;
+        k_row_lengths<<<grid_for(n, T), T, 0, st>>>(n, g->rp_in, g->col_in, ilen, dmax);
+        if (g->symmetric)
+            ALB_CK(cudaMemcpyAsync(olen, ilen, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, st));
+        else
+            k_row_lengths<<<grid_for(n, T), T, 0, st>>>(n, g->rp_out, g->col_out, olen, dmax + 1);
+        ALB_CK(cudaGetLastError());
+        if (sigma <= 1) {
+            k_identity<<<grid_for(n, T), T, 0, st>>>(n, s.perm);
+        } else {
+            int tpb = std::min(1024, std::max(32, ((sigma / 16 + 31) / 32) * 32));
+            int items = (sigma + tpb - 1) / tpb;
+            size_t sm = sizeof(int32_t) * sigma + sizeof(int32_t) * 16 * tpb +
+                        2 * sizeof(uint16_t) * sigma;
+            ALB_CK(cudaFuncSetAttribute(k_window_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)sm));
+            unsigned nwin = (unsigned)((n + sigma - 1) / sigma);
+            k_window_sort<<<nwin, tpb, sm, st>>>(n, sigma, items, ilen, s.perm);
+        }
+        ALB_CK(cudaGetLastError());
+        k_positions<<<grid_for(n, T), T, 0, st>>>(n, s.perm, ilen, olen, s.inv, s.ideg, s.odeg);
+        k_widths<<<grid_for(s.nslices, T), T, 0, st>>>(n, s.nslices, C, s.ideg, s.width, ssize);
+        ALB_CK(cudaGetLastError());
+        ALB_TRY(exclusive_scan(ssize, s.slice_off, s.nslices, st));
+        ALB_TRY(exclusive_scan(s.odeg, s.prow, n, st));
+        int64_t hsz[2] = {0, 0};
+        ALB_CK(cudaMemcpyAsync(&hsz[0], s.slice_off + s.nslices, sizeof(int64_t),
+                               cudaMemcpyDeviceToHost, st));
+        ALB_CK(cudaMemcpyAsync(&hsz[1], s.prow + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        int32_t hmax[2] = {0, 0};
+        ALB_CK(cudaMemcpyAsync(hmax, dmax, sizeof(hmax), cudaMemcpyDeviceToHost, st));
+        ALB_CK(cudaStreamSynchronize(st));
+        s.ncol = hsz[0];
+        s.m_out = hsz[1];
+        s.max_deg = std::max(hmax[0], hmax[1]);
+        ALB_TRY(dmalloc((void **)&s.col, sizeof(int32_t) * (size_t)std::max<int64_t>(s.ncol, 4),
+                        "SELL columns"));
+        ALB_TRY(dmalloc((void **)&s.pcol, sizeof(int32_t) * (size_t)std::max<int64_t>(s.m_out, 1),
+                        "push columns"));
+        k_fill_sell<<<grid_for(npad, T), T, 0, st>>>(n, npad, C, s.log2C, s.perm, s.inv, s.width,
+                                                     s.slice_off, g->rp_in, g->col_in, s.col);
+        k_fill_push<<<grid_for(n, T), T, 0, st>>>(n, s.perm, s.inv, s.prow, g->rp_out, g->col_out,
+                                                  s.pcol);
+        k_vinit<<<grid_for(s.nwords, T), T, 0, st>>>(n, s.nwords, s.ideg, s.vinit, dcnt);
+        ALB_CK(cudaGetLastError());
+        unsigned long long hc[3];
+        ALB_CK(cudaMemcpyAsync(hc, dcnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
+        ALB_CK(cudaStreamSynchronize(st));
+        s.active0 = (int64_t)hc[0];
+        s.zero_in = (int64_t)hc[1];
+        s.m_in = (int64_t)hc[2];
+        return ALB_OK;
+    }();
+    tmp_free();
+    if (rc != ALB_OK) {
+        free_sell(g->sell);
+        return rc;
+    }
+    s.built = true;
+    return ALB_OK;
+}
+
+}  // namespace
+}  // namespace alb
+
+using namespace alb;
+
+extern "C" {
+
+alb_status alb_graph_create(int64_t n, const int64_t *rowptr, const int32_t *col, uint32_t flags,
+                            alb_graph **out) {
+    if (!out) return fail(ALB_ERR_INVALID, "alb_graph_create: out is NULL");
+    *out = nullptr;
+    if (n <= 0 || n > INT32_MAX || !rowptr || (!col && rowptr[n] > 0))
+        return fail(ALB_ERR_INVALID, "alb_graph_create: bad arguments (n=%lld)", (long long)n);
+    try {
+        return create_impl(n, rowptr, col, flags, out);
+    } catch (const std::bad_alloc &) {
+        return fail(ALB_ERR_OOM, "alb_graph_create: host allocation failed");
+    }
+}
+
+alb_status alb_graph_create32(int32_t n, const int32_t *rowptr, const int32_t *col,
+                              uint32_t flags, alb_graph **out) {
+    if (!out) return fail(ALB_ERR_INVALID, "alb_graph_create32: out is NULL");
+    *out = nullptr;
+    if (n <= 0 || !rowptr) return fail(ALB_ERR_INVALID, "alb_graph_create32: bad arguments");
+    try {
+        std::vector<int64_t> rp((size_t)n + 1);
+        for (int64_t i = 0; i <= n; i++) rp[i] = rowptr[i];
+        if (!col && rp[n] > 0) return fail(ALB_ERR_INVALID, "alb_graph_create32: col is NULL");
+        return create_impl(n, rp.data(), col, flags, out);
+    } catch (const std::bad_alloc &) {
+        return fail(ALB_ERR_OOM, "alb_graph_create32: host allocation failed");
+    }
+}
+
+void alb_graph_destroy(alb_graph *g) {
+    if (!g) return;
+    int prev = -1;
+    cudaGetDevice(&prev);
+    cudaSetDevice(g->device);
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    loop_cache_free(g);
+    bfs_scratch_free(g);
+    free_sell(g->sell);
+    if (g->col_out != g->col_in) dfree(g->col_out);
+    if (g->rp_out != g->rp_in) dfree(g->rp_out);
+    dfree(g->col_in);
+    dfree(g->rp_in);
+    if (g->ev0) cudaEventDestroy(g->ev0);
+    if (g->ev1) cudaEventDestroy(g->ev1);
+    if (g->stream) cudaStreamDestroy(g->stream);
+    cudaGetLastError();
+    if (prev >= 0) cudaSetDevice(prev);
+    delete g;
+}
+
+alb_status alb_graph_info(const alb_graph *g, int64_t *n, int64_t *nnz) {
+    if (!g) return fail(ALB_ERR_INVALID, "alb_graph_info: graph is NULL");
+    if (n) *n = g->n;
+    if (nnz) *nnz = g->nnz_in;
+    return ALB_OK;
+}
+
+void alb_sell_opts_default(alb_sell_opts *o) {
+    if (!o) return;
+    o->C = 32;
+    o->sigma = 1024;
+}
+
+alb_status alb_sell_build(alb_graph *g, const alb_sell_opts *o, double *ms) {
+    if (!g) return fail(ALB_ERR_INVALID, "alb_sell_build: graph is NULL");
+    alb_sell_opts d;
+    alb_sell_opts_default(&d);
+    if (!o) o = &d;
+    if (!(o->C == 8 || o->C == 16 || o->C == 32 || o->C == 64))
+        return fail(ALB_ERR_UNSUPPORTED, "alb_sell_build: C must be 8, 16, 32 or 64 (got %d)", o->C);
+    if (o->sigma < 1 || o->sigma > 16384)
+        return fail(ALB_ERR_UNSUPPORTED, "alb_sell_build: sigma must be in [1, 16384] (got %d)",
+                    o->sigma);
+    ALB_CK(cudaSetDevice(g->device));
+    ALB_CK(cudaEventRecord(g->ev0, g->stream));
+    alb_status rc;
+    try {
+        rc = sell_build_impl(g, o->C, o->sigma);
+    } catch (const std::bad_alloc &) {
+        rc = fail(ALB_ERR_OOM, "alb_sell_build: host allocation failed");
+    }
+    if (rc != ALB_OK) return rc;
+    ALB_CK(cudaEventRecord(g->ev1, g->stream));
+    ALB_CK(cudaEventSynchronize(g->ev1));
+    if (ms) {
+        float f = 0;
+        ALB_CK(cudaEventElapsedTime(&f, g->ev0, g->ev1));
+        *ms = f;
+    }
+    return ALB_OK;
+}
+
+alb_status alb_sell_export(const alb_graph *g, int64_t *nslices, int32_t *perm, int32_t *width,
+                           int64_t *slice_off, int32_t *col) {
+    if (!g) return fail(ALB_ERR_INVALID, "alb_sell_export: graph is NULL");
+    if (!g->sell.built) return fail(ALB_ERR_STATE, "alb_sell_export: SELL not built");
+    const Sell &s = g->sell;
+    ALB_CK(cudaSetDevice(g->device));
+    if (nslices) *nslices = s.nslices;
+    if (perm) ALB_CK(cudaMemcpy(perm, s.perm, sizeof(int32_t) * g->n, cudaMemcpyDeviceToHost));
+    if (width)
+        ALB_CK(cudaMemcpy(width, s.width, sizeof(int32_t) * s.nslices, cudaMemcpyDeviceToHost));
+    if (slice_off)
+        ALB_CK(cudaMemcpy(slice_off, s.slice_off, sizeof(int64_t) * (s.nslices + 1),
+                          cudaMemcpyDeviceToHost));
+    if (col) ALB_CK(cudaMemcpy(col, s.col, sizeof(int32_t) * s.ncol, cudaMemcpyDeviceToHost));
+    return ALB_OK;
+}
+
+}  // extern "C"

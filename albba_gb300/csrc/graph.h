@@ -1,0 +1,94 @@
+// The device-resident graph behind the opaque alb_graph handle.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <vector>
+
+#include "albba.h"
+#include "dev.cuh"
+#include "internal.h"
+
+namespace alb {
+
+// Device allocation with host fault injection; returns ALB_OK or ALB_ERR_OOM.
+alb_status dmalloc(void **p, size_t bytes, const char *what);
+void dfree(void *p);
+
+// CUDA error check that records the failing call and returns ALB_ERR_CUDA.
+#define ALB_CK(call)                                                                 \
+    do {                                                                             \
+        cudaError_t e_ = (call);                                                     \
+        if (e_ != cudaSuccess) {                                                     \
+            cudaGetLastError();                                                      \
+            return ::alb::fail(ALB_ERR_CUDA, "%s failed: %s (%s:%d)", #call,        \
+                               cudaGetErrorString(e_), __FILE__, __LINE__);          \
+        }                                                                            \
+    } while (0)
+
+#define ALB_TRY(expr)                        \
+    do {                                     \
+        alb_status s_ = (expr);              \
+        if (s_ != ALB_OK) return s_;         \
+    } while (0)
+
+struct CachedLoop;  // CUDA graph for the device-driven level loop (bfs.cu)
+
+struct Sell {
+    bool built = false;
+    int32_t C = 32, log2C = 5, sigma = 1024;
+    int64_t nslices = 0, nwords = 0, ncol = 0;
+    int32_t *perm = nullptr, *inv = nullptr, *ideg = nullptr, *odeg = nullptr;
+    int32_t *width = nullptr;
+    int64_t *slice_off = nullptr;
+    int32_t *col = nullptr;
+    int64_t *prow = nullptr;
+    int32_t *pcol = nullptr;
+    uint32_t *vinit = nullptr;
+    int64_t m_in = 0, m_out = 0;   // entries without self-loops
+    int64_t active0 = 0;           // words of vinit that are not full
+    int64_t zero_in = 0;           // rows without sources
+    int32_t max_deg = 0;
+};
+
+struct BfsScratch {
+    bool ready = false;
+    uint32_t *bm0 = nullptr, *bm1 = nullptr, *vis = nullptr;
+    int32_t *q0 = nullptr, *q1 = nullptr;
+    int32_t *level_pos = nullptr;
+    uint32_t *parent_pos = nullptr;
+    int32_t *out_level = nullptr, *out_parent = nullptr;  // staging for host outputs
+    BfsCtl *ctl = nullptr;
+    BfsCtl *h_ctl = nullptr;  // pinned mirror
+    alb_level_rec *trace = nullptr;
+    int32_t trace_cap = 0;
+};
+
+}  // namespace alb
+
+struct alb_graph {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int64_t n = 0;
+    int64_t nnz_in = 0, nnz_out = 0;
+    bool symmetric = false;
+    // original-id CSRs on the device (pull side = sources, push side = targets)
+    int64_t *rp_in = nullptr;
+    int32_t *col_in = nullptr;
+    int64_t *rp_out = nullptr;
+    int32_t *col_out = nullptr;
+    alb::Sell sell;
+    alb::BfsScratch bfs;
+    alb::CachedLoop *loop = nullptr;
+    std::vector<alb_level_rec> last_trace;
+    bool last_trace_valid = false;
+};
+
+namespace alb {
+alb_status bfs_scratch_alloc(alb_graph *g);
+void bfs_scratch_free(alb_graph *g);
+void loop_cache_free(alb_graph *g);
+BfsArgs make_args(alb_graph *g);
+}  // namespace alb

@@ -1,0 +1,180 @@
+/*
+ * albba_gb300 -- GB300-native linear-algebra BFS (C ABI).
+ *
+ * One process, one GPU (the current CUDA device when a graph is created).
+ * Every entry point returns an alb_status (0 = ALB_OK, negative = error) and
+ * never exits the process; alb_last_error() gives a message for the calling
+ * thread's last failure. A graph is not thread-safe; distinct graphs may be
+ * used from distinct threads.
+ *
+ * The reference (scalbba/albba) exposes the hot path as one plugin function,
+ * run_custom_bfs_test (bfs/src/bfs.h:13-24), fed by a CSR loaded in
+ * bfs/src/main.c:86-126. This header splits that path into its stages so a
+ * caller can hold a graph on the device and run many roots:
+ *
+ *   reference                                   this library
+ *   read_Dmatrix -> SparseMatrixCSR             alb_graph_create / _create32
+ *     (bfs/src/biio.h:127-149, main.c:91)
+ *   sellcs_preprocess (bfs_SELLCSv2.c:34-59)    alb_sell_build
+ *   level loop (bfs_SELLCSv2.c:296-762)         alb_bfs / alb_bfs_device
+ *   frontier[] / num_iter / num_vex / bfs_time  alb_stats + alb_level_trace
+ *   (no counterpart)                            alb_msbfs64, alb_worklist_*,
+ *                                               alb_selector_*, alb_tune_*
+ *
+ * The drop-in with the reference's exact plugin signature is
+ * include/albba_bfs_plugin.h.
+ *
+ * Index space: vertex ids are int32 (n < 2^31); row offsets are int64, so a
+ * graph may hold more than 2^31 stored entries (the reference's int nnz,
+ * bfs/src/sparse_matrix.h:26, cannot).
+ */
+#ifndef ALBBA_H
+#define ALBBA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t alb_status;
+#define ALB_OK 0
+#define ALB_ERR_INVALID (-1)     /* bad argument (null pointer, root out of range, ...) */
+#define ALB_ERR_OOM (-2)         /* device or host allocation failed */
+#define ALB_ERR_CUDA (-3)        /* CUDA runtime error (includes "no GPU") */
+#define ALB_ERR_TIMEOUT (-4)     /* a bounded device-side wait gave up */
+#define ALB_ERR_STATE (-5)       /* call order (e.g. BFS before alb_sell_build) */
+#define ALB_ERR_IO (-6)          /* file read/write failed or file malformed */
+#define ALB_ERR_UNSUPPORTED (-7) /* option outside the supported range */
+#define ALB_ERR_DEVICE (-8)      /* a kernel reported an internal bound violation */
+
+/* Thread-local message for the last failing call on this thread. */
+const char *alb_last_error(void);
+/* Library version string. */
+const char *alb_version(void);
+
+/* ---------------------------------------------------------------- graphs */
+
+typedef struct alb_graph alb_graph;
+
+/* CSR orientation flags for alb_graph_create*. */
+#define ALB_CSR_OUT 0u       /* row u lists the targets of u's edges */
+#define ALB_CSR_IN 1u        /* row v lists the sources of v's edges: the
+                                reference's working matrix after its
+                                transpose (bfs/src/main.c:117-126) */
+#define ALB_CSR_SYMMETRIC 2u /* A == A^T (both of the above) */
+#define ALB_CSR_SORTED 4u    /* caller guarantees ascending rows (skips the
+                                check; rows are sorted when the flag is absent) */
+
+/* Copy a host CSR (int64 offsets) to the current device. Duplicate entries
+ * are kept as given; self-loops are ignored by the traversal. */
+alb_status alb_graph_create(int64_t n, const int64_t *rowptr, const int32_t *col,
+                            uint32_t flags, alb_graph **out);
+/* Same, from the reference's int32 CSR (bfs/src/sparse_matrix.h:18-28). */
+alb_status alb_graph_create32(int32_t n, const int32_t *rowptr, const int32_t *col,
+                              uint32_t flags, alb_graph **out);
+void alb_graph_destroy(alb_graph *g);
+
+alb_status alb_graph_info(const alb_graph *g, int64_t *n, int64_t *nnz);
+
+/* ------------------------------------------------------------ SELL-C-sigma */
+
+typedef struct {
+    int32_t C;     /* slice height: 8, 16, 32 (default) or 64 */
+    int32_t sigma; /* sort window in rows: 1 .. 16384 (default 1024) */
+} alb_sell_opts;
+
+void alb_sell_opts_default(alb_sell_opts *o);
+
+/* Build the device SELL-C-sigma matrix (degree sort inside sigma windows by
+ * a device segmented radix sort, slice-major 4-interleaved int32 columns in
+ * sorted-position space) and the position-space push CSR. Replaces
+ * sellcs_preprocess (bfs/src/bfs_SELLCSv2.c:34-59). *ms (optional) receives
+ * the build time in milliseconds. Rebuilding with new options is allowed. */
+alb_status alb_sell_build(alb_graph *g, const alb_sell_opts *o, double *ms);
+
+/* Copy the built SELL arrays to host buffers (any pointer may be NULL):
+ * perm[n] (position -> original id), width[nslices], slice_off[nslices+1]
+ * (int64, in int32 entries), col[slice_off[nslices]]. */
+alb_status alb_sell_export(const alb_graph *g, int64_t *nslices, int32_t *perm,
+                           int32_t *width, int64_t *slice_off, int32_t *col);
+
+/* -------------------------------------------------------------------- BFS */
+
+/* Direction policy. Policies change speed only, never the BFS result. */
+#define ALB_POLICY_BEAMER 0    /* Beamer alpha/beta direction optimisation */
+#define ALB_POLICY_REF004 1    /* the reference's rule: pull when the frontier
+                                  holds more than 4% of n
+                                  (bfs/src/bfs_SELLCSv2.c:283-284, 344-356) */
+#define ALB_POLICY_LEARNED 2   /* device MLP selector (falls back to BEAMER
+                                  when no weights are loaded) */
+#define ALB_POLICY_TOPDOWN 3   /* every level top-down push */
+#define ALB_POLICY_BOTTOMUP 4  /* every level bottom-up pull with bypass
+                                  (level 0 runs top-down) */
+#define ALB_POLICY_BOTTOMUP_NOBYPASS 5 /* bottom-up pull, no slice bypass */
+
+/* Level-loop driver. */
+#define ALB_LOOP_HOST 0       /* one set of launches per level, host decides */
+#define ALB_LOOP_GRAPH 1      /* CUDA graph with a device-driven while node */
+#define ALB_LOOP_PERSISTENT 2 /* one cooperative kernel for all levels */
+
+/* Variant ids (per-level direction records, selector classes). */
+#define ALB_DIR_TOPDOWN 0
+#define ALB_DIR_BOTTOMUP 1
+#define ALB_DIR_BOTTOMUP_NOBYPASS 2
+
+typedef struct {
+    int32_t policy;  /* ALB_POLICY_* (default BEAMER) */
+    int32_t loop;    /* ALB_LOOP_* (default GRAPH) */
+    float alpha;     /* top-down -> bottom-up when m_f > m_u / alpha (14) */
+    float beta;      /* bottom-up -> top-down when n_f < n / beta (24) */
+    int32_t block;   /* threads per block for the level kernels (256) */
+    int32_t trace;   /* record per-level statistics (alb_level_trace) */
+} alb_bfs_opts;
+
+void alb_bfs_opts_default(alb_bfs_opts *o);
+
+typedef struct {
+    int32_t num_levels;   /* non-empty levels (the reference's num_iter) */
+    int32_t levels_topdown;
+    int32_t levels_bottomup;
+    int32_t pad_;
+    int64_t reached;      /* vertices reached (the reference's num_vex) */
+    int64_t edges;        /* stored push-side entries of reached vertices */
+    double ms;            /* device time of the traversal, SELL build excluded */
+} alb_stats;
+
+/* Single-root BFS. level[v] = depth or -1; parent[v] = smallest original id
+ * among v's sources one level up (root -> root, unreached -> -1). Host
+ * output buffers of n int32 each; either may be NULL. */
+alb_status alb_bfs(alb_graph *g, int32_t root, const alb_bfs_opts *o,
+                   int32_t *level, int32_t *parent, alb_stats *st);
+/* Same with device output buffers (n int32 each, either may be NULL). */
+alb_status alb_bfs_device(alb_graph *g, int32_t root, const alb_bfs_opts *o,
+                          int32_t *d_level, int32_t *d_parent, alb_stats *st);
+
+typedef struct {
+    int32_t dir;           /* ALB_DIR_* used for this level */
+    int32_t level;         /* frontier depth */
+    int64_t nf;            /* frontier vertices */
+    int64_t mf;            /* push-side entries of the frontier */
+    int64_t nu;            /* unvisited vertices before this level */
+    int64_t mu;            /* pull-side entries of unvisited vertices */
+    int64_t active_slices; /* slices with an unvisited row */
+    int64_t t_ns;          /* device timestamp at level start (ns) */
+} alb_level_rec;
+
+/* Per-level records of the last traversal on g (requires opts.trace). */
+alb_status alb_level_trace(const alb_graph *g, int32_t cap, alb_level_rec *out,
+                           int32_t *count);
+
+/* ---------------------------------------------------------------- testing */
+
+/* Host-side fault injection: the k-th next device allocation made by the
+ * library fails with ALB_ERR_OOM (k >= 1); k = 0 disarms. */
+void alb_debug_fail_alloc_after(int32_t k);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
