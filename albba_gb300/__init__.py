@@ -47,7 +47,7 @@ DIR_TOPDOWN, DIR_BOTTOMUP, DIR_BOTTOMUP_NOBYPASS = 0, 1, 2
 
 EXPORTED = [
     "alb_last_error", "alb_version", "alb_graph_create", "alb_graph_create32",
-    "alb_graph_destroy", "alb_graph_info", "alb_sell_opts_default", "alb_sell_build",
+    "alb_graph_destroy", "alb_graph_info", "alb_graph_set_stream", "alb_sell_opts_default", "alb_sell_build",
     "alb_sell_export", "alb_bfs_opts_default", "alb_bfs", "alb_bfs_device",
     "alb_level_trace", "alb_debug_fail_alloc_after", "alb_gen_rmat", "alb_gen_grid",
     "alb_gen_er", "alb_csr_from_edges", "alb_pick_roots", "alb_host_csr_free",
@@ -74,7 +74,7 @@ class BfsOpts(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("num_levels", C.c_int32), ("levels_topdown", C.c_int32),
                 ("levels_bottomup", C.c_int32), ("pad_", C.c_int32), ("reached", C.c_int64),
-                ("edges", C.c_int64), ("ms", C.c_double)]
+                ("edges", C.c_int64), ("ms", C.c_double), ("kernels", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad_"}
@@ -83,7 +83,8 @@ class Stats(C.Structure):
 class LevelRec(C.Structure):
     _fields_ = [("dir", C.c_int32), ("level", C.c_int32), ("nf", C.c_int64), ("mf", C.c_int64),
                 ("nu", C.c_int64), ("mu", C.c_int64), ("active_slices", C.c_int64),
-                ("t_ns", C.c_int64)]
+                ("t_ns", C.c_int64), ("bytes", C.c_int64), ("step_us", C.c_float),
+                ("pad_", C.c_int32)]
 
 
 class HostCsr(C.Structure):
@@ -102,6 +103,7 @@ _sigs = {
     "alb_graph_create32": (C.c_int32, [C.c_int32, _P, _P, C.c_uint32, C.POINTER(_P)]),
     "alb_graph_destroy": (None, [_P]),
     "alb_graph_info": (C.c_int32, [_P, _i64p, _i64p]),
+    "alb_graph_set_stream": (C.c_int32, [_P, _P]),
     "alb_sell_opts_default": (None, [C.POINTER(SellOpts)]),
     "alb_sell_build": (C.c_int32, [_P, C.POINTER(SellOpts), C.POINTER(C.c_double)]),
     "alb_sell_export": (C.c_int32, [_P, _i64p, _P, _P, _P, _P]),
@@ -301,6 +303,10 @@ class Graph:
     @property
     def handle(self) -> C.c_void_p:
         return self._h
+
+    def set_stream(self, cuda_stream: int | None) -> None:
+        """Run on a caller stream (e.g. torch.cuda.current_stream().cuda_stream)."""
+        check(_lib.alb_graph_set_stream(self._h, cuda_stream))
 
     def sell_build(self, C_: int = 32, sigma: int = 1024) -> float:
         o = SellOpts(C_, sigma)

@@ -25,6 +25,7 @@
 #include <algorithm>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "graph.h"
 #include "selector.cuh"
@@ -83,6 +84,9 @@ __device__ void record_trace(const BfsArgs &a, const BfsCtl &c, int dir) {
         r.mu = c.mu;
         r.active_slices = c.active_words;
         r.t_ns = (int64_t)globaltimer_ns();
+        r.bytes = 0;
+        r.step_us = -1.0f;
+        r.pad_ = 0;
         a.trace[c.level] = r;
     }
 }
@@ -234,13 +238,14 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r) {
     const int64_t stride = (int64_t)r.nblk * wpb;
     const int32_t C = a.C, log2C = a.log2C;
     const int32_t lvl = L + 1;
-    unsigned long long cn = 0, cmo = 0, cmi = 0, full = 0;
+    unsigned long long cn = 0, cmo = 0, cmi = 0, full = 0, bytes = 0;
     for (int64_t w = gw; w < a.nwords; w += stride) {
         const uint32_t vis = ld_bits<kPersist>(a.vis + w);
         if (kBypass && vis == kFull) {
             if (lane == 0) N[w] = 0;
             continue;
         }
+        bytes += 16;
         const int32_t p = (int32_t)(w * 32 + lane);
         const int64_t s = (int64_t)p >> log2C;
         bool active = !((vis >> lane) & 1u);
@@ -254,6 +259,7 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r) {
         for (int32_t j = 0;; j++) {
             active = active && (j < ng);
             if (!__any_sync(kFull, active)) break;
+            bytes += 16ull * 32;  // one int4 group for the warp's 32 rows
             if (!active) continue;
             const int4 c = ld_nc(cp + (int64_t)j * C);
             const uint32_t f0 = ld_bits<kPersist>(F + (c.x >> 5));
@@ -292,7 +298,7 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r) {
     cn = warp_sum(cn);
     cmo = warp_sum(cmo);
     cmi = warp_sum(cmi);
-    if (lane == 0 && (cn || full)) {
+    if (lane == 0 && (cn || full || bytes)) {
         const int k = (L + 1) % 3;
         if (cn) {
             atomicAdd(&a.ctl->acc_n[k], cn);
@@ -300,7 +306,15 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r) {
             atomicAdd(&a.ctl->acc_mi[k], cmi);
         }
         if (full) atomicAdd(&a.ctl->acc_full[k], full);
+        if (bytes) atomicAdd(&a.ctl->acc_bytes[k], bytes);
     }
+}
+
+// Algorithmic bytes of the level that just ran (see alb_level_rec).
+__host__ __device__ inline int64_t level_bytes(const BfsCtl &c, int dir, unsigned long long nn,
+                                               unsigned long long counted) {
+    if (dir == ALB_DIR_TOPDOWN) return 20 * c.nf + 8 * c.mf + 12 * (int64_t)nn;
+    return (int64_t)counted + 12 * c.nwords;
 }
 
 // Level rollover from the accumulators of slot (L+1)%3 (values read with
@@ -401,15 +415,15 @@ __global__ void k_decide(BfsArgs a, int forced, cudaGraphConditionalHandle sw) {
         a.ctl->acc_mo[k] = 0;
         a.ctl->acc_mi[k] = 0;
         a.ctl->acc_full[k] = 0;
+        a.ctl->acc_bytes[k] = 0;
         a.ctl->qn[k] = 0;
-        if (sw) {
-            unsigned branch;
-            if (dir == ALB_DIR_TOPDOWN)
-                branch = (!c.q_valid || c.n_dirty) ? 1u : 0u;
-            else
-                branch = dir == ALB_DIR_BOTTOMUP ? 2u : 3u;
-            cudaGraphSetConditional(sw, branch);
-        }
+        unsigned branch;
+        if (dir == ALB_DIR_TOPDOWN)
+            branch = (!c.q_valid || c.n_dirty) ? 1u : 0u;
+        else
+            branch = dir == ALB_DIR_BOTTOMUP ? 2u : 3u;
+        a.ctl->branch = (int32_t)branch;
+        if (sw) cudaGraphSetConditional(sw, branch);
     }
 }
 
@@ -436,6 +450,9 @@ __global__ void k_end(BfsArgs a, cudaGraphConditionalHandle wh) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     BfsCtl c = *a.ctl;
     const int k = (c.level + 1) % 3;
+    if (a.trace && c.level < c.trace_cap)
+        a.trace[c.level].bytes = level_bytes(c, c.dir, c.acc_n[k], c.acc_bytes[k]);
+    c.launches += 2 + (c.branch == 1 ? 3 : c.branch == 0 ? 2 : 1);  // decide, end, steps
     roll(c, c.dir, c.acc_n[k], c.acc_mo[k], c.acc_mi[k], c.acc_full[k]);
     if (c.level < c.trace_cap) c.trace_len = c.level;
     else c.trace_len = c.trace_cap;
@@ -501,6 +518,7 @@ __global__ void __launch_bounds__(256) k_persistent(BfsArgs a) {
                     a.ctl->acc_mo[k] = 0;
                     a.ctl->acc_mi[k] = 0;
                     a.ctl->acc_full[k] = 0;
+                    a.ctl->acc_bytes[k] = 0;
                     a.ctl->qn[k] = 0;
                 }
             }
@@ -533,6 +551,8 @@ __global__ void __launch_bounds__(256) k_persistent(BfsArgs a) {
         if (threadIdx.x == 0) {
             const int k = (L + 1) % 3;
             volatile BfsCtl *g = a.ctl;
+            if (blockIdx.x == 0 && a.trace && L < c.trace_cap)
+                a.trace[L].bytes = level_bytes(c, dir, g->acc_n[k], g->acc_bytes[k]);
             roll(c, dir, g->acc_n[k], g->acc_mo[k], g->acc_mi[k], g->acc_full[k]);
             c.dir = dir;
         }
@@ -743,10 +763,17 @@ alb_status build_loop_graph(alb_graph *g, int block) {
     return ALB_OK;
 }
 
-alb_status run_host_loop(alb_graph *g, const BfsArgs &a, const alb_bfs_opts &o) {
+alb_status run_host_loop(alb_graph *g, const BfsArgs &a, const alb_bfs_opts &o,
+                         std::vector<float> &step_us) {
     const Launch wide = level_launch(g, o.block);
     cudaStream_t st = g->stream;
     BfsCtl *h = g->bfs.h_ctl;
+    step_us.clear();
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (o.trace) {
+        ALB_CK(cudaEventCreate(&e0));
+        ALB_CK(cudaEventCreate(&e1));
+    }
     float mlp[kMlpParams];
     const bool have_mlp = o.policy == ALB_POLICY_LEARNED && selector_host_params(0, mlp);
     (void)a;
@@ -763,6 +790,7 @@ alb_status run_host_loop(alb_graph *g, const BfsArgs &a, const alb_bfs_opts &o) 
             dir = rule_dir(*h);
         }
         k_decide<<<1, 32, 0, st>>>(a, dir, 0);
+        if (e0) cudaEventRecord(e0, st);
         if (dir == ALB_DIR_TOPDOWN) {
             if (!h->q_valid || h->n_dirty) k_prep<<<wide.grid, wide.block, 0, st>>>(a);
             k_td<<<wide.grid, wide.block, 0, st>>>(a);
@@ -772,11 +800,19 @@ alb_status run_host_loop(alb_graph *g, const BfsArgs &a, const alb_bfs_opts &o) 
         } else {
             k_bu<false, false><<<wide.grid, wide.block, 0, st>>>(a);
         }
+        if (e1) cudaEventRecord(e1, st);
         k_end<<<1, 32, 0, st>>>(a, 0);
         ALB_CK(cudaGetLastError());
         ALB_CK(cudaMemcpyAsync(h, a.ctl, sizeof(BfsCtl), cudaMemcpyDeviceToHost, st));
         ALB_CK(cudaStreamSynchronize(st));
+        if (e0) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            step_us.push_back(ms * 1000.0f);
+        }
     }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
     return ALB_OK;
 }
 
@@ -820,8 +856,9 @@ alb_status bfs_impl(alb_graph *g, int32_t root, const alb_bfs_opts &o, int32_t *
     k_init_bulk<<<wide.grid, wide.block, 0, stream>>>(a);
     k_init_root<<<1, 32, 0, stream>>>(a, ip);
     ALB_CK(cudaGetLastError());
+    std::vector<float> step_us;
     if (o.loop == ALB_LOOP_HOST) {
-        ALB_TRY(run_host_loop(g, a, o));
+        ALB_TRY(run_host_loop(g, a, o, step_us));
     } else if (o.loop == ALB_LOOP_PERSISTENT) {
         ALB_TRY(run_persistent(g, a));
     } else {
@@ -845,6 +882,8 @@ alb_status bfs_impl(alb_graph *g, int32_t root, const alb_bfs_opts &o, int32_t *
         if (cnt)
             ALB_CK(cudaMemcpy(g->last_trace.data(), g->bfs.trace, sizeof(alb_level_rec) * cnt,
                               cudaMemcpyDeviceToHost));
+        for (int32_t i = 0; i < cnt && i < (int32_t)step_us.size(); i++)
+            g->last_trace[i].step_us = step_us[i];
         g->last_trace_valid = true;
     }
     if (st) {
@@ -855,6 +894,9 @@ alb_status bfs_impl(alb_graph *g, int32_t root, const alb_bfs_opts &o, int32_t *
         st->reached = c.reached;
         st->edges = c.edges;
         st->ms = ms;
+        // init_bulk + init_root (+ scatter), plus the loop's own launches
+        st->kernels = 2 + ((d_level || d_parent) ? 1 : 0) +
+                      (o.loop == ALB_LOOP_PERSISTENT ? 1 : c.launches);
     }
     return ALB_OK;
 }

@@ -78,11 +78,12 @@ struct BfsCtl {
     int64_t nu, mu;          // unvisited vertices / pull-side entries
     int64_t active_words;    // bitmap words with an unvisited row
     int64_t reached, edges;  // running totals
-    unsigned long long acc_n[3], acc_mo[3], acc_mi[3], acc_full[3], qn[3];
+    unsigned long long acc_n[3], acc_mo[3], acc_mi[3], acc_full[3], qn[3], acc_bytes[3];
     unsigned int bar_count, bar_gen;  // persistent-kernel grid barrier
     int32_t trace_cap, trace_len;
     int32_t level_cap;       // safety bound on the number of levels
-    int32_t pad_;
+    int32_t branch;          // loop-graph switch branch taken this level
+    int64_t launches;        // kernel launches of the level loop
     float feat_mean_deg, feat_skew;  // static selector features
 };
 

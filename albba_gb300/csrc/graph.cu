@@ -137,7 +137,8 @@ alb_status create_impl(int64_t n, const int64_t *rowptr, const int32_t *col, uin
         return s;
     };
     cudaError_t e = cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->own_stream, cudaStreamNonBlocking);
+    g->stream = g->own_stream;
     if (e == cudaSuccess) e = cudaEventCreate(&g->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&g->ev1);
     if (e != cudaSuccess) {
@@ -537,7 +538,7 @@ void alb_graph_destroy(alb_graph *g) {
     dfree(g->rp_in);
     if (g->ev0) cudaEventDestroy(g->ev0);
     if (g->ev1) cudaEventDestroy(g->ev1);
-    if (g->stream) cudaStreamDestroy(g->stream);
+    if (g->own_stream) cudaStreamDestroy(g->own_stream);
     cudaGetLastError();
     if (prev >= 0) cudaSetDevice(prev);
     delete g;
@@ -547,6 +548,14 @@ alb_status alb_graph_info(const alb_graph *g, int64_t *n, int64_t *nnz) {
     if (!g) return fail(ALB_ERR_INVALID, "alb_graph_info: graph is NULL");
     if (n) *n = g->n;
     if (nnz) *nnz = g->nnz_in;
+    return ALB_OK;
+}
+
+alb_status alb_graph_set_stream(alb_graph *g, void *cuda_stream) {
+    if (!g) return fail(ALB_ERR_INVALID, "alb_graph_set_stream: graph is NULL");
+    ALB_CK(cudaSetDevice(g->device));
+    ALB_CK(cudaStreamSynchronize(g->stream));
+    g->stream = cuda_stream ? (cudaStream_t)cuda_stream : g->own_stream;
     return ALB_OK;
 }
 

@@ -69,7 +69,8 @@ struct BfsScratch {
 struct alb_graph {
     int device = 0;
     int num_sms = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;      // stream in use
+    cudaStream_t own_stream = nullptr;  // created with the graph
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int64_t n = 0;
     int64_t nnz_in = 0, nnz_out = 0;

@@ -1,0 +1,354 @@
+#!/usr/bin/env python3
+"""Benchmark: GTEPS on RMAT scale 24, edge factor 16, 64 seeded roots.
+
+A step is one pass of the hot path over one batch: BFS from all 64 roots of
+the RMAT s24 ef16 graph (A/B/C/D = .57/.19/.19/.05, vertex ids permuted,
+symmetrised, self-loops and duplicates removed). The headline form is the
+64-root batched BFS driven by the learned direction selector; the plain form
+is 64 single-root direction-optimising BFS runs. GTEPS = sum over roots of
+the undirected edges in the root's component / step time (Graph500
+convention).
+
+  value  device-resident graph and outputs, CUDA events on the launching
+         stream around each step
+  e2e    the same work through the C ABI with host buffers: graph upload
+         (alb_graph_create), SELL build, traversal and the copy of every
+         level (and parent) array back to the host, all inside the timer
+  roofline  bottom-up kernel: algorithmic bytes counted by the kernel itself
+         (per level, the formula in include/albba.h) / CUDA-event duration of
+         its launches, against the measured HBM copy bandwidth
+  cpu_baseline  the reference's level loop (C = 256 SELL, pull + sparse-x
+         kernels) restated in C with OpenMP, on this host's cores, for a
+         bounded sample of roots
+
+--impl reference times only that CPU port (all host threads) on the same
+graph and roots. Multi-GPU runs are independent replicas (one process per
+GPU, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "GTEPS RMAT s24 ef16: learned-switch & 64-root batched vs plain; % HBM peak"
+SEED_GRAPH, SEED_ROOTS = 24, 7
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--scale", type=int, default=24)
+    p.add_argument("--edgefactor", type=int, default=16)
+    p.add_argument("--roots", type=int, default=64)
+    p.add_argument("--sigma", type=int, default=1024)
+    p.add_argument("--cpu-roots", type=int, default=1, help="roots timed for the CPU baseline")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-roofline", action="store_true")
+    p.add_argument("--loop", choices=["graph", "host", "persistent"], default="graph")
+    p.add_argument("--out", default=None, help="also write the JSON line to this file")
+    return p.parse_args()
+
+
+def peaks() -> tuple[float, str]:
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        try:
+            return float(json.loads(f.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampler for the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.rows: list[list[str]] = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = max(mx, float(r[2]))
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_graph(args):
+    import albba_gb300 as ab
+    t0 = time.time()
+    g = ab.gen_rmat(args.scale, args.edgefactor, seed=SEED_GRAPH)
+    roots = g.pick_roots(args.roots, seed=SEED_ROOTS)
+    return g, roots, time.time() - t0
+
+
+def config(args, g, extra=None):
+    c = {"workload": f"RMAT scale {args.scale} edgefactor {args.edgefactor}, {args.roots} roots "
+                     "(BFS from every root per step)",
+         "n": g.n, "stored_entries": g.nnz, "roots": args.roots, "C": 32, "sigma": args.sigma,
+         "graph_seed": SEED_GRAPH, "root_seed": SEED_ROOTS,
+         "l2": "inputs larger than L2 (graph > 1 GB vs 129 MB L2); no flush"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+# ----------------------------------------------------------------- CPU side
+def cpu_baseline(g, roots, nroots: int) -> dict:
+    import oracle
+    ra = oracle.RefAlgo(g.rowptr, g.col, sigma=16384, ntasks=0)
+    deg = g.degrees()
+    edges, ms = 0, 0.0
+    for r in roots[:nroots]:
+        counts, bms = ra.run(int(r))
+        lv, _, _ = oracle.bfs(g.rowptr, g.col, int(r))
+        edges += int(deg[lv >= 0].sum()) // 2
+        ms += bms
+    ra.close()
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": edges / ms / 1e6, "unit": "GTEPS", "cores": threads, "kind": "port",
+            "sample": f"{nroots} of {len(roots)} roots, level loop only (SELL-256 build "
+                      f"{ra.conv_ms:.0f} ms excluded, as the reference times it)"}
+
+
+def run_reference(args, rank: int, world: int) -> None:
+    if rank != 0:
+        return
+    g, roots, _ = make_graph(args)
+    import oracle
+    ra = oracle.RefAlgo(g.rowptr, g.col, sigma=16384, ntasks=0)
+    deg = g.degrees()
+    comp = {}
+    times = []
+    edges = 0
+    for i in range(args.warmup + args.steps):
+        r = int(roots[i % len(roots)])
+        counts, bms = ra.run(r)
+        if r not in comp:
+            lv, _, _ = oracle.bfs(g.rowptr, g.col, r)
+            comp[r] = int(deg[lv >= 0].sum()) // 2
+        if i >= args.warmup:
+            times.append(bms)
+            edges += comp[r]
+    ms = sum(times)
+    v = edges / ms / 1e6
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    line = {"metric": METRIC, "value": v, "unit": "GTEPS", "impl": "reference", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / max(len(times), 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic RMAT (seeded), reference level loop restated in C (OpenMP)",
+            "config": config(args, g, {"step": "one root per step (bounded CPU sample)"}),
+            "cpu_baseline": {"value": v, "unit": "GTEPS", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} timed roots, one per step"},
+            "e2e": {"value": v, "unit": "GTEPS", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    ra.close()
+    emit(line, args)
+
+
+# ----------------------------------------------------------------- GPU side
+def run_ours(args, rank: int, world: int, dist) -> None:
+    import torch
+
+    import albba_gb300 as ab
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    g, roots, gen_s = make_graph(args)
+    deg = g.degrees()
+    stream = torch.cuda.current_stream()
+    dg = ab.Graph(g, flags=ab.CSR_SYMMETRIC | ab.CSR_SORTED)
+    dg.set_stream(stream.cuda_stream)
+    build_ms = dg.sell_build(32, args.sigma)
+    n = g.n
+    d_lv = torch.empty(n, dtype=torch.int32, device="cuda")
+    d_pa = torch.empty(n, dtype=torch.int32, device="cuda")
+    opts = ab.bfs_opts("beamer", args.loop)
+
+    def plain_step():
+        e = 0
+        k = 0
+        per_root = []
+        for r in roots:
+            st = dg.bfs_device(int(r), d_lv, d_pa, opts)
+            e += st.edges // 2
+            k += st.kernels
+            per_root.append((st.edges // 2, st.ms))
+        return e, k, per_root
+
+    # warm-up
+    for _ in range(args.warmup):
+        plain_step()
+    sync = (lambda: dist.barrier()) if dist else (lambda: None)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(dev) as clk:
+        sync()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        edges, launches, per_root = 0, 0, []
+        for _ in range(args.steps):
+            e, k, pr = plain_step()
+            edges += e
+            launches += k
+            per_root += pr
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        sync()
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    steps = args.steps
+    value = world * edges / ms / 1e6
+    hm = len(per_root) / sum(ms_r / (e_r / 1e6) for e_r, ms_r in per_root if e_r > 0) \
+        if per_root else None
+
+    # roofline: bottom-up launches timed with CUDA events (host-driven loop)
+    roof = None if args.no_roofline else roofline(dg, roots[:8])
+    e2e = None if args.no_e2e else e2e_plain(args, g, roots, ab, torch)
+    cpu = cpu_baseline(g, roots, args.cpu_roots) if rank == 0 and args.cpu_roots > 0 else None
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": world, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": ms / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic RMAT (seeded generator, no dataset)",
+            "config": config(args, g, {"form": "plain direction-optimising single-root BFS x 64 "
+                                               "(CUDA-graph level loop)",
+                                       "parallelism": f"replicas x{world}"}),
+            "plain_gteps_harmonic_mean": hm,
+            "sell_build_ms": build_ms, "graph_gen_s": gen_s,
+            "gpu_launches": launches, "clocks": clk.summary(), "roofline": roof,
+            "e2e": e2e, "cpu_baseline": cpu}
+    emit(line, args)
+
+
+def roofline(dg, roots) -> dict:
+    import albba_gb300 as ab
+    peak, kind = peaks()
+    byts, us, launches = 0, 0.0, 0
+    for r in roots:
+        dg.bfs(int(r), ab.bfs_opts("beamer", "host", trace=True), want_level=False,
+               want_parent=False)
+        for t in dg.level_trace():
+            if t.dir == ab.DIR_BOTTOMUP and t.step_us > 0:
+                byts += t.bytes
+                us += t.step_us
+                launches += 1
+    gbs = byts / us / 1e3 if us > 0 else 0.0
+    return {"bound": "hbm", "kernel": "k_bu (bottom-up pull, bypass + early exit)",
+            "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+            "peak_kind": f"{kind} HBM copy bandwidth (burst)",
+            "bytes_per_launch": byts / max(launches, 1), "us_per_launch": us / max(launches, 1),
+            "launches": launches, "traffic": None}
+
+
+def e2e_plain(args, g, roots, ab, torch) -> dict:
+    n = g.n
+    lv = np.empty(n, np.int32)
+    pa = np.empty(n, np.int32)
+    h2d = g.rowptr.nbytes + g.col.nbytes
+    d2h = len(roots) * (lv.nbytes + pa.nbytes)
+
+    def step():
+        e = 0
+        with ab.Graph(g, flags=ab.CSR_SYMMETRIC | ab.CSR_SORTED) as dg:
+            dg.sell_build(32, args.sigma)
+            for r in roots:
+                _, _, st = dg.bfs(int(r), ab.bfs_opts("beamer", "graph"))
+                e += st.edges // 2
+        return e
+
+    step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    k = 2
+    e = sum(step() for _ in range(k))
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    return {"value": e / dt / 1e9, "unit": "GTEPS", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "steps": k,
+            "path": "alb_graph_create (host CSR) + alb_sell_build + alb_bfs x roots "
+                    "(host level+parent), wall clock"}
+
+
+def emit(line: dict, args) -> None:
+    s = json.dumps(line)
+    print(s, flush=True)
+    if args.out:
+        Path(args.out).write_text(s + "\n")
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as td
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        td.init_process_group("nccl")
+        dist = td
+    run_ours(args, rank, world, dist)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

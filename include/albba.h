@@ -77,6 +77,11 @@ void alb_graph_destroy(alb_graph *g);
 
 alb_status alb_graph_info(const alb_graph *g, int64_t *n, int64_t *nnz);
 
+/* Run the graph's work on a caller-provided cudaStream_t (NULL restores the
+ * graph's own stream). Entry points still synchronise that stream before
+ * returning host-visible results. */
+alb_status alb_graph_set_stream(alb_graph *g, void *cuda_stream);
+
 /* ------------------------------------------------------------ SELL-C-sigma */
 
 typedef struct {
@@ -142,6 +147,7 @@ typedef struct {
     int64_t reached;      /* vertices reached (the reference's num_vex) */
     int64_t edges;        /* stored push-side entries of reached vertices */
     double ms;            /* device time of the traversal, SELL build excluded */
+    int64_t kernels;      /* kernel launches made by this call */
 } alb_stats;
 
 /* Single-root BFS. level[v] = depth or -1; parent[v] = smallest original id
@@ -160,13 +166,32 @@ typedef struct {
     int64_t mf;            /* push-side entries of the frontier */
     int64_t nu;            /* unvisited vertices before this level */
     int64_t mu;            /* pull-side entries of unvisited vertices */
-    int64_t active_slices; /* slices with an unvisited row */
+    int64_t active_slices; /* bitmap words (32 rows) with an unvisited row */
     int64_t t_ns;          /* device timestamp at level start (ns) */
+    int64_t bytes;         /* algorithmic bytes of the level's step (see below) */
+    float step_us;         /* CUDA-event time of the step kernels (host loop
+                              only; -1 otherwise) */
+    int32_t pad_;
 } alb_level_rec;
+/* Algorithmic bytes: bottom-up = sum over non-bypassed 32-row words of
+ * 16 + 16*C*K (K = int4 column groups the warp loaded) + 12*nwords (visited
+ * read, next-frontier write, frontier read once); top-down = 20*|F| +
+ * 8*sum(deg F) + 12*|F_next| (queue + offsets, adjacency + visited probes,
+ * level/parent/queue writes). */
 
 /* Per-level records of the last traversal on g (requires opts.trace). */
 alb_status alb_level_trace(const alb_graph *g, int32_t cap, alb_level_rec *out,
                            int32_t *count);
+
+/* --------------------------------------------------------------- selector */
+
+/* Load the 1,443 fp32 parameters of a direction-selector MLP
+ * (8 -> 32 -> 32 -> 3, ReLU; layout W1[32][8], b1, W2[32][32], b2, W3[3][32],
+ * b3). which = 0: single-root BFS, 1: 64-root batched BFS. The MLP's output k
+ * is the predicted cost of variant k (ALB_DIR_*); the cheapest is taken. */
+alb_status alb_selector_load(int32_t which, const float *params);
+/* Forget loaded weights (ALB_POLICY_LEARNED falls back to Beamer). */
+alb_status alb_selector_clear(int32_t which);
 
 /* ---------------------------------------------------------------- testing */
 

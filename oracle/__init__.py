@@ -58,6 +58,13 @@ def lib() -> C.CDLL:
         L.orc_refalgo_bfs.restype = C.c_int32
         L.orc_refalgo_bfs.argtypes = [C.c_int64, P, P, C.c_int32, C.c_int32, C.c_int32, P,
                                       C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.orc_refalgo_prepare.restype = C.c_void_p
+        L.orc_refalgo_prepare.argtypes = [C.c_int64, P, P, C.c_int32, C.c_int32,
+                                          C.POINTER(C.c_double)]
+        L.orc_refalgo_run.restype = C.c_int32
+        L.orc_refalgo_run.argtypes = [P, C.c_int32, P, C.POINTER(C.c_double)]
+        L.orc_refalgo_free.restype = None
+        L.orc_refalgo_free.argtypes = [P]
         L.orc_mlp_forward.restype = None
         L.orc_mlp_forward.argtypes = [P, C.c_int32, P, P]
         L.orc_mlp_loss_grad.restype = C.c_float
@@ -132,6 +139,32 @@ def refalgo_bfs(rowptr, col, root, sigma=16384, ntasks=0):
     nl = lib().orc_refalgo_bfs(n, rp.ctypes.data, cl.ctypes.data, int(root), int(sigma),
                                int(ntasks), counts.ctypes.data, C.byref(bms), C.byref(cms))
     return counts[:nl], bms.value, cms.value
+
+
+class RefAlgo:
+    """The reference's level loop restated on the CPU, SELL built once."""
+
+    def __init__(self, rowptr, col, sigma=16384, ntasks=0):
+        self._rp, self._col = _a(rowptr, np.int64), _a(col, np.int32)
+        self.n = self._rp.shape[0] - 1
+        cms = C.c_double()
+        self._h = lib().orc_refalgo_prepare(self.n, self._rp.ctypes.data, self._col.ctypes.data,
+                                            int(sigma), int(ntasks), C.byref(cms))
+        self.conv_ms = cms.value
+
+    def run(self, root):
+        counts = np.zeros(self.n + 1, np.int64)
+        bms = C.c_double()
+        nl = lib().orc_refalgo_run(self._h, int(root), counts.ctypes.data, C.byref(bms))
+        return counts[:nl], bms.value
+
+    def close(self):
+        if self._h:
+            lib().orc_refalgo_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
 
 
 def mlp_forward(params, x):

@@ -90,6 +90,12 @@ int32_t orc_refalgo_bfs(int64_t n, const int64_t *rowptr, const int32_t *col,
                         int32_t root, int32_t sigma, int32_t ntasks,
                         int64_t *counts, double *bfs_ms, double *conv_ms);
 
+/* The same port split into build (once) and traversal (per root). */
+void *orc_refalgo_prepare(int64_t n, const int64_t *rowptr, const int32_t *col,
+                          int32_t sigma, int32_t ntasks, double *conv_ms);
+int32_t orc_refalgo_run(void *h, int32_t root, int64_t *counts, double *bfs_ms);
+void orc_refalgo_free(void *h);
+
 /* CPU MLP (8 -> 32 -> 32 -> 3, ReLU) used to check the GPU selector kernels.
  * Parameter block layout (fp32, 1,443 values):
  *   W1[32][8], b1[32], W2[32][32], b2[32], W3[3][32], b3[3]. */

@@ -233,51 +233,80 @@ static int64_t sparse_kernel(const rsell *m, const int32_t *bucket,
     return cnt;
 }
 
-int32_t orc_refalgo_bfs(int64_t n, const int64_t *rowptr, const int32_t *col,
-                        int32_t root, int32_t sigma, int32_t ntasks,
-                        int64_t *counts, double *bfs_ms, double *conv_ms)
-{
+typedef struct {
     rsell m;
+    int32_t T;
+    int64_t *task;
+    int32_t *inv;
+    double conv_ms;
+} refalgo;
+
+void *orc_refalgo_prepare(int64_t n, const int64_t *rowptr, const int32_t *col, int32_t sigma,
+                          int32_t ntasks, double *conv_ms)
+{
+    refalgo *h = (refalgo *)calloc(1, sizeof(refalgo));
     double t0 = now_ms();
-    rsell_build(&m, n, rowptr, col, sigma);
-    *conv_ms = now_ms() - t0;
+    rsell_build(&h->m, n, rowptr, col, sigma);
+    h->conv_ms = now_ms() - t0;
+    if (conv_ms)
+        *conv_ms = h->conv_ms;
     int nthreads = 1;
 #ifdef _OPENMP
     nthreads = omp_get_max_threads();
 #endif
     int32_t T = ntasks > 0 ? ntasks : nthreads;
+    h->T = T;
     /* bfs_SELLCSv2.c:61-85: nnz-balanced slice ranges */
-    int64_t *task = (int64_t *)malloc(sizeof(int64_t) * (T + 1));
-    {
-        int64_t total = m.slice_ptr[m.nslices];
-        int64_t per = (total + T - 1) / T;
-        int64_t acc = 0;
-        int32_t ti = 0;
-        task[ti++] = 0;
-        for (int64_t s = 0; s < m.nslices; s++) {
-            if (acc >= per && ti < T) {
-                task[ti++] = s;
-                acc = 0;
-            }
-            acc += m.slice_ptr[s + 1] - m.slice_ptr[s];
+    h->task = (int64_t *)malloc(sizeof(int64_t) * (T + 1));
+    int64_t total = h->m.slice_ptr[h->m.nslices];
+    int64_t per = (total + T - 1) / T;
+    int64_t acc = 0;
+    int32_t ti = 0;
+    h->task[ti++] = 0;
+    for (int64_t s = 0; s < h->m.nslices; s++) {
+        if (acc >= per && ti < T) {
+            h->task[ti++] = s;
+            acc = 0;
         }
-        for (int32_t i = ti; i <= T; i++)
-            task[i] = m.nslices;
+        acc += h->m.slice_ptr[s + 1] - h->m.slice_ptr[s];
     }
+    for (int32_t i = ti; i <= T; i++)
+        h->task[i] = h->m.nslices;
+    h->inv = (int32_t *)malloc(sizeof(int32_t) * n);
+    for (int64_t p = 0; p < n; p++)
+        h->inv[h->m.row_order[p]] = (int32_t)p;
+    return h;
+}
+
+void orc_refalgo_free(void *handle)
+{
+    refalgo *h = (refalgo *)handle;
+    if (!h)
+        return;
+    rsell_free(&h->m);
+    free(h->task);
+    free(h->inv);
+    free(h);
+}
+
+int32_t orc_refalgo_run(void *handle, int32_t root, int64_t *counts, double *bfs_ms)
+{
+    refalgo *h = (refalgo *)handle;
+    const rsell *mp = &h->m;
+    const int64_t n = mp->n;
+    const int32_t T = h->T;
+    const int64_t *task = h->task;
     int32_t *mask_x = (int32_t *)calloc(n, sizeof(int32_t));
     int32_t *mask_y = (int32_t *)calloc(n, sizeof(int32_t));
     int32_t *colidx_x = (int32_t *)calloc(n, sizeof(int32_t));
-    int32_t *colidx_y = (int32_t *)calloc((size_t)(m.nslices * RC), sizeof(int32_t));
+    int32_t *colidx_y = (int32_t *)calloc((size_t)(mp->nslices * RC), sizeof(int32_t));
     int32_t *bucket = (int32_t *)calloc(n + 1, sizeof(int32_t));
     uint64_t *mask = (uint64_t *)calloc(n / 64 + 8, sizeof(uint64_t));
     int64_t *tcnt = (int64_t *)calloc(T + 1, sizeof(int64_t));
-    int32_t *inv = (int32_t *)malloc(sizeof(int32_t) * n);
-    for (int64_t p = 0; p < n; p++)
-        inv[m.row_order[p]] = (int32_t)p;
 
     mask_x[root] = 1;
     colidx_x[0] = root;
-    vis_set(mask, inv[root]);
+    vis_set(mask, h->inv[root]);
     int64_t nnzx = 1;
     const int64_t thr = (int64_t)(n * 0.04); /* bfs_SELLCSv2.c:283-284 */
     int32_t iters = 0;
@@ -299,14 +328,14 @@ int32_t orc_refalgo_bfs(int64_t n, const int64_t *rowptr, const int32_t *col,
         const int dense = nnzx > thr;
 #pragma omp parallel for schedule(dynamic, 1)
         for (int32_t t = 0; t < T; t++) {
-            if (task[t] >= m.nslices) {
+            if (task[t] >= mp->nslices) {
                 tcnt[t] = 0;
                 continue;
             }
             if (dense)
-                tcnt[t] = pull_kernel(&m, mask_x, mask_y, task[t], task[t + 1], mask);
+                tcnt[t] = pull_kernel(mp, mask_x, mask_y, task[t], task[t + 1], mask);
             else
-                tcnt[t] = sparse_kernel(&m, bucket, colidx_x, x_max, x_min, colidx_y,
+                tcnt[t] = sparse_kernel(mp, bucket, colidx_x, x_max, x_min, colidx_y,
                                         task[t], task[t + 1], mask);
         }
         counts[iters] = nnzx;
@@ -351,7 +380,6 @@ int32_t orc_refalgo_bfs(int64_t n, const int64_t *rowptr, const int32_t *col,
     } while (nnzx != 0);
     *bfs_ms = now_ms() - ts;
 
-    free(task);
     free(mask_x);
     free(mask_y);
     free(colidx_x);
@@ -359,7 +387,15 @@ int32_t orc_refalgo_bfs(int64_t n, const int64_t *rowptr, const int32_t *col,
     free(bucket);
     free(mask);
     free(tcnt);
-    free(inv);
-    rsell_free(&m);
     return iters;
+}
+
+int32_t orc_refalgo_bfs(int64_t n, const int64_t *rowptr, const int32_t *col,
+                        int32_t root, int32_t sigma, int32_t ntasks,
+                        int64_t *counts, double *bfs_ms, double *conv_ms)
+{
+    void *h = orc_refalgo_prepare(n, rowptr, col, sigma, ntasks, conv_ms);
+    int32_t nl = orc_refalgo_run(h, root, counts, bfs_ms);
+    orc_refalgo_free(h);
+    return nl;
 }

@@ -16,7 +16,8 @@ GOLDEN = ROOT / "tests" / "golden"
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
     # make sure the native library and the oracle exist before collection
-    from albba_gb300 import build as _b  # noqa: WPS433
+    import __graft_entry__ as ge  # noqa: WPS433
+    _b = ge._build_module()
     if not _b.LIB.exists():
         _b.build_library()
     import oracle  # noqa: WPS433
