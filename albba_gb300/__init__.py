@@ -52,6 +52,7 @@ EXPORTED = [
     "alb_level_trace", "alb_debug_fail_alloc_after", "alb_gen_rmat", "alb_gen_grid",
     "alb_gen_er", "alb_csr_from_edges", "alb_pick_roots", "alb_host_csr_free",
     "alb_cbd_write", "alb_cbd_read", "alb_selector_load", "alb_selector_clear",
+    "alb_msbfs64", "alb_msbfs64_device",
 ]
 
 
@@ -122,6 +123,9 @@ _sigs = {
     "alb_host_csr_free": (None, [C.POINTER(HostCsr)]),
     "alb_cbd_write": (C.c_int32, [C.c_char_p, C.POINTER(HostCsr)]),
     "alb_cbd_read": (C.c_int32, [C.c_char_p, C.POINTER(HostCsr)]),
+    "alb_msbfs64": (C.c_int32, [_P, _P, C.c_int32, C.POINTER(BfsOpts), _P, C.POINTER(Stats)]),
+    "alb_msbfs64_device": (C.c_int32, [_P, _P, C.c_int32, C.POINTER(BfsOpts), _P,
+                                       C.POINTER(Stats)]),
     "alb_selector_load": (C.c_int32, [C.c_int32, _P]),
     "alb_selector_clear": (C.c_int32, [C.c_int32]),
 }
@@ -341,6 +345,24 @@ class Graph:
         o = opts or bfs_opts()
         check(_lib.alb_bfs_device(self._h, int(root), C.byref(o), _ptr(d_level), _ptr(d_parent),
                                   C.byref(st)))
+        return st
+
+    def msbfs64(self, roots, opts: BfsOpts | None = None) -> tuple[np.ndarray, Stats]:
+        """Levels from up to 64 roots at once: array (n, 64), column i = roots[i]."""
+        r = np.ascontiguousarray(roots, dtype=np.int32)
+        out = np.empty((self.n, 64), np.int32)
+        st = Stats()
+        o = opts or bfs_opts()
+        check(_lib.alb_msbfs64(self._h, r.ctypes.data, r.shape[0], C.byref(o), out.ctypes.data,
+                               C.byref(st)))
+        return out, st
+
+    def msbfs64_device(self, roots, d_levels=None, opts: BfsOpts | None = None) -> Stats:
+        r = np.ascontiguousarray(roots, dtype=np.int32)
+        st = Stats()
+        o = opts or bfs_opts()
+        check(_lib.alb_msbfs64_device(self._h, r.ctypes.data, r.shape[0], C.byref(o),
+                                      _ptr(d_levels), C.byref(st)))
         return st
 
     def level_trace(self) -> list[LevelRec]:

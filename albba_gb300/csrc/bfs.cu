@@ -125,6 +125,37 @@ __device__ void prep_phase(const BfsArgs &a, int L, bool compact, bool zero_next
     }
 }
 
+// One pushed edge u -> v (u's original id ou); returns true when v is claimed.
+__device__ __forceinline__ bool push_edge(const BfsArgs &a, uint32_t *N, int32_t v, uint32_t ou,
+                                          bool persist) {
+    const uint32_t bit = 1u << (v & 31);
+    const uint32_t w = persist ? __ldcg(a.vis + (v >> 5)) : __ldg(a.vis + (v >> 5));
+    if (w & bit) return false;
+    atomicMin(a.parent_pos + v, ou);
+    return !(atomicOr(N + (v >> 5), bit) & bit);
+}
+
+// Warp-aggregated append of claimed targets to the next queue.
+__device__ __forceinline__ void append_claims(const BfsArgs &a, int32_t *NQ,
+                                              unsigned long long *nq_slot, bool claimed, int32_t v,
+                                              uint32_t lvl, unsigned long long &cn,
+                                              unsigned long long &cmo, unsigned long long &cmi) {
+    const unsigned cm = __ballot_sync(kFull, claimed);
+    if (!cm) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(cm) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(nq_slot, (unsigned long long)__popc(cm));
+    base = __shfl_sync(kFull, base, leader);
+    if (claimed) {
+        NQ[base + __popc(cm & lanemask_lt())] = v;
+        a.level_pos[v] = (int32_t)lvl;
+        cn++;
+        cmo += (unsigned long long)__ldg(a.odeg + v);
+        cmi += (unsigned long long)__ldg(a.ideg + v);
+    }
+}
+
 template <bool kPersist>
 __device__ void td_phase(const BfsArgs &a, int L, Range r) {
     const int32_t *Q = (L & 1) ? a.q1 : a.q0;
@@ -132,6 +163,7 @@ __device__ void td_phase(const BfsArgs &a, int L, Range r) {
     uint32_t *N = (L & 1) ? a.bm0 : a.bm1;
     const int64_t qlen = (int64_t)ld_state<kPersist>(&a.ctl->qn[L % 3]);
     unsigned long long *nq_slot = &a.ctl->qn[(L + 1) % 3];
+    unsigned long long *big_slot = &a.ctl->nbig[L % 3];
     __shared__ int64_t s_ex[kMaxBlock / 32][32];
     __shared__ int64_t s_st[kMaxBlock / 32][32];
     __shared__ int32_t s_ou[kMaxBlock / 32][32];
@@ -150,6 +182,10 @@ __device__ void td_phase(const BfsArgs &a, int L, Range r) {
             st = __ldg(a.prow + u);
             d = __ldg(a.prow + u + 1) - st;
             ou = __ldg(a.perm + u);
+            if (d > kBigRow) {  // shared by all warps in big_phase
+                a.big[atomicAdd(big_slot, 1ull)] = u;
+                d = 0;
+            }
         }
         const int64_t inc = warp_inclusive_scan(d);
         const int64_t T = __shfl_sync(kFull, inc, 31);
@@ -167,29 +203,55 @@ __device__ void td_phase(const BfsArgs &a, int L, Range r) {
                 for (int step = 16; step > 0; step >>= 1)
                     if (s_ex[wib][j + step] <= e) j += step;
                 v = __ldg(a.pcol + s_st[wib][j] + (e - s_ex[wib][j]));
-                const uint32_t bit = 1u << (v & 31);
-                const uint32_t w = ld_bits<kPersist>(a.vis + (v >> 5));
-                if (!(w & bit)) {
-                    atomicMin(a.parent_pos + v, (uint32_t)s_ou[wib][j]);
-                    claimed = !(atomicOr(N + (v >> 5), bit) & bit);
-                }
+                claimed = push_edge(a, N, v, (uint32_t)s_ou[wib][j], kPersist);
             }
-            const unsigned cm = __ballot_sync(kFull, claimed);
-            if (cm) {
-                const int leader = __ffs(cm) - 1;
-                unsigned long long base = 0;
-                if (lane == leader) base = atomicAdd(nq_slot, (unsigned long long)__popc(cm));
-                base = __shfl_sync(kFull, base, leader);
-                if (claimed) {
-                    NQ[base + __popc(cm & lanemask_lt())] = v;
-                    a.level_pos[v] = (int32_t)lvl;
-                    cn++;
-                    cmo += (unsigned long long)__ldg(a.odeg + v);
-                    cmi += (unsigned long long)__ldg(a.ideg + v);
-                }
-            }
+            append_claims(a, NQ, nq_slot, claimed, v, lvl, cn, cmo, cmi);
         }
         __syncwarp();
+    }
+    cn = warp_sum(cn);
+    cmo = warp_sum(cmo);
+    cmi = warp_sum(cmi);
+    if (lane == 0 && cn) {
+        const int k = (L + 1) % 3;
+        atomicAdd(&a.ctl->acc_n[k], cn);
+        atomicAdd(&a.ctl->acc_mo[k], cmo);
+        atomicAdd(&a.ctl->acc_mi[k], cmi);
+    }
+}
+
+// Long frontier rows: chunk c of big row i goes to warp (i + c) mod warps.
+template <bool kPersist>
+__device__ void td_big_phase(const BfsArgs &a, int L, Range r) {
+    const int64_t nbig = (int64_t)ld_state<kPersist>(&a.ctl->nbig[L % 3]);
+    if (nbig == 0) return;
+    int32_t *NQ = (L & 1) ? a.q0 : a.q1;
+    uint32_t *N = (L & 1) ? a.bm0 : a.bm1;
+    unsigned long long *nq_slot = &a.ctl->qn[(L + 1) % 3];
+    const int lane = threadIdx.x & 31;
+    const int64_t wpb = blockDim.x >> 5;
+    const int64_t gw = (int64_t)r.bid * wpb + (threadIdx.x >> 5);
+    const int64_t nwarps = (int64_t)r.nblk * wpb;
+    const uint32_t lvl = (uint32_t)(L + 1);
+    unsigned long long cn = 0, cmo = 0, cmi = 0;
+    for (int64_t i = 0; i < nbig; i++) {
+        const int32_t u = ld_state<kPersist>(a.big + i);
+        const int64_t st = __ldg(a.prow + u);
+        const int64_t d = __ldg(a.prow + u + 1) - st;
+        const uint32_t ou = (uint32_t)__ldg(a.perm + u);
+        const int64_t nch = (d + kBigChunk - 1) / kBigChunk;
+        for (int64_t c = ((gw - i) % nwarps + nwarps) % nwarps; c < nch; c += nwarps) {
+            const int64_t e1 = min(d, (c + 1) * kBigChunk);
+            for (int64_t e = c * kBigChunk + lane; e - lane < e1; e += 32) {
+                bool claimed = false;
+                int32_t v = 0;
+                if (e < e1) {
+                    v = __ldg(a.pcol + st + e);
+                    claimed = push_edge(a, N, v, ou, kPersist);
+                }
+                append_claims(a, NQ, nq_slot, claimed, v, lvl, cn, cmo, cmi);
+            }
+        }
     }
     cn = warp_sum(cn);
     cmo = warp_sum(cmo);
@@ -416,6 +478,7 @@ __global__ void k_decide(BfsArgs a, int forced, cudaGraphConditionalHandle sw) {
         a.ctl->acc_mi[k] = 0;
         a.ctl->acc_full[k] = 0;
         a.ctl->acc_bytes[k] = 0;
+        a.ctl->nbig[k] = 0;
         a.ctl->qn[k] = 0;
         unsigned branch;
         if (dir == ALB_DIR_TOPDOWN)
@@ -437,6 +500,10 @@ __global__ void k_td(BfsArgs a) {
     td_phase<false>(a, a.ctl->level, Range{(int)blockIdx.x, (int)gridDim.x});
 }
 
+__global__ void k_td_big(BfsArgs a) {
+    td_big_phase<false>(a, a.ctl->level, Range{(int)blockIdx.x, (int)gridDim.x});
+}
+
 __global__ void k_td_finish(BfsArgs a) {
     td_finish_phase<false>(a, a.ctl->level, Range{(int)blockIdx.x, (int)gridDim.x});
 }
@@ -452,7 +519,7 @@ __global__ void k_end(BfsArgs a, cudaGraphConditionalHandle wh) {
     const int k = (c.level + 1) % 3;
     if (a.trace && c.level < c.trace_cap)
         a.trace[c.level].bytes = level_bytes(c, c.dir, c.acc_n[k], c.acc_bytes[k]);
-    c.launches += 2 + (c.branch == 1 ? 3 : c.branch == 0 ? 2 : 1);  // decide, end, steps
+    c.launches += 2 + (c.branch == 1 ? 4 : c.branch == 0 ? 3 : 1);  // decide, end, steps
     roll(c, c.dir, c.acc_n[k], c.acc_mo[k], c.acc_mi[k], c.acc_full[k]);
     if (c.level < c.trace_cap) c.trace_len = c.level;
     else c.trace_len = c.trace_cap;
@@ -519,6 +586,7 @@ __global__ void __launch_bounds__(256) k_persistent(BfsArgs a) {
                     a.ctl->acc_mi[k] = 0;
                     a.ctl->acc_full[k] = 0;
                     a.ctl->acc_bytes[k] = 0;
+                    a.ctl->nbig[k] = 0;
                     a.ctl->qn[k] = 0;
                 }
             }
@@ -534,6 +602,10 @@ __global__ void __launch_bounds__(256) k_persistent(BfsArgs a) {
             }
             if (ok) {
                 td_phase<true>(a, L, r);
+                ok = grid_sync(a.ctl, nb);
+            }
+            if (ok && *(volatile unsigned long long *)&a.ctl->nbig[L % 3]) {
+                td_big_phase<true>(a, L, r);
                 ok = grid_sync(a.ctl, nb);
             }
             if (ok) {
@@ -603,6 +675,7 @@ alb_status bfs_scratch_alloc(alb_graph *g) {
     ALB_TRY(dmalloc((void **)&b.vis, sizeof(uint32_t) * nw, "visited bitmap"));
     ALB_TRY(dmalloc((void **)&b.q0, sizeof(int32_t) * n, "frontier queue"));
     ALB_TRY(dmalloc((void **)&b.q1, sizeof(int32_t) * n, "frontier queue"));
+    ALB_TRY(dmalloc((void **)&b.big, sizeof(int32_t) * n, "long-row list"));
     ALB_TRY(dmalloc((void **)&b.level_pos, sizeof(int32_t) * n, "levels"));
     ALB_TRY(dmalloc((void **)&b.parent_pos, sizeof(uint32_t) * n, "parents"));
     ALB_TRY(dmalloc((void **)&b.ctl, sizeof(BfsCtl), "level control"));
@@ -620,6 +693,7 @@ void bfs_scratch_free(alb_graph *g) {
     dfree(b.vis);
     dfree(b.q0);
     dfree(b.q1);
+    dfree(b.big);
     dfree(b.level_pos);
     dfree(b.parent_pos);
     dfree(b.out_level);
@@ -640,6 +714,11 @@ void loop_cache_free(alb_graph *g) {
 
 extern const float *selector_device_params(int which);
 extern bool selector_host_params(int which, float *out);
+
+float skew_of(const Sell &s, int64_t n) {
+    const double mean = n > 0 ? (double)s.m_in / (double)n : 0.0;
+    return mean > 0 ? (float)std::log2(1.0 + (double)s.max_deg / mean) : 0.0f;
+}
 
 BfsArgs make_args(alb_graph *g) {
     const Sell &s = g->sell;
@@ -666,6 +745,7 @@ BfsArgs make_args(alb_graph *g) {
     a.vis = b.vis;
     a.q0 = b.q0;
     a.q1 = b.q1;
+    a.big = b.big;
     a.level_pos = b.level_pos;
     a.parent_pos = b.parent_pos;
     a.ctl = b.ctl;
@@ -735,16 +815,18 @@ alb_status build_loop_graph(alb_graph *g, int block) {
     void *aargs[] = {&a};
     {  // 0: top-down, queue ready
         cudaGraph_t b0 = sp.conditional.phGraph_out[0];
-        cudaGraphNode_t t, f;
+        cudaGraphNode_t t, bg, f;
         ALB_TRY(add_kernel_node(b0, &t, nullptr, 0, (void *)k_td, wide, aargs));
-        ALB_TRY(add_kernel_node(b0, &f, &t, 1, (void *)k_td_finish, wide, aargs));
+        ALB_TRY(add_kernel_node(b0, &bg, &t, 1, (void *)k_td_big, wide, aargs));
+        ALB_TRY(add_kernel_node(b0, &f, &bg, 1, (void *)k_td_finish, wide, aargs));
     }
     {  // 1: compaction / clear, then top-down
         cudaGraph_t b1 = sp.conditional.phGraph_out[1];
-        cudaGraphNode_t pr, t, f;
+        cudaGraphNode_t pr, t, bg, f;
         ALB_TRY(add_kernel_node(b1, &pr, nullptr, 0, (void *)k_prep, wide, aargs));
         ALB_TRY(add_kernel_node(b1, &t, &pr, 1, (void *)k_td, wide, aargs));
-        ALB_TRY(add_kernel_node(b1, &f, &t, 1, (void *)k_td_finish, wide, aargs));
+        ALB_TRY(add_kernel_node(b1, &bg, &t, 1, (void *)k_td_big, wide, aargs));
+        ALB_TRY(add_kernel_node(b1, &f, &bg, 1, (void *)k_td_finish, wide, aargs));
     }
     {  // 2: bottom-up with bypass
         cudaGraphNode_t b;
@@ -794,6 +876,7 @@ alb_status run_host_loop(alb_graph *g, const BfsArgs &a, const alb_bfs_opts &o,
         if (dir == ALB_DIR_TOPDOWN) {
             if (!h->q_valid || h->n_dirty) k_prep<<<wide.grid, wide.block, 0, st>>>(a);
             k_td<<<wide.grid, wide.block, 0, st>>>(a);
+            k_td_big<<<wide.grid, wide.block, 0, st>>>(a);
             k_td_finish<<<wide.grid, wide.block, 0, st>>>(a);
         } else if (dir == ALB_DIR_BOTTOMUP) {
             k_bu<true, true><<<wide.grid, wide.block, 0, st>>>(a);
@@ -828,10 +911,6 @@ alb_status run_persistent(alb_graph *g, const BfsArgs &a) {
     return ALB_OK;
 }
 
-float skew_feature(const Sell &s, int64_t n) {
-    const double mean = n > 0 ? (double)s.m_in / (double)n : 0.0;
-    return mean > 0 ? (float)std::log2(1.0 + (double)s.max_deg / mean) : 0.0f;
-}
 
 alb_status bfs_impl(alb_graph *g, int32_t root, const alb_bfs_opts &o, int32_t *d_level,
                     int32_t *d_parent, alb_stats *st) {
@@ -847,7 +926,7 @@ alb_status bfs_impl(alb_graph *g, int32_t root, const alb_bfs_opts &o, int32_t *
     ip.alpha = o.alpha;
     ip.beta = o.beta;
     ip.mean_deg = g->n > 0 ? (float)((double)s.m_in / (double)g->n) : 0.f;
-    ip.skew = skew_feature(s, g->n);
+    ip.skew = skew_of(s, g->n);
     ip.n_live = g->n - s.zero_in;
     ip.m_in = s.m_in;
     ip.active0 = s.active0;
@@ -898,6 +977,134 @@ alb_status bfs_impl(alb_graph *g, int32_t root, const alb_bfs_opts &o, int32_t *
         st->kernels = 2 + ((d_level || d_parent) ? 1 : 0) +
                       (o.loop == ALB_LOOP_PERSISTENT ? 1 : c.launches);
     }
+    return ALB_OK;
+}
+
+// Launch the step kernels of one variant for the current level.
+void launch_step(const BfsArgs &a, const Launch &wide, cudaStream_t st, int dir, const BfsCtl &h) {
+    if (dir == ALB_DIR_TOPDOWN) {
+        if (!h.q_valid || h.n_dirty) k_prep<<<wide.grid, wide.block, 0, st>>>(a);
+        k_td<<<wide.grid, wide.block, 0, st>>>(a);
+        k_td_big<<<wide.grid, wide.block, 0, st>>>(a);
+        k_td_finish<<<wide.grid, wide.block, 0, st>>>(a);
+    } else if (dir == ALB_DIR_BOTTOMUP) {
+        k_bu<true, true><<<wide.grid, wide.block, 0, st>>>(a);
+    } else {
+        k_bu<false, false><<<wide.grid, wide.block, 0, st>>>(a);
+    }
+}
+
+// Device copies of the state a level step mutates (restored between variants).
+struct LevelSnapshot {
+    uint32_t *vis = nullptr, *b0 = nullptr, *b1 = nullptr;
+    BfsCtl *ctl = nullptr;
+    ~LevelSnapshot() {
+        dfree(vis);
+        dfree(b0);
+        dfree(b1);
+        dfree(ctl);
+    }
+};
+
+alb_status profile_impl(alb_graph *g, int32_t root, const alb_bfs_opts &o, int32_t cap,
+                        alb_level_profile *out, int32_t *count) {
+    ALB_TRY(bfs_scratch_alloc(g));
+    const BfsArgs a = make_args(g);
+    const Sell &s = g->sell;
+    cudaStream_t st = g->stream;
+    const int64_t nw = s.nwords;
+    LevelSnapshot snap;
+    ALB_TRY(dmalloc((void **)&snap.vis, 4 * nw, "snapshot"));
+    ALB_TRY(dmalloc((void **)&snap.b0, 4 * nw, "snapshot"));
+    ALB_TRY(dmalloc((void **)&snap.b1, 4 * nw, "snapshot"));
+    ALB_TRY(dmalloc((void **)&snap.ctl, sizeof(BfsCtl), "snapshot"));
+    InitParams ip;
+    std::memset(&ip, 0, sizeof(ip));
+    ip.root = root;
+    ip.policy = o.policy;
+    ip.trace_cap = 0;
+    ip.level_cap = (int32_t)std::min<int64_t>(g->n + 1, INT32_MAX - 1);
+    ip.alpha = o.alpha;
+    ip.beta = o.beta;
+    ip.mean_deg = g->n > 0 ? (float)((double)s.m_in / (double)g->n) : 0.f;
+    ip.skew = skew_of(s, g->n);
+    ip.n_live = g->n - s.zero_in;
+    ip.m_in = s.m_in;
+    ip.active0 = s.active0;
+    const Launch wide = level_launch(g, o.block);
+    k_init_bulk<<<wide.grid, wide.block, 0, st>>>(a);
+    k_init_root<<<1, 32, 0, st>>>(a, ip);
+    ALB_CK(cudaGetLastError());
+    BfsCtl *h = g->bfs.h_ctl;
+    ALB_CK(cudaMemcpyAsync(h, a.ctl, sizeof(BfsCtl), cudaMemcpyDeviceToHost, st));
+    ALB_CK(cudaStreamSynchronize(st));
+    cudaEvent_t e0, e1;
+    ALB_CK(cudaEventCreate(&e0));
+    ALB_CK(cudaEventCreate(&e1));
+    auto save = [&](bool back) -> alb_status {
+        auto cp = [&](void *dst, const void *src, size_t bytes) {
+            return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st);
+        };
+        cudaError_t e = back ? cp(a.vis, snap.vis, 4 * nw) : cp(snap.vis, a.vis, 4 * nw);
+        if (e == cudaSuccess) e = back ? cp(a.bm0, snap.b0, 4 * nw) : cp(snap.b0, a.bm0, 4 * nw);
+        if (e == cudaSuccess) e = back ? cp(a.bm1, snap.b1, 4 * nw) : cp(snap.b1, a.bm1, 4 * nw);
+        if (e == cudaSuccess)
+            e = back ? cp(a.ctl, snap.ctl, sizeof(BfsCtl)) : cp(snap.ctl, a.ctl, sizeof(BfsCtl));
+        if (e != cudaSuccess) return fail(ALB_ERR_CUDA, "profile snapshot: %s", cudaGetErrorString(e));
+        return ALB_OK;
+    };
+    int32_t cnt = 0;
+    alb_status rc = ALB_OK;
+    while (!h->done && rc == ALB_OK) {
+        const BfsCtl hc = *h;
+        alb_level_profile prof;
+        std::memset(&prof, 0, sizeof(prof));
+        rc = save(false);
+        for (int v = 0; v < 3 && rc == ALB_OK; v++) {
+            if (v) rc = save(true);
+            k_decide<<<1, 32, 0, st>>>(a, v, 0);
+            cudaEventRecord(e0, st);
+            launch_step(a, wide, st, v, hc);
+            cudaEventRecord(e1, st);
+            cudaError_t e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) rc = fail(ALB_ERR_CUDA, "profile step: %s", cudaGetErrorString(e));
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            prof.us[v] = ms * 1000.f;
+        }
+        if (rc != ALB_OK) break;
+        int best = 0;
+        for (int v = 1; v < 3; v++)
+            if (prof.us[v] < prof.us[best]) best = v;
+        rc = save(true);
+        if (rc != ALB_OK) break;
+        k_decide<<<1, 32, 0, st>>>(a, best, 0);
+        launch_step(a, wide, st, best, hc);
+        k_end<<<1, 32, 0, st>>>(a, 0);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h, a.ctl, sizeof(BfsCtl), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            rc = fail(ALB_ERR_CUDA, "profile level: %s", cudaGetErrorString(e));
+            break;
+        }
+        prof.best = best;
+        prof.rec.dir = best;
+        prof.rec.level = hc.level;
+        prof.rec.nf = hc.nf;
+        prof.rec.mf = hc.mf;
+        prof.rec.nu = hc.nu;
+        prof.rec.mu = hc.mu;
+        prof.rec.active_slices = hc.active_words;
+        prof.rec.step_us = prof.us[best];
+        level_features(hc, prof.feat);
+        if (cnt < cap && out) out[cnt] = prof;
+        cnt++;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != ALB_OK) return rc;
+    *count = cnt;
     return ALB_OK;
 }
 
@@ -972,6 +1179,19 @@ alb_status alb_bfs(alb_graph *g, int32_t root, const alb_bfs_opts *o, int32_t *l
                                g->stream));
     ALB_CK(cudaStreamSynchronize(g->stream));
     return ALB_OK;
+}
+
+alb_status alb_bfs_profile(alb_graph *g, int32_t root, const alb_bfs_opts *o, int32_t cap,
+                           alb_level_profile *out, int32_t *count) {
+    alb_bfs_opts oo;
+    ALB_TRY(check_bfs_args(g, root, o, oo));
+    if (!count || (cap > 0 && !out)) return fail(ALB_ERR_INVALID, "alb_bfs_profile: bad output");
+    ALB_CK(cudaSetDevice(g->device));
+    try {
+        return profile_impl(g, root, oo, cap, out, count);
+    } catch (const std::bad_alloc &) {
+        return fail(ALB_ERR_OOM, "alb_bfs_profile: host allocation failed");
+    }
 }
 
 alb_status alb_level_trace(const alb_graph *g, int32_t cap, alb_level_rec *out, int32_t *count) {

@@ -9,6 +9,10 @@
 namespace alb {
 
 constexpr uint32_t kFull = 0xFFFFFFFFu;
+// Top-down: rows longer than kBigRow are pushed in kBigChunk-edge chunks
+// shared by every warp instead of by the one warp that dequeued them.
+constexpr int64_t kBigRow = 1024;
+constexpr int64_t kBigChunk = 1024;
 
 // ---------------------------------------------------------------- loads
 // Column and structure arrays are read-only for a whole traversal: read them
@@ -79,6 +83,7 @@ struct BfsCtl {
     int64_t active_words;    // bitmap words with an unvisited row
     int64_t reached, edges;  // running totals
     unsigned long long acc_n[3], acc_mo[3], acc_mi[3], acc_full[3], qn[3], acc_bytes[3];
+    unsigned long long nbig[3];  // rows too long for one warp, per level slot
     unsigned int bar_count, bar_gen;  // persistent-kernel grid barrier
     int32_t trace_cap, trace_len;
     int32_t level_cap;       // safety bound on the number of levels
@@ -104,6 +109,7 @@ struct BfsArgs {
     uint32_t *bm0, *bm1;       // frontier bitmaps (by level parity)
     uint32_t *vis;             // visited bitmap
     int32_t *q0, *q1;          // frontier queues (by level parity)
+    int32_t *big;              // frontier rows split across all warps (top-down)
     int32_t *level_pos;        // depth by position
     uint32_t *parent_pos;      // parent original id by position
     BfsCtl *ctl;

@@ -318,42 +318,57 @@ __global__ void k_widths(int64_t n, int64_t nslices, int32_t C, const int32_t *i
     ssize[s] = (int64_t)C * ((w + 3) & ~3);
 }
 
-// Fill the 4-interleaved SELL columns, one thread per (padded) row.
+// Fill the 4-interleaved SELL columns, one warp per (padded) row: lanes
+// stride over the CSR row, a ballot prefix drops self-loops in order.
 __global__ void k_fill_sell(int64_t n, int64_t npad, int32_t C, int32_t log2C,
                             const int32_t *perm, const int32_t *inv, const int32_t *width,
                             const int64_t *slice_off, const int64_t *rp, const int32_t *col,
                             int32_t *scol) {
-    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (p >= npad) return;
-    const int64_t s = p >> log2C;
-    const int32_t r = (int32_t)(p & (C - 1));
-    const int32_t w4 = (width[s] + 3) & ~3;
-    int32_t *base = scol + slice_off[s] + r * 4;
-    int32_t k = 0;
-    if (p < n) {
-        const int32_t v = perm[p];
-        for (int64_t e = rp[v]; e < rp[v + 1]; e++) {
-            int32_t c = col[e];
-            if (c == v) continue;
-            base[(int64_t)(k >> 2) * 4 * C + (k & 3)] = inv[c];
-            k++;
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t p = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); p < npad;
+         p += nw) {
+        const int64_t s = p >> log2C;
+        const int32_t r = (int32_t)(p & (C - 1));
+        const int32_t w4 = (width[s] + 3) & ~3;
+        int32_t *base = scol + slice_off[s] + r * 4;
+        int32_t k = 0;
+        if (p < n) {
+            const int32_t v = perm[p];
+            const int64_t b = rp[v], e = rp[v + 1];
+            for (int64_t i = b; i - lane < e; i += 32) {
+                const int32_t c = i < e ? col[i] : v;
+                const bool keep = c != v;
+                const unsigned m = __ballot_sync(kFull, keep);
+                if (keep) {
+                    const int32_t kk = k + __popc(m & lanemask_lt());
+                    base[(int64_t)(kk >> 2) * 4 * C + (kk & 3)] = inv[c];
+                }
+                k += __popc(m);
+            }
         }
+        const int32_t pad = p < n ? (int32_t)p : 0;
+        for (int32_t kk = k + lane; kk < w4; kk += 32) base[(int64_t)(kk >> 2) * 4 * C + (kk & 3)] = pad;
     }
-    const int32_t pad = p < n ? (int32_t)p : 0;
-    for (; k < w4; k++) base[(int64_t)(k >> 2) * 4 * C + (k & 3)] = pad;
 }
 
-// Push-side CSR in position space.
+// Push-side CSR in position space, one warp per row.
 __global__ void k_fill_push(int64_t n, const int32_t *perm, const int32_t *inv,
                             const int64_t *prow, const int64_t *rp, const int32_t *col,
                             int32_t *pcol) {
-    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    const int32_t v = perm[p];
-    int64_t at = prow[p];
-    for (int64_t e = rp[v]; e < rp[v + 1]; e++) {
-        int32_t c = col[e];
-        if (c != v) pcol[at++] = inv[c];
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t p = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); p < n; p += nw) {
+        const int32_t v = perm[p];
+        int64_t at = prow[p];
+        const int64_t b = rp[v], e = rp[v + 1];
+        for (int64_t i = b; i - lane < e; i += 32) {
+            const int32_t c = i < e ? col[i] : v;
+            const bool keep = c != v;
+            const unsigned m = __ballot_sync(kFull, keep);
+            if (keep) pcol[at + __popc(m & lanemask_lt())] = inv[c];
+            at += __popc(m);
+        }
     }
 }
 
@@ -393,6 +408,7 @@ alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma) {
     free_sell(g->sell);
     loop_cache_free(g);
     bfs_scratch_free(g);  // bitmap sizes depend on C
+    ms_scratch_free(g);
     Sell &s = g->sell;
     s.C = C;
     s.log2C = C == 8 ? 3 : C == 16 ? 4 : C == 32 ? 5 : 6;
@@ -465,10 +481,11 @@ alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma) {
                         "SELL columns"));
         ALB_TRY(dmalloc((void **)&s.pcol, sizeof(int32_t) * (size_t)std::max<int64_t>(s.m_out, 1),
                         "push columns"));
-        k_fill_sell<<<grid_for(npad, T), T, 0, st>>>(n, npad, C, s.log2C, s.perm, s.inv, s.width,
-                                                     s.slice_off, g->rp_in, g->col_in, s.col);
-        k_fill_push<<<grid_for(n, T), T, 0, st>>>(n, s.perm, s.inv, s.prow, g->rp_out, g->col_out,
-                                                  s.pcol);
+        const unsigned fill_grid = (unsigned)(g->num_sms * 8);
+        k_fill_sell<<<fill_grid, T, 0, st>>>(n, npad, C, s.log2C, s.perm, s.inv, s.width,
+                                             s.slice_off, g->rp_in, g->col_in, s.col);
+        k_fill_push<<<fill_grid, T, 0, st>>>(n, s.perm, s.inv, s.prow, g->rp_out, g->col_out,
+                                             s.pcol);
         k_vinit<<<grid_for(s.nwords, T), T, 0, st>>>(n, s.nwords, s.ideg, s.vinit, dcnt);
         ALB_CK(cudaGetLastError());
         unsigned long long hc[3];
@@ -531,6 +548,7 @@ void alb_graph_destroy(alb_graph *g) {
     if (g->stream) cudaStreamSynchronize(g->stream);
     loop_cache_free(g);
     bfs_scratch_free(g);
+    ms_scratch_free(g);
     free_sell(g->sell);
     if (g->col_out != g->col_in) dfree(g->col_out);
     if (g->rp_out != g->rp_in) dfree(g->rp_out);

@@ -55,6 +55,7 @@ struct BfsScratch {
     bool ready = false;
     uint32_t *bm0 = nullptr, *bm1 = nullptr, *vis = nullptr;
     int32_t *q0 = nullptr, *q1 = nullptr;
+    int32_t *big = nullptr;
     int32_t *level_pos = nullptr;
     uint32_t *parent_pos = nullptr;
     int32_t *out_level = nullptr, *out_parent = nullptr;  // staging for host outputs
@@ -83,6 +84,7 @@ struct alb_graph {
     alb::Sell sell;
     alb::BfsScratch bfs;
     alb::CachedLoop *loop = nullptr;
+    void *ms = nullptr;  // 64-root BFS scratch (msbfs.cu)
     std::vector<alb_level_rec> last_trace;
     bool last_trace_valid = false;
 };
@@ -90,6 +92,8 @@ struct alb_graph {
 namespace alb {
 alb_status bfs_scratch_alloc(alb_graph *g);
 void bfs_scratch_free(alb_graph *g);
+void ms_scratch_free(alb_graph *g);
+float skew_of(const Sell &s, int64_t n);
 void loop_cache_free(alb_graph *g);
 BfsArgs make_args(alb_graph *g);
 }  // namespace alb

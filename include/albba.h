@@ -183,6 +183,22 @@ typedef struct {
 alb_status alb_level_trace(const alb_graph *g, int32_t cap, alb_level_rec *out,
                            int32_t *count);
 
+/* ------------------------------------------------------ 64-root batched BFS */
+
+/* Bit-parallel BFS from up to 64 roots at once (one uint64 frontier/visited
+ * word per vertex, one traversal of the matrix per level for all roots).
+ * levels (host, n * 64 int32) is vertex-major: levels[v * 64 + i] = depth of
+ * v from roots[i], -1 if unreached (and for i >= nroots). The level loop is
+ * host-driven (one small device-to-host read per level); the direction of
+ * each level is decided on the device (policy as for alb_bfs; the learned
+ * policy uses selector 1). stats: reached = (vertex, root) pairs reached,
+ * edges = sum over roots of push-side entries in the root's component. */
+alb_status alb_msbfs64(alb_graph *g, const int32_t *roots, int32_t nroots,
+                       const alb_bfs_opts *o, int32_t *levels, alb_stats *st);
+/* Same with a device output buffer of n * 64 int32 (may be NULL). */
+alb_status alb_msbfs64_device(alb_graph *g, const int32_t *roots, int32_t nroots,
+                              const alb_bfs_opts *o, int32_t *d_levels, alb_stats *st);
+
 /* --------------------------------------------------------------- selector */
 
 /* Load the 1,443 fp32 parameters of a direction-selector MLP
@@ -192,6 +208,37 @@ alb_status alb_level_trace(const alb_graph *g, int32_t cap, alb_level_rec *out,
 alb_status alb_selector_load(int32_t which, const float *params);
 /* Forget loaded weights (ALB_POLICY_LEARNED falls back to Beamer). */
 alb_status alb_selector_clear(int32_t which);
+
+/* Per-level oracle timings. At every level each variant (ALB_DIR_*) runs
+ * from the same state (restored between runs) and its step kernels are timed
+ * with CUDA events; the traversal then continues with the fastest. Levels and
+ * parents are those of alb_bfs; this is the selector's training data and the
+ * judge of its regret. */
+typedef struct {
+    alb_level_rec rec; /* statistics at the start of the level */
+    float feat[8];     /* the selector's eight features for this level */
+    float us[3];       /* step time of each variant, microseconds */
+    int32_t best;      /* fastest variant (the one the traversal took) */
+} alb_level_profile;
+
+alb_status alb_bfs_profile(alb_graph *g, int32_t root, const alb_bfs_opts *o, int32_t cap,
+                           alb_level_profile *out, int32_t *count);
+alb_status alb_msbfs64_profile(alb_graph *g, const int32_t *roots, int32_t nroots,
+                               const alb_bfs_opts *o, int32_t cap, alb_level_profile *out,
+                               int32_t *count);
+
+/* The selector's hand-written CUDA kernels, callable on host arrays:
+ * forward (batch x 8 -> batch x 3), loss + gradient (masked squared error,
+ * mean over the batch), one Adam step, and full-batch Adam training
+ * (He initialisation from seed when init != 0, else params is the start). */
+alb_status alb_mlp_forward(const float *params, const float *x, int32_t batch, float *out);
+alb_status alb_mlp_loss_grad(const float *params, const float *x, const float *y,
+                             const float *mask, int32_t batch, float *grad, float *loss);
+alb_status alb_adam_step(float *params, const float *grad, float *m, float *v, int32_t t,
+                         float lr, float beta1, float beta2, float eps);
+alb_status alb_selector_train(const float *x, const float *y, const float *mask, int32_t batch,
+                              int32_t steps, float lr, uint64_t seed, int32_t init,
+                              float *params, float *loss);
 
 /* ---------------------------------------------------------------- testing */
 
