@@ -48,11 +48,12 @@ DIR_TOPDOWN, DIR_BOTTOMUP, DIR_BOTTOMUP_NOBYPASS = 0, 1, 2
 EXPORTED = [
     "alb_last_error", "alb_version", "alb_graph_create", "alb_graph_create32",
     "alb_graph_destroy", "alb_graph_info", "alb_graph_set_stream", "alb_sell_opts_default", "alb_sell_build",
-    "alb_sell_export", "alb_bfs_opts_default", "alb_bfs", "alb_bfs_device",
+    "alb_sell_export", "alb_sell_long_export", "alb_bfs_opts_default", "alb_bfs", "alb_bfs_device",
     "alb_level_trace", "alb_debug_fail_alloc_after", "alb_gen_rmat", "alb_gen_grid",
     "alb_gen_er", "alb_csr_from_edges", "alb_pick_roots", "alb_host_csr_free",
     "alb_cbd_write", "alb_cbd_read", "alb_selector_load", "alb_selector_clear",
-    "alb_msbfs64", "alb_msbfs64_device",
+    "alb_msbfs64", "alb_msbfs64_device", "alb_bfs_profile", "alb_msbfs64_profile",
+    "alb_mlp_forward", "alb_mlp_loss_grad", "alb_adam_step", "alb_selector_train",
 ]
 
 
@@ -64,7 +65,7 @@ class AlbError(RuntimeError):
 
 # ------------------------------------------------------------------- structs
 class SellOpts(C.Structure):
-    _fields_ = [("C", C.c_int32), ("sigma", C.c_int32)]
+    _fields_ = [("C", C.c_int32), ("sigma", C.c_int32), ("long_row", C.c_int32)]
 
 
 class BfsOpts(C.Structure):
@@ -88,6 +89,11 @@ class LevelRec(C.Structure):
                 ("pad_", C.c_int32)]
 
 
+class LevelProfile(C.Structure):
+    _fields_ = [("rec", LevelRec), ("feat", C.c_float * 8), ("us", C.c_float * 3),
+                ("best", C.c_int32)]
+
+
 class HostCsr(C.Structure):
     _fields_ = [("n", C.c_int64), ("nnz", C.c_int64), ("rowptr", C.POINTER(C.c_int64)),
                 ("col", C.POINTER(C.c_int32))]
@@ -108,6 +114,7 @@ _sigs = {
     "alb_sell_opts_default": (None, [C.POINTER(SellOpts)]),
     "alb_sell_build": (C.c_int32, [_P, C.POINTER(SellOpts), C.POINTER(C.c_double)]),
     "alb_sell_export": (C.c_int32, [_P, _i64p, _P, _P, _P, _P]),
+    "alb_sell_long_export": (C.c_int32, [_P, _i64p, _P, _P, _P]),
     "alb_bfs_opts_default": (None, [C.POINTER(BfsOpts)]),
     "alb_bfs": (C.c_int32, [_P, C.c_int32, C.POINTER(BfsOpts), _P, _P, C.POINTER(Stats)]),
     "alb_bfs_device": (C.c_int32, [_P, C.c_int32, C.POINTER(BfsOpts), _P, _P, C.POINTER(Stats)]),
@@ -126,6 +133,16 @@ _sigs = {
     "alb_msbfs64": (C.c_int32, [_P, _P, C.c_int32, C.POINTER(BfsOpts), _P, C.POINTER(Stats)]),
     "alb_msbfs64_device": (C.c_int32, [_P, _P, C.c_int32, C.POINTER(BfsOpts), _P,
                                        C.POINTER(Stats)]),
+    "alb_bfs_profile": (C.c_int32, [_P, C.c_int32, C.POINTER(BfsOpts), C.c_int32,
+                                    C.POINTER(LevelProfile), _i32p]),
+    "alb_msbfs64_profile": (C.c_int32, [_P, _P, C.c_int32, C.POINTER(BfsOpts), C.c_int32,
+                                        C.POINTER(LevelProfile), _i32p]),
+    "alb_mlp_forward": (C.c_int32, [_P, _P, C.c_int32, _P]),
+    "alb_mlp_loss_grad": (C.c_int32, [_P, _P, _P, _P, C.c_int32, _P, C.POINTER(C.c_float)]),
+    "alb_adam_step": (C.c_int32, [_P, _P, _P, _P, C.c_int32, C.c_float, C.c_float, C.c_float,
+                                  C.c_float]),
+    "alb_selector_train": (C.c_int32, [_P, _P, _P, C.c_int32, C.c_int32, C.c_float, C.c_uint64,
+                                       C.c_int32, _P, C.POINTER(C.c_float)]),
     "alb_selector_load": (C.c_int32, [C.c_int32, _P]),
     "alb_selector_clear": (C.c_int32, [C.c_int32]),
 }
@@ -312,8 +329,9 @@ class Graph:
         """Run on a caller stream (e.g. torch.cuda.current_stream().cuda_stream)."""
         check(_lib.alb_graph_set_stream(self._h, cuda_stream))
 
-    def sell_build(self, C_: int = 32, sigma: int = 1024) -> float:
-        o = SellOpts(C_, sigma)
+    def sell_build(self, C_: int = 32, sigma: int = 1024, long_row: int = 256) -> float:
+        """Build SELL-C-sigma on the device; returns the build time in ms."""
+        o = SellOpts(C_, sigma, long_row)
         ms = C.c_double()
         check(_lib.alb_sell_build(self._h, C.byref(o), C.byref(ms)))
         return ms.value
@@ -329,6 +347,16 @@ class Graph:
         check(_lib.alb_sell_export(self._h, None, perm.ctypes.data, width.ctypes.data, None,
                                    col.ctypes.data))
         return SellExport(ns.value, perm, width, off, col)
+
+    def sell_long_export(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        nl = C.c_int64()
+        check(_lib.alb_sell_long_export(self._h, C.byref(nl), None, None, None))
+        lrow = np.empty(max(nl.value, 1), np.int32)
+        lptr = np.empty(nl.value + 1, np.int64)
+        check(_lib.alb_sell_long_export(self._h, None, lrow.ctypes.data, lptr.ctypes.data, None))
+        lcol = np.empty(max(int(lptr[-1]), 1), np.int32)
+        check(_lib.alb_sell_long_export(self._h, None, None, None, lcol.ctypes.data))
+        return lrow[: nl.value], lptr, lcol[: int(lptr[-1])]
 
     def bfs(self, root: int, opts: BfsOpts | None = None, want_level: bool = True,
             want_parent: bool = True) -> tuple[np.ndarray | None, np.ndarray | None, Stats]:
@@ -365,12 +393,71 @@ class Graph:
                                       _ptr(d_levels), C.byref(st)))
         return st
 
+    def bfs_profile(self, root: int, opts: BfsOpts | None = None) -> list[LevelProfile]:
+        """Per-level step times of all three variants (see alb_bfs_profile)."""
+        o = opts or bfs_opts()
+        cnt = C.c_int32()
+        cap = 4096
+        buf = (LevelProfile * cap)()
+        check(_lib.alb_bfs_profile(self._h, int(root), C.byref(o), cap, buf, C.byref(cnt)))
+        return list(buf[: min(cnt.value, cap)])
+
+    def msbfs64_profile(self, roots, opts: BfsOpts | None = None) -> list[LevelProfile]:
+        r = np.ascontiguousarray(roots, dtype=np.int32)
+        o = opts or bfs_opts()
+        cnt = C.c_int32()
+        cap = 4096
+        buf = (LevelProfile * cap)()
+        check(_lib.alb_msbfs64_profile(self._h, r.ctypes.data, r.shape[0], C.byref(o), cap, buf,
+                                       C.byref(cnt)))
+        return list(buf[: min(cnt.value, cap)])
+
     def level_trace(self) -> list[LevelRec]:
         cnt = C.c_int32()
         check(_lib.alb_level_trace(self._h, 0, None, C.byref(cnt)))
         buf = (LevelRec * max(cnt.value, 1))()
         check(_lib.alb_level_trace(self._h, cnt.value, buf, C.byref(cnt)))
         return list(buf[: cnt.value])
+
+
+NPARAM = 1443
+
+
+def mlp_forward(params, x) -> np.ndarray:
+    p = np.ascontiguousarray(params, np.float32)
+    xx = np.ascontiguousarray(x, np.float32)
+    out = np.empty((xx.shape[0], 3), np.float32)
+    check(_lib.alb_mlp_forward(p.ctypes.data, xx.ctypes.data, xx.shape[0], out.ctypes.data))
+    return out
+
+
+def mlp_loss_grad(params, x, y, mask) -> tuple[float, np.ndarray]:
+    p = np.ascontiguousarray(params, np.float32)
+    xx, yy, mm = (np.ascontiguousarray(a, np.float32) for a in (x, y, mask))
+    g = np.empty(NPARAM, np.float32)
+    loss = C.c_float()
+    check(_lib.alb_mlp_loss_grad(p.ctypes.data, xx.ctypes.data, yy.ctypes.data, mm.ctypes.data,
+                                 xx.shape[0], g.ctypes.data, C.byref(loss)))
+    return loss.value, g
+
+
+def adam_step(params, grad, m, v, t, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8) -> None:
+    """In place on params, m, v (float32 numpy arrays), on the GPU."""
+    g = np.ascontiguousarray(grad, np.float32)
+    check(_lib.alb_adam_step(params.ctypes.data, g.ctypes.data, m.ctypes.data, v.ctypes.data,
+                             int(t), lr, b1, b2, eps))
+
+
+def selector_train(x, y, mask, steps: int = 3000, lr: float = 3e-3, seed: int = 0,
+                   params=None) -> tuple[np.ndarray, float]:
+    """Full-batch Adam on the GPU; He init from seed unless params is given."""
+    xx, yy, mm = (np.ascontiguousarray(a, np.float32) for a in (x, y, mask))
+    p = np.zeros(NPARAM, np.float32) if params is None else np.array(params, np.float32)
+    loss = C.c_float()
+    check(_lib.alb_selector_train(xx.ctypes.data, yy.ctypes.data, mm.ctypes.data, xx.shape[0],
+                                  steps, lr, seed, 1 if params is None else 0, p.ctypes.data,
+                                  C.byref(loss)))
+    return p, loss.value
 
 
 def selector_load(which: int, params: np.ndarray) -> None:

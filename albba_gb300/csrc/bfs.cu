@@ -372,6 +372,57 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r) {
     }
 }
 
+// Bottom-up pull of the long rows (kept out of the slices): one warp per row,
+// 32 sources per step; the lowest lane with a frontier hit in the first
+// step that has one is the earliest, i.e. smallest-id, source.
+template <bool kPersist, bool kEarly>
+__device__ void bu_long_phase(const BfsArgs &a, int L, Range r) {
+    if (a.nlong == 0) return;
+    const uint32_t *F = (L & 1) ? a.bm1 : a.bm0;
+    uint32_t *N = (L & 1) ? a.bm0 : a.bm1;
+    const int lane = threadIdx.x & 31;
+    const int64_t wpb = blockDim.x >> 5;
+    const int64_t nwarps = (int64_t)r.nblk * wpb;
+    unsigned long long cn = 0, cmo = 0, cmi = 0, full = 0, bytes = 0;
+    for (int64_t i = (int64_t)r.bid * wpb + (threadIdx.x >> 5); i < a.nlong; i += nwarps) {
+        const int32_t p = __ldg(a.lrow + i);
+        const uint32_t bit = 1u << (p & 31);
+        if (ld_bits<kPersist>(a.vis + (p >> 5)) & bit) continue;
+        const int64_t st = __ldg(a.lptr + i), en = __ldg(a.lptr + i + 1);
+        bytes += 16;
+        int32_t found = -1;
+        for (int64_t e0 = st; e0 < en; e0 += 32) {
+            const int64_t e = e0 + lane;
+            const int32_t c = e < en ? __ldg(a.lcol + e) : p;
+            const bool hit = (ld_bits<kPersist>(F + (c >> 5)) >> (c & 31)) & 1u;
+            const unsigned m = __ballot_sync(kFull, hit);
+            bytes += 128;
+            if (m && found < 0) found = __shfl_sync(kFull, c, __ffs(m) - 1);
+            if (kEarly && found >= 0) break;
+        }
+        if (found >= 0 && lane == 0) {
+            a.level_pos[p] = L + 1;
+            a.parent_pos[p] = (uint32_t)__ldg(a.perm + found);
+            atomicOr(N + (p >> 5), bit);
+            const uint32_t old = atomicOr(a.vis + (p >> 5), bit);
+            full += (old != kFull && (old | bit) == kFull);
+            cn++;
+            cmo += (unsigned long long)__ldg(a.odeg + p);
+            cmi += (unsigned long long)__ldg(a.ideg + p);
+        }
+    }
+    if (lane == 0 && (cn || full || bytes)) {
+        const int k = (L + 1) % 3;
+        if (cn) {
+            atomicAdd(&a.ctl->acc_n[k], cn);
+            atomicAdd(&a.ctl->acc_mo[k], cmo);
+            atomicAdd(&a.ctl->acc_mi[k], cmi);
+        }
+        if (full) atomicAdd(&a.ctl->acc_full[k], full);
+        if (bytes) atomicAdd(&a.ctl->acc_bytes[k], bytes);
+    }
+}
+
 // Algorithmic bytes of the level that just ran (see alb_level_rec).
 __host__ __device__ inline int64_t level_bytes(const BfsCtl &c, int dir, unsigned long long nn,
                                                unsigned long long counted) {
@@ -513,13 +564,18 @@ __global__ void k_bu(BfsArgs a) {
     bu_phase<false, kBypass, kEarly>(a, a.ctl->level, Range{(int)blockIdx.x, (int)gridDim.x});
 }
 
+template <bool kEarly>
+__global__ void k_bu_long(BfsArgs a) {
+    bu_long_phase<false, kEarly>(a, a.ctl->level, Range{(int)blockIdx.x, (int)gridDim.x});
+}
+
 __global__ void k_end(BfsArgs a, cudaGraphConditionalHandle wh) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     BfsCtl c = *a.ctl;
     const int k = (c.level + 1) % 3;
     if (a.trace && c.level < c.trace_cap)
         a.trace[c.level].bytes = level_bytes(c, c.dir, c.acc_n[k], c.acc_bytes[k]);
-    c.launches += 2 + (c.branch == 1 ? 4 : c.branch == 0 ? 3 : 1);  // decide, end, steps
+    c.launches += 2 + (c.branch == 1 ? 4 : c.branch == 0 ? 3 : 2);  // decide, end, steps
     roll(c, c.dir, c.acc_n[k], c.acc_mo[k], c.acc_mi[k], c.acc_full[k]);
     if (c.level < c.trace_cap) c.trace_len = c.level;
     else c.trace_len = c.trace_cap;
@@ -615,9 +671,17 @@ __global__ void __launch_bounds__(256) k_persistent(BfsArgs a) {
         } else if (dir == ALB_DIR_BOTTOMUP) {
             bu_phase<true, true, true>(a, L, r);
             ok = grid_sync(a.ctl, nb);
+            if (ok && a.nlong) {
+                bu_long_phase<true, true>(a, L, r);
+                ok = grid_sync(a.ctl, nb);
+            }
         } else {
             bu_phase<true, false, false>(a, L, r);
             ok = grid_sync(a.ctl, nb);
+            if (ok && a.nlong) {
+                bu_long_phase<true, false>(a, L, r);
+                ok = grid_sync(a.ctl, nb);
+            }
         }
         if (!ok) break;
         if (threadIdx.x == 0) {
@@ -739,6 +803,10 @@ BfsArgs make_args(alb_graph *g) {
     a.col4 = (const int4 *)s.col;
     a.prow = s.prow;
     a.pcol = s.pcol;
+    a.nlong = s.nlong;
+    a.lrow = s.lrow;
+    a.lptr = s.lptr;
+    a.lcol = s.lcol;
     a.vinit = s.vinit;
     a.bm0 = b.bm0;
     a.bm1 = b.bm1;
@@ -828,15 +896,19 @@ alb_status build_loop_graph(alb_graph *g, int block) {
         ALB_TRY(add_kernel_node(b1, &bg, &t, 1, (void *)k_td_big, wide, aargs));
         ALB_TRY(add_kernel_node(b1, &f, &bg, 1, (void *)k_td_finish, wide, aargs));
     }
-    {  // 2: bottom-up with bypass
-        cudaGraphNode_t b;
+    {  // 2: bottom-up with bypass, then the long rows
+        cudaGraphNode_t b, l;
         ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[2], &b, nullptr, 0,
                                 (void *)k_bu<true, true>, wide, aargs));
+        ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[2], &l, &b, 1,
+                                (void *)k_bu_long<true>, wide, aargs));
     }
-    {  // 3: bottom-up without bypass
-        cudaGraphNode_t b;
+    {  // 3: bottom-up without bypass, then the long rows
+        cudaGraphNode_t b, l;
         ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[3], &b, nullptr, 0,
                                 (void *)k_bu<false, false>, wide, aargs));
+        ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[3], &l, &b, 1,
+                                (void *)k_bu_long<false>, wide, aargs));
     }
     void *eargs[] = {&a, &wh};
     cudaGraphNode_t nend;
@@ -880,8 +952,10 @@ alb_status run_host_loop(alb_graph *g, const BfsArgs &a, const alb_bfs_opts &o,
             k_td_finish<<<wide.grid, wide.block, 0, st>>>(a);
         } else if (dir == ALB_DIR_BOTTOMUP) {
             k_bu<true, true><<<wide.grid, wide.block, 0, st>>>(a);
+            k_bu_long<true><<<wide.grid, wide.block, 0, st>>>(a);
         } else {
             k_bu<false, false><<<wide.grid, wide.block, 0, st>>>(a);
+            k_bu_long<false><<<wide.grid, wide.block, 0, st>>>(a);
         }
         if (e1) cudaEventRecord(e1, st);
         k_end<<<1, 32, 0, st>>>(a, 0);
@@ -989,8 +1063,10 @@ void launch_step(const BfsArgs &a, const Launch &wide, cudaStream_t st, int dir,
         k_td_finish<<<wide.grid, wide.block, 0, st>>>(a);
     } else if (dir == ALB_DIR_BOTTOMUP) {
         k_bu<true, true><<<wide.grid, wide.block, 0, st>>>(a);
+        k_bu_long<true><<<wide.grid, wide.block, 0, st>>>(a);
     } else {
         k_bu<false, false><<<wide.grid, wide.block, 0, st>>>(a);
+        k_bu_long<false><<<wide.grid, wide.block, 0, st>>>(a);
     }
 }
 

@@ -12,7 +12,7 @@ constexpr uint32_t kFull = 0xFFFFFFFFu;
 // Top-down: rows longer than kBigRow are pushed in kBigChunk-edge chunks
 // shared by every warp instead of by the one warp that dequeued them.
 constexpr int64_t kBigRow = 1024;
-constexpr int64_t kBigChunk = 1024;
+constexpr int64_t kBigChunk = 128;
 
 // ---------------------------------------------------------------- loads
 // Column and structure arrays are read-only for a whole traversal: read them
@@ -105,6 +105,10 @@ struct BfsArgs {
     const int4 *col4;          // SELL columns, 4-interleaved
     const int64_t *prow;       // push CSR (position space)
     const int32_t *pcol;
+    int64_t nlong;             // rows kept out of the slices (pulled per warp)
+    const int32_t *lrow;
+    const int64_t *lptr;
+    const int32_t *lcol;
     const uint32_t *vinit;     // initial visited mask
     uint32_t *bm0, *bm1;       // frontier bitmaps (by level parity)
     uint32_t *vis;             // visited bitmap

@@ -121,6 +121,9 @@ void free_sell(Sell &s) {
     dfree(s.prow);
     dfree(s.pcol);
     dfree(s.vinit);
+    dfree(s.lrow);
+    dfree(s.lptr);
+    dfree(s.lcol);
     s = Sell();
 }
 
@@ -304,15 +307,19 @@ __global__ void k_positions(int64_t n, const int32_t *perm, const int32_t *ilen,
     odeg[p] = olen[v];
 }
 
+__device__ __forceinline__ bool is_long(int32_t d, int32_t long_row) {
+    return long_row > 0 && d > long_row;
+}
+
 // width[s] and the padded slice size C * w4 (int64) for the scan.
-__global__ void k_widths(int64_t n, int64_t nslices, int32_t C, const int32_t *ideg,
-                         int32_t *width, int64_t *ssize) {
+__global__ void k_widths(int64_t n, int64_t nslices, int32_t C, int32_t long_row,
+                         const int32_t *ideg, int32_t *width, int64_t *ssize) {
     int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (s >= nslices) return;
     int32_t w = 0;
     for (int32_t r = 0; r < C; r++) {
         int64_t p = s * C + r;
-        if (p < n) w = max(w, ideg[p]);
+        if (p < n && !is_long(ideg[p], long_row)) w = max(w, ideg[p]);
     }
     width[s] = w;
     ssize[s] = (int64_t)C * ((w + 3) & ~3);
@@ -320,10 +327,10 @@ __global__ void k_widths(int64_t n, int64_t nslices, int32_t C, const int32_t *i
 
 // Fill the 4-interleaved SELL columns, one warp per (padded) row: lanes
 // stride over the CSR row, a ballot prefix drops self-loops in order.
-__global__ void k_fill_sell(int64_t n, int64_t npad, int32_t C, int32_t log2C,
-                            const int32_t *perm, const int32_t *inv, const int32_t *width,
-                            const int64_t *slice_off, const int64_t *rp, const int32_t *col,
-                            int32_t *scol) {
+__global__ void k_fill_sell(int64_t n, int64_t npad, int32_t C, int32_t log2C, int32_t long_row,
+                            const int32_t *perm, const int32_t *inv, const int32_t *ideg,
+                            const int32_t *width, const int64_t *slice_off, const int64_t *rp,
+                            const int32_t *col, int32_t *scol) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int64_t p = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); p < npad;
@@ -333,10 +340,10 @@ __global__ void k_fill_sell(int64_t n, int64_t npad, int32_t C, int32_t log2C,
         const int32_t w4 = (width[s] + 3) & ~3;
         int32_t *base = scol + slice_off[s] + r * 4;
         int32_t k = 0;
-        if (p < n) {
+        if (p < n && !is_long(ideg[p], long_row)) {
             const int32_t v = perm[p];
             const int64_t b = rp[v], e = rp[v + 1];
-            for (int64_t i = b; i - lane < e; i += 32) {
+            for (int64_t i = b + lane; i - lane < e; i += 32) {
                 const int32_t c = i < e ? col[i] : v;
                 const bool keep = c != v;
                 const unsigned m = __ballot_sync(kFull, keep);
@@ -362,11 +369,47 @@ __global__ void k_fill_push(int64_t n, const int32_t *perm, const int32_t *inv,
         const int32_t v = perm[p];
         int64_t at = prow[p];
         const int64_t b = rp[v], e = rp[v + 1];
-        for (int64_t i = b; i - lane < e; i += 32) {
+        for (int64_t i = b + lane; i - lane < e; i += 32) {
             const int32_t c = i < e ? col[i] : v;
             const bool keep = c != v;
             const unsigned m = __ballot_sync(kFull, keep);
             if (keep) pcol[at + __popc(m & lanemask_lt())] = inv[c];
+            at += __popc(m);
+        }
+    }
+}
+
+// Long-row list: flags, then scatter of positions and lengths after a scan.
+__global__ void k_long_flags(int64_t n, int32_t long_row, const int32_t *ideg, int32_t *flag) {
+    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p < n) flag[p] = is_long(ideg[p], long_row) ? 1 : 0;
+}
+
+__global__ void k_long_scatter(int64_t n, const int32_t *flag, const int64_t *idx,
+                               const int32_t *ideg, int32_t *lrow, int32_t *llen) {
+    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p < n && flag[p]) {
+        lrow[idx[p]] = (int32_t)p;
+        llen[idx[p]] = ideg[p];
+    }
+}
+
+// Sources of the long rows (pull side, position space), one warp per row.
+__global__ void k_fill_long(int64_t nlong, const int32_t *lrow, const int64_t *lptr,
+                            const int32_t *perm, const int32_t *inv, const int64_t *rp,
+                            const int32_t *col, int32_t *lcol) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t i = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); i < nlong;
+         i += nw) {
+        const int32_t v = perm[lrow[i]];
+        int64_t at = lptr[i];
+        const int64_t b = rp[v], e = rp[v + 1];
+        for (int64_t j = b + lane; j - lane < e; j += 32) {
+            const int32_t c = j < e ? col[j] : v;
+            const bool keep = c != v;
+            const unsigned m = __ballot_sync(kFull, keep);
+            if (keep) lcol[at + __popc(m & lanemask_lt())] = inv[c];
             at += __popc(m);
         }
     }
@@ -402,7 +445,7 @@ __global__ void k_vinit(int64_t n, int64_t nwords, const int32_t *ideg, uint32_t
 
 inline unsigned grid_for(int64_t count, int tpb) { return (unsigned)((count + tpb - 1) / tpb); }
 
-alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma) {
+alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma, int32_t long_row) {
     const int64_t n = g->n;
     cudaStream_t st = g->stream;
     free_sell(g->sell);
@@ -413,6 +456,7 @@ alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma) {
     s.C = C;
     s.log2C = C == 8 ? 3 : C == 16 ? 4 : C == 32 ? 5 : 6;
     s.sigma = sigma;
+    s.long_row = long_row;
     s.nslices = (n + C - 1) / C;
     const int64_t npad = s.nslices * C;
     s.nwords = (npad + 31) / 32;
@@ -463,7 +507,8 @@ alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma) {
         }
         ALB_CK(cudaGetLastError());
         k_positions<<<grid_for(n, T), T, 0, st>>>(n, s.perm, ilen, olen, s.inv, s.ideg, s.odeg);
-        k_widths<<<grid_for(s.nslices, T), T, 0, st>>>(n, s.nslices, C, s.ideg, s.width, ssize);
+        k_widths<<<grid_for(s.nslices, T), T, 0, st>>>(n, s.nslices, C, long_row, s.ideg, s.width,
+                                                        ssize);
         ALB_CK(cudaGetLastError());
         ALB_TRY(exclusive_scan(ssize, s.slice_off, s.nslices, st));
         ALB_TRY(exclusive_scan(s.odeg, s.prow, n, st));
@@ -482,10 +527,46 @@ alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma) {
         ALB_TRY(dmalloc((void **)&s.pcol, sizeof(int32_t) * (size_t)std::max<int64_t>(s.m_out, 1),
                         "push columns"));
         const unsigned fill_grid = (unsigned)(g->num_sms * 8);
-        k_fill_sell<<<fill_grid, T, 0, st>>>(n, npad, C, s.log2C, s.perm, s.inv, s.width,
-                                             s.slice_off, g->rp_in, g->col_in, s.col);
+        k_fill_sell<<<fill_grid, T, 0, st>>>(n, npad, C, s.log2C, long_row, s.perm, s.inv, s.ideg,
+                                             s.width, s.slice_off, g->rp_in, g->col_in, s.col);
         k_fill_push<<<fill_grid, T, 0, st>>>(n, s.perm, s.inv, s.prow, g->rp_out, g->col_out,
                                              s.pcol);
+        // long rows: flags -> scan -> scatter -> offsets -> fill
+        {
+            int32_t *flag = nullptr, *llen = nullptr;
+            int64_t *idx = nullptr;
+            struct Tmp {
+                int32_t *&a, *&b;
+                int64_t *&c;
+                ~Tmp() {
+                    dfree(a);
+                    dfree(b);
+                    dfree(c);
+                }
+            } tmp{flag, llen, idx};
+            ALB_TRY(dmalloc((void **)&flag, sizeof(int32_t) * n, "long-row flags"));
+            ALB_TRY(dmalloc((void **)&idx, sizeof(int64_t) * (n + 1), "long-row index"));
+            k_long_flags<<<grid_for(n, T), T, 0, st>>>(n, long_row, s.ideg, flag);
+            ALB_CK(cudaGetLastError());
+            ALB_TRY(exclusive_scan(flag, idx, n, st));
+            ALB_CK(cudaMemcpy(&s.nlong, idx + n, sizeof(int64_t), cudaMemcpyDeviceToHost));
+            ALB_TRY(dmalloc((void **)&s.lrow, sizeof(int32_t) * std::max<int64_t>(s.nlong, 1),
+                            "long rows"));
+            ALB_TRY(dmalloc((void **)&llen, sizeof(int32_t) * std::max<int64_t>(s.nlong, 1),
+                            "long-row lengths"));
+            ALB_TRY(dmalloc((void **)&s.lptr, sizeof(int64_t) * (s.nlong + 1), "long-row offsets"));
+            k_long_scatter<<<grid_for(n, T), T, 0, st>>>(n, flag, idx, s.ideg, s.lrow, llen);
+            ALB_CK(cudaGetLastError());
+            ALB_TRY(exclusive_scan(llen, s.lptr, s.nlong, st));
+            int64_t nent = 0;
+            ALB_CK(cudaMemcpy(&nent, s.lptr + s.nlong, sizeof(int64_t), cudaMemcpyDeviceToHost));
+            ALB_TRY(dmalloc((void **)&s.lcol, sizeof(int32_t) * std::max<int64_t>(nent, 1),
+                            "long-row sources"));
+            if (s.nlong)
+                k_fill_long<<<fill_grid, T, 0, st>>>(s.nlong, s.lrow, s.lptr, s.perm, s.inv,
+                                                     g->rp_in, g->col_in, s.lcol);
+            ALB_CK(cudaGetLastError());
+        }
         k_vinit<<<grid_for(s.nwords, T), T, 0, st>>>(n, s.nwords, s.ideg, s.vinit, dcnt);
         ALB_CK(cudaGetLastError());
         unsigned long long hc[3];
@@ -581,6 +662,7 @@ void alb_sell_opts_default(alb_sell_opts *o) {
     if (!o) return;
     o->C = 32;
     o->sigma = 1024;
+    o->long_row = 256;
 }
 
 alb_status alb_sell_build(alb_graph *g, const alb_sell_opts *o, double *ms) {
@@ -597,7 +679,7 @@ alb_status alb_sell_build(alb_graph *g, const alb_sell_opts *o, double *ms) {
     ALB_CK(cudaEventRecord(g->ev0, g->stream));
     alb_status rc;
     try {
-        rc = sell_build_impl(g, o->C, o->sigma);
+        rc = sell_build_impl(g, o->C, o->sigma, o->long_row);
     } catch (const std::bad_alloc &) {
         rc = fail(ALB_ERR_OOM, "alb_sell_build: host allocation failed");
     }
@@ -626,6 +708,24 @@ alb_status alb_sell_export(const alb_graph *g, int64_t *nslices, int32_t *perm, 
         ALB_CK(cudaMemcpy(slice_off, s.slice_off, sizeof(int64_t) * (s.nslices + 1),
                           cudaMemcpyDeviceToHost));
     if (col) ALB_CK(cudaMemcpy(col, s.col, sizeof(int32_t) * s.ncol, cudaMemcpyDeviceToHost));
+    return ALB_OK;
+}
+
+alb_status alb_sell_long_export(const alb_graph *g, int64_t *nlong, int32_t *lrow, int64_t *lptr,
+                                int32_t *lcol) {
+    if (!g) return fail(ALB_ERR_INVALID, "alb_sell_long_export: graph is NULL");
+    if (!g->sell.built) return fail(ALB_ERR_STATE, "alb_sell_long_export: SELL not built");
+    const Sell &s = g->sell;
+    ALB_CK(cudaSetDevice(g->device));
+    if (nlong) *nlong = s.nlong;
+    if (lrow && s.nlong)
+        ALB_CK(cudaMemcpy(lrow, s.lrow, sizeof(int32_t) * s.nlong, cudaMemcpyDeviceToHost));
+    if (lptr) ALB_CK(cudaMemcpy(lptr, s.lptr, sizeof(int64_t) * (s.nlong + 1), cudaMemcpyDeviceToHost));
+    if (lcol) {
+        int64_t nent = 0;
+        ALB_CK(cudaMemcpy(&nent, s.lptr + s.nlong, sizeof(int64_t), cudaMemcpyDeviceToHost));
+        if (nent) ALB_CK(cudaMemcpy(lcol, s.lcol, sizeof(int32_t) * nent, cudaMemcpyDeviceToHost));
+    }
     return ALB_OK;
 }
 

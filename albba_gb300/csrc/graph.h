@@ -45,6 +45,12 @@ struct Sell {
     int64_t *prow = nullptr;
     int32_t *pcol = nullptr;
     uint32_t *vinit = nullptr;
+    // rows longer than long_row: empty in the SELL, pulled warp-cooperatively
+    int32_t long_row = 0;
+    int64_t nlong = 0;
+    int32_t *lrow = nullptr;   // their positions, ascending
+    int64_t *lptr = nullptr;   // nlong + 1 offsets into lcol
+    int32_t *lcol = nullptr;   // their sources (positions), row order
     int64_t m_in = 0, m_out = 0;   // entries without self-loops
     int64_t active0 = 0;           // words of vinit that are not full
     int64_t zero_in = 0;           // rows without sources

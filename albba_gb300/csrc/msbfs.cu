@@ -49,6 +49,10 @@ struct MsArgs {
     const int4 *col4;
     const int64_t *prow;
     const int32_t *pcol;
+    int64_t nlong;  // rows kept out of the slices, pulled one warp each
+    const int32_t *lrow;
+    const int64_t *lptr;
+    const int32_t *lcol;
     uint64_t *V;
     uint64_t *S;  // K slots of npad words
     uint32_t *D;
@@ -228,6 +232,74 @@ __global__ void k_ms_bu(MsArgs a, int j) {
         }
         if (cfull) atomicAdd(&a.ctl->acc_full[k], cfull);
         if (bytes) atomicAdd(&a.ctl->acc_bytes[k], bytes);
+    }
+}
+
+__device__ __forceinline__ uint64_t warp_or64(uint64_t v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v |= __shfl_xor_sync(kFull, v, o);
+    return v;
+}
+
+// Long rows (kept out of the slices): one warp per row ORs the frontier
+// words of 32 sources per step and stops once every root is accounted for.
+template <bool kEarly>
+__global__ void k_ms_bu_long(MsArgs a, int j) {
+    if (a.nlong == 0) return;
+    const uint64_t *F = slot(a, j);
+    uint64_t *N = slot(a, j + 1);
+    const int lane = threadIdx.x & 31;
+    const int64_t wpb = blockDim.x >> 5;
+    const int64_t nwarps = (int64_t)gridDim.x * wpb;
+    const int L = a.ctl->level;
+    const int k = (L + 1) % 3;
+    unsigned long long cn = 0, cbits = 0, cmo = 0, cmi = 0, cfull = 0, cedges = 0, bytes = 0;
+    unsigned long long cdone = 0;
+    for (int64_t i = blockIdx.x * wpb + (threadIdx.x >> 5); i < a.nlong; i += nwarps) {
+        const int32_t p = __ldg(a.lrow + i);
+        const uint64_t vis = __ldg(a.V + p);
+        if (vis == kAll) continue;
+        const int64_t st = __ldg(a.lptr + i), en = __ldg(a.lptr + i + 1);
+        bytes += 24;
+        uint64_t acc = 0;
+        for (int64_t e0 = st; e0 < en; e0 += 32) {
+            const int64_t e = e0 + lane;
+            const uint64_t f = e < en ? __ldg(F + __ldg(a.lcol + e)) : 0ull;
+            acc |= warp_or64(f);
+            bytes += 128;
+            if (kEarly && (acc | vis) == kAll) break;
+        }
+        const uint64_t nb = acc & ~vis;
+        if (lane == 0 && nb) {
+            N[p] = nb;  // the slice pass wrote 0 here
+            const uint64_t nv = vis | nb;
+            a.V[p] = nv;
+            const int pc = __popcll(nb);
+            const int32_t od = __ldg(a.odeg + p);
+            cn++;
+            cbits += pc;
+            cmo += od;
+            cedges += (unsigned long long)pc * od;
+            if (nv == kAll) {
+                cdone++;
+                cmi += __ldg(a.ideg + p);
+                const uint32_t bit = 1u << (p & 31);
+                const uint32_t od2 = atomicOr(a.D + (p >> 5), bit);
+                cfull += (od2 != kFull && (od2 | bit) == kFull);
+            }
+        }
+    }
+    if (lane == 0 && (cn || bytes)) {
+        if (cn) {
+            atomicAdd(&a.ctl->acc_n[k], cn);
+            atomicAdd(&a.ctl->acc_bits[k], cbits);
+            atomicAdd(&a.ctl->acc_mo[k], cmo);
+            atomicAdd(&a.ctl->acc_mi[k], cmi);
+            atomicAdd(&a.ctl->acc_edges[k], cedges);
+            if (cdone) atomicAdd(&a.ctl->acc_done[k], cdone);
+        }
+        if (cfull) atomicAdd(&a.ctl->acc_full[k], cfull);
+        atomicAdd(&a.ctl->acc_bytes[k], bytes);
     }
 }
 
@@ -567,6 +639,10 @@ MsArgs ms_args(alb_graph *g, MsScratch &m) {
     a.col4 = (const int4 *)s.col;
     a.prow = s.prow;
     a.pcol = s.pcol;
+    a.nlong = s.nlong;
+    a.lrow = s.lrow;
+    a.lptr = s.lptr;
+    a.lcol = s.lcol;
     a.V = m.V;
     a.S = m.S;
     a.D = m.D;
@@ -711,10 +787,12 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
                 launches += 3;
             } else if (d == ALB_DIR_BOTTOMUP) {
                 k_ms_bu<true, true><<<wide, block, 0, stream>>>(a, j);
-                launches++;
+                k_ms_bu_long<true><<<wide, block, 0, stream>>>(a, j);
+                launches += 2;
             } else {
                 k_ms_bu<false, false><<<wide, block, 0, stream>>>(a, j);
-                launches++;
+                k_ms_bu_long<false><<<wide, block, 0, stream>>>(a, j);
+                launches += 2;
             }
             return ALB_OK;
         };

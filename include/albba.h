@@ -85,8 +85,10 @@ alb_status alb_graph_set_stream(alb_graph *g, void *cuda_stream);
 /* ------------------------------------------------------------ SELL-C-sigma */
 
 typedef struct {
-    int32_t C;     /* slice height: 8, 16, 32 (default) or 64 */
-    int32_t sigma; /* sort window in rows: 1 .. 16384 (default 1024) */
+    int32_t C;        /* slice height: 8, 16, 32 (default) or 64 */
+    int32_t sigma;    /* sort window in rows: 1 .. 16384 (default 1024) */
+    int32_t long_row; /* rows longer than this are kept out of the slices and
+                         pulled by a whole warp each (default 256; <= 0: none) */
 } alb_sell_opts;
 
 void alb_sell_opts_default(alb_sell_opts *o);
@@ -103,6 +105,10 @@ alb_status alb_sell_build(alb_graph *g, const alb_sell_opts *o, double *ms);
  * (int64, in int32 entries), col[slice_off[nslices]]. */
 alb_status alb_sell_export(const alb_graph *g, int64_t *nslices, int32_t *perm,
                            int32_t *width, int64_t *slice_off, int32_t *col);
+/* The long-row list: lrow[nlong] positions (ascending), lptr[nlong+1],
+ * lcol[lptr[nlong]] sources as positions in row order (NULL to skip). */
+alb_status alb_sell_long_export(const alb_graph *g, int64_t *nlong, int32_t *lrow,
+                                int64_t *lptr, int32_t *lcol);
 
 /* -------------------------------------------------------------------- BFS */
 

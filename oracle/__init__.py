@@ -52,9 +52,11 @@ def lib() -> C.CDLL:
         L.orc_sell_order.restype = None
         L.orc_sell_order.argtypes = [C.c_int64, P, C.c_int32, P]
         L.orc_sell_size.restype = C.c_int64
-        L.orc_sell_size.argtypes = [C.c_int64, P, P, C.c_int32]
+        L.orc_sell_size.argtypes = [C.c_int64, P, P, C.c_int32, C.c_int32]
         L.orc_sell_build.restype = None
-        L.orc_sell_build.argtypes = [C.c_int64, P, P, P, C.c_int32, P, P, P, P]
+        L.orc_sell_build.argtypes = [C.c_int64, P, P, P, C.c_int32, C.c_int32, P, P, P, P]
+        L.orc_sell_long.restype = C.c_int64
+        L.orc_sell_long.argtypes = [C.c_int64, P, P, P, C.c_int32, P, P, P]
         L.orc_refalgo_bfs.restype = C.c_int32
         L.orc_refalgo_bfs.argtypes = [C.c_int64, P, P, C.c_int32, C.c_int32, C.c_int32, P,
                                       C.POINTER(C.c_double), C.POINTER(C.c_double)]
@@ -116,18 +118,35 @@ def sell_order(deg, sigma):
     return out
 
 
-def sell_build(rowptr, col, order, C_):
+def sell_build(rowptr, col, order, C_, long_row=0):
+    """Position-space SELL layout; rows longer than long_row (> 0) stay empty."""
     rp, cl, od = _a(rowptr, np.int64), _a(col, np.int32), _a(order, np.int32)
     n = rp.shape[0] - 1
     ns = (n + C_ - 1) // C_
-    size = lib().orc_sell_size(n, rp.ctypes.data, od.ctypes.data, C_)
+    size = lib().orc_sell_size(n, rp.ctypes.data, od.ctypes.data, C_, int(long_row))
     inv = np.empty(n, np.int32)
     width = np.empty(ns, np.int32)
     off = np.empty(ns + 1, np.int64)
     scol = np.empty(max(size, 1), np.int32)
-    lib().orc_sell_build(n, rp.ctypes.data, cl.ctypes.data, od.ctypes.data, C_, inv.ctypes.data,
-                         width.ctypes.data, off.ctypes.data, scol.ctypes.data)
+    lib().orc_sell_build(n, rp.ctypes.data, cl.ctypes.data, od.ctypes.data, C_, int(long_row),
+                         inv.ctypes.data, width.ctypes.data, off.ctypes.data, scol.ctypes.data)
     return inv, width, off, scol[:size]
+
+
+def sell_long(rowptr, col, order, long_row):
+    """(lrow, lptr, lcol) of the rows longer than long_row, position space."""
+    rp, cl, od = _a(rowptr, np.int64), _a(col, np.int32), _a(order, np.int32)
+    n = rp.shape[0] - 1
+    k = lib().orc_sell_long(n, rp.ctypes.data, cl.ctypes.data, od.ctypes.data, int(long_row),
+                            None, None, None)
+    lrow = np.empty(max(k, 1), np.int32)
+    lptr = np.empty(k + 1, np.int64)
+    lib().orc_sell_long(n, rp.ctypes.data, cl.ctypes.data, od.ctypes.data, int(long_row),
+                        lrow.ctypes.data, lptr.ctypes.data, None)
+    lcol = np.empty(max(int(lptr[-1]), 1), np.int32)
+    lib().orc_sell_long(n, rp.ctypes.data, cl.ctypes.data, od.ctypes.data, int(long_row),
+                        lrow.ctypes.data, lptr.ctypes.data, lcol.ctypes.data)
+    return lrow[:k], lptr, lcol[: int(lptr[-1])]
 
 
 def refalgo_bfs(rowptr, col, root, sigma=16384, ntasks=0):

@@ -168,14 +168,20 @@ static int32_t row_len(const int64_t *rowptr, int32_t r)
     return (int32_t)(rowptr[r + 1] - rowptr[r]);
 }
 
+static int32_t sell_len(const int64_t *rowptr, int32_t r, int32_t long_row)
+{
+    int32_t d = row_len(rowptr, r);
+    return (long_row > 0 && d > long_row) ? 0 : d;
+}
+
 int64_t orc_sell_size(int64_t n, const int64_t *rowptr, const int32_t *order,
-                      int32_t C)
+                      int32_t C, int32_t long_row)
 {
     int64_t nslices = (n + C - 1) / C, total = 0;
     for (int64_t s = 0; s < nslices; s++) {
         int32_t w = 0;
         for (int64_t r = 0; r < C && s * C + r < n; r++) {
-            int32_t d = row_len(rowptr, order[s * C + r]);
+            int32_t d = sell_len(rowptr, order[s * C + r], long_row);
             if (d > w)
                 w = d;
         }
@@ -185,7 +191,7 @@ int64_t orc_sell_size(int64_t n, const int64_t *rowptr, const int32_t *order,
 }
 
 void orc_sell_build(int64_t n, const int64_t *rowptr, const int32_t *adj,
-                    const int32_t *order, int32_t C, int32_t *inv,
+                    const int32_t *order, int32_t C, int32_t long_row, int32_t *inv,
                     int32_t *width, int64_t *slice_off, int32_t *col)
 {
     int64_t nslices = (n + C - 1) / C;
@@ -195,7 +201,7 @@ void orc_sell_build(int64_t n, const int64_t *rowptr, const int32_t *adj,
     for (int64_t s = 0; s < nslices; s++) {
         int32_t w = 0;
         for (int64_t r = 0; r < C && s * C + r < n; r++) {
-            int32_t d = row_len(rowptr, order[s * C + r]);
+            int32_t d = sell_len(rowptr, order[s * C + r], long_row);
             if (d > w)
                 w = d;
         }
@@ -204,7 +210,7 @@ void orc_sell_build(int64_t n, const int64_t *rowptr, const int32_t *adj,
         slice_off[s] = off;
         for (int64_t r = 0; r < C; r++) {
             int64_t p = s * C + r;
-            int32_t d = p < n ? row_len(rowptr, order[p]) : 0;
+            int32_t d = p < n ? sell_len(rowptr, order[p], long_row) : 0;
             const int32_t *row = p < n ? adj + rowptr[order[p]] : 0;
             for (int32_t k = 0; k < w4; k++) {
                 int64_t at = off + (int64_t)(k / 4) * 4 * C + r * 4 + (k % 4);
@@ -219,6 +225,34 @@ void orc_sell_build(int64_t n, const int64_t *rowptr, const int32_t *adj,
         off += (int64_t)C * w4;
     }
     slice_off[nslices] = off;
+}
+
+int64_t orc_sell_long(int64_t n, const int64_t *rowptr, const int32_t *adj,
+                      const int32_t *order, int32_t long_row, int32_t *lrow,
+                      int64_t *lptr, int32_t *lcol)
+{
+    int32_t *inv = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n > 0 ? n : 1));
+    for (int64_t p = 0; p < n; p++)
+        inv[order[p]] = (int32_t)p;
+    int64_t k = 0, at = 0;
+    for (int64_t p = 0; p < n; p++) {
+        int32_t d = row_len(rowptr, order[p]);
+        if (!(long_row > 0 && d > long_row))
+            continue;
+        if (lrow) {
+            lrow[k] = (int32_t)p;
+            lptr[k] = at;
+            if (lcol)
+                for (int32_t j = 0; j < d; j++)
+                    lcol[at + j] = inv[adj[rowptr[order[p]] + j]];
+        }
+        at += d;
+        k++;
+    }
+    if (lrow)
+        lptr[k] = at;
+    free(inv);
+    return k;
 }
 
 /* ------------------------------------------------------------------------ */

@@ -63,21 +63,32 @@ int32_t orc_validate(int64_t n, const int64_t *out_rowptr, const int32_t *out_co
 void orc_sell_order(int64_t n, const int32_t *deg, int32_t sigma, int32_t *order);
 
 /* Size of the 4-interleaved SELL column array (int32 entries) for slice
- * height C, given the row order. */
+ * height C, given the row order. Rows longer than long_row (when > 0) are
+ * stored empty in the SELL and kept in a separate long-row list. */
 int64_t orc_sell_size(int64_t n, const int64_t *rowptr, const int32_t *order,
-                      int32_t C);
+                      int32_t C, int32_t long_row);
 
 /* Build the SELL-C-sigma layout used by the GPU path (position space):
  *   perm[p]  = order[p], inv[perm[p]] = p
- *   width[s] = max row length in slice s, w4 = width rounded up to 4
+ *   a row is long when long_row > 0 and its length exceeds long_row; long
+ *   rows have no SELL entries (length 0 below)
+ *   width[s] = max (non-long) row length in slice s, w4 = width rounded up to 4
  *   slice_off[s] = sum over t < s of C * w4[t]          (int64, nslices+1)
  *   col[slice_off[s] + (k/4)*4*C + r*4 + k%4] = inv[adj(perm[s*C+r])[k]]
  *       for k < deg; k in [deg, w4) holds the row's own position s*C+r;
  *       rows past n hold 0.
  * col must hold orc_sell_size(...) entries. */
 void orc_sell_build(int64_t n, const int64_t *rowptr, const int32_t *adj,
-                    const int32_t *order, int32_t C, int32_t *inv,
+                    const int32_t *order, int32_t C, int32_t long_row, int32_t *inv,
                     int32_t *width, int64_t *slice_off, int32_t *col);
+
+/* Long-row list of the same layout: lrow[i] = positions of long rows in
+ * ascending order, lptr (nlong+1) offsets, lcol = their entries relabelled to
+ * positions, in row order. Returns nlong; call with lrow == NULL for the
+ * count and lcol == NULL to skip the entries. */
+int64_t orc_sell_long(int64_t n, const int64_t *rowptr, const int32_t *adj,
+                      const int32_t *order, int32_t long_row, int32_t *lrow,
+                      int64_t *lptr, int32_t *lcol);
 
 /* Timed CPU port of the reference's level loop (C = 256 SELL with active-lane
  * ("DFC") layout, pull kernel above 4% of n frontier, sparse-x kernel below),

@@ -63,19 +63,26 @@ def test_config0_every_policy(rmat16_dev, policy, loop):
         check_root(g, dg, r, ab.bfs_opts(policy, loop))
 
 
-@pytest.mark.parametrize("C_,sigma", [(32, 1), (32, 1024), (32, 16384), (8, 64), (16, 256),
-                                      (64, 4096), (64, 1)])
-def test_sell_export_matches_oracle(rmat16, C_, sigma):
+@pytest.mark.parametrize("C_,sigma,long_row", [(32, 1, 256), (32, 1024, 256), (32, 16384, 0),
+                                               (8, 64, 64), (16, 256, 1000), (64, 4096, 256),
+                                               (64, 1, 0)])
+def test_sell_export_matches_oracle(rmat16, C_, sigma, long_row):
     g, roots = rmat16
     with ab.Graph(g) as dg:
-        dg.sell_build(C_, sigma)
+        dg.sell_build(C_, sigma, long_row)
         ex = dg.sell_export()
         order = oracle.sell_order(np.diff(g.rowptr).astype(np.int32), sigma)
-        inv, width, off, scol = oracle.sell_build(g.rowptr, g.col, order, C_)
+        inv, width, off, scol = oracle.sell_build(g.rowptr, g.col, order, C_, long_row)
         assert np.array_equal(ex.perm, order)
         assert np.array_equal(ex.width, width)
         assert np.array_equal(ex.slice_off, off)
         assert np.array_equal(ex.col, scol)
+        lrow, lptr, lcol = dg.sell_long_export()
+        olrow, olptr, olcol = oracle.sell_long(g.rowptr, g.col, order, long_row)
+        assert np.array_equal(lrow, olrow) and np.array_equal(lptr, olptr)
+        assert np.array_equal(lcol, olcol)
+        if long_row > 0:
+            assert len(lrow) > 0
         for r in roots[:4]:
             for loop in ("graph", "persistent"):
                 check_root(g, dg, r, ab.bfs_opts("beamer", loop))
@@ -91,11 +98,12 @@ def test_other_families(spec):
     g = make_graph(spec)
     roots = list(range(min(g.n, 13))) if spec["kind"] == "tiny" else g.pick_roots(8, 3).tolist()
     with ab.Graph(g) as dg:
-        for C_, sigma in ((32, 1), (32, 256)):
-            dg.sell_build(C_, sigma)
+        for C_, sigma, long_row in ((32, 1, 256), (32, 256, 8), (16, 64, 0)):
+            dg.sell_build(C_, sigma, long_row)
             for r in roots:
                 for loop in ("graph", "host", "persistent"):
                     check_root(g, dg, r, ab.bfs_opts("beamer", loop))
+                check_root(g, dg, r, ab.bfs_opts("bottomup_nobypass", "graph"))
 
 
 def test_isolated_root_and_empty_levels():

@@ -13,7 +13,7 @@ import albba_gb300 as ab
 from conftest import ROOT
 
 HEADERS = sorted((ROOT / "include").glob("*.h"))
-DECL = re.compile(r"^[A-Za-z_][\w\s\*]*?\b((?:alb|run_custom|print_additional)\w*)\s*\(", re.M)
+DECL = re.compile(r"^[A-Za-z_][\w\s\*]*?\b((?:alb|run_custom|print_additional|bfs_gb300)\w*)\s*\(", re.M)
 
 
 def declared(header: Path) -> set[str]:

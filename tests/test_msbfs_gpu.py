@@ -63,8 +63,8 @@ def test_other_families(spec):
     roots = np.arange(min(g.n, 13), dtype=np.int32) if spec["kind"] == "tiny" \
         else g.pick_roots(64, 3)
     with ab.Graph(g) as dg:
-        for C_, sigma in ((32, 1), (16, 256), (64, 64)):
-            dg.sell_build(C_, sigma)
+        for C_, sigma, long_row in ((32, 1, 256), (16, 256, 4), (64, 64, 0)):
+            dg.sell_build(C_, sigma, long_row)
             for policy in ("beamer", "topdown", "bottomup"):
                 check(g, dg, roots, ab.bfs_opts(policy))
 
