@@ -54,6 +54,8 @@ EXPORTED = [
     "alb_cbd_write", "alb_cbd_read", "alb_selector_load", "alb_selector_clear",
     "alb_msbfs64", "alb_msbfs64_device", "alb_bfs_profile", "alb_msbfs64_profile",
     "alb_mlp_forward", "alb_mlp_loss_grad", "alb_adam_step", "alb_selector_train",
+    "alb_worklist_create", "alb_worklist_destroy", "alb_worklist_add", "alb_worklist_size",
+    "alb_worklist_run", "alb_worklist_run_device",
 ]
 
 
@@ -143,6 +145,12 @@ _sigs = {
                                   C.c_float]),
     "alb_selector_train": (C.c_int32, [_P, _P, _P, C.c_int32, C.c_int32, C.c_float, C.c_uint64,
                                        C.c_int32, _P, C.POINTER(C.c_float)]),
+    "alb_worklist_create": (C.c_int32, [C.POINTER(_P)]),
+    "alb_worklist_destroy": (None, [_P]),
+    "alb_worklist_add": (C.c_int32, [_P, _P, _P, C.c_int32, C.c_float, C.c_float]),
+    "alb_worklist_size": (C.c_int32, [_P, _i64p, _i32p]),
+    "alb_worklist_run": (C.c_int32, [_P, C.c_int32, _P, C.POINTER(Stats)]),
+    "alb_worklist_run_device": (C.c_int32, [_P, C.c_int32, _P, C.POINTER(Stats)]),
     "alb_selector_load": (C.c_int32, [C.c_int32, _P]),
     "alb_selector_clear": (C.c_int32, [C.c_int32]),
 }
@@ -418,6 +426,56 @@ class Graph:
         buf = (LevelRec * max(cnt.value, 1))()
         check(_lib.alb_level_trace(self._h, cnt.value, buf, C.byref(cnt)))
         return list(buf[: cnt.value])
+
+
+class Worklist:
+    """Persistent multi-graph BFS (alb_worklist_*). Keeps its graphs alive."""
+
+    def __init__(self):
+        self._h = _P()
+        check(_lib.alb_worklist_create(C.byref(self._h)))
+        self._graphs: list[Graph] = []
+        self._layout: list[tuple[int, int, int]] = []  # (graph index, root, n)
+
+    def add(self, g: Graph, roots, alpha: float = 14.0, beta: float = 24.0) -> None:
+        r = np.ascontiguousarray(roots, dtype=np.int32)
+        check(_lib.alb_worklist_add(self._h, g.handle, r.ctypes.data, r.shape[0], alpha, beta))
+        self._graphs.append(g)
+        for x in r:
+            self._layout.append((len(self._graphs) - 1, int(x), g.n))
+
+    def size(self) -> tuple[int, int]:
+        e, k = C.c_int64(), C.c_int32()
+        check(_lib.alb_worklist_size(self._h, C.byref(e), C.byref(k)))
+        return e.value, k.value
+
+    def run(self, block: int = 256) -> tuple[list[np.ndarray], Stats]:
+        total, _ = self.size()
+        out = np.empty(max(total, 1), np.int32)
+        st = Stats()
+        check(_lib.alb_worklist_run(self._h, block, out.ctypes.data, C.byref(st)))
+        res, off = [], 0
+        for _, _, n in self._layout:
+            res.append(out[off: off + n])
+            off += n
+        return res, st
+
+    def run_device(self, d_levels, block: int = 256) -> Stats:
+        st = Stats()
+        check(_lib.alb_worklist_run_device(self._h, block, _ptr(d_levels), C.byref(st)))
+        return st
+
+    @property
+    def layout(self):
+        return list(self._layout)
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            _lib.alb_worklist_destroy(self._h)
+            self._h = _P()
+
+    def __del__(self):
+        self.close()
 
 
 NPARAM = 1443

@@ -156,6 +156,20 @@ __device__ __forceinline__ void append_claims(const BfsArgs &a, int32_t *NQ,
     }
 }
 
+// Rows per warp for the short-row pass: as many frontier rows as keep every
+// warp busy (1 when the frontier is small, up to 32 when it is large).
+__device__ __forceinline__ int rows_per_warp(int64_t qlen, int64_t nwarps) {
+    int G = 32;
+    while (G > 1 && (int64_t)(G >> 1) * nwarps >= qlen) G >>= 1;
+    return G;
+}
+
+// Big-row counter: entry count in the top 26 bits, chunk total in the low 38.
+// One atomicAdd of (1 << 38 | chunks) gives a row its index and chunk base
+// together, so chunk bases grow with the index and can be binary-searched.
+constexpr int kBigShift = 38;
+constexpr unsigned long long kBigMask = (1ull << kBigShift) - 1;
+
 template <bool kPersist>
 __device__ void td_phase(const BfsArgs &a, int L, Range r) {
     const int32_t *Q = (L & 1) ? a.q1 : a.q0;
@@ -170,20 +184,26 @@ __device__ void td_phase(const BfsArgs &a, int L, Range r) {
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int64_t wpb = blockDim.x >> 5;
     const int64_t gw = (int64_t)r.bid * wpb + wib;
-    const int64_t stride = (int64_t)r.nblk * wpb * 32;
+    const int64_t nwarps = (int64_t)r.nblk * wpb;
+    const int G = rows_per_warp(qlen, nwarps);
+    const int64_t stride = nwarps * G;
     unsigned long long cn = 0, cmo = 0, cmi = 0;
     const uint32_t lvl = (uint32_t)(L + 1);
-    for (int64_t cb = gw * 32; cb < qlen; cb += stride) {
+    for (int64_t cb = gw * G; cb < qlen; cb += stride) {
         const int64_t i = cb + lane;
-        int32_t u = i < qlen ? ld_state<kPersist>(Q + i) : -1;
+        int32_t u = (lane < G && i < qlen) ? ld_state<kPersist>(Q + i) : -1;
         int64_t st = 0, d = 0;
         int32_t ou = 0;
         if (u >= 0) {
             st = __ldg(a.prow + u);
             d = __ldg(a.prow + u + 1) - st;
             ou = __ldg(a.perm + u);
-            if (d > kBigRow) {  // shared by all warps in big_phase
-                a.big[atomicAdd(big_slot, 1ull)] = u;
+            if (d > kBigRow) {  // pushed in chunks by all warps in td_big_phase
+                const unsigned long long nch = (unsigned long long)((d + kBigChunk - 1) / kBigChunk);
+                const unsigned long long old = atomicAdd(big_slot, (1ull << kBigShift) | nch);
+                const int64_t idx = (int64_t)(old >> kBigShift);
+                a.big[idx] = u;
+                a.big_base[idx] = (int64_t)(old & kBigMask);
                 d = 0;
             }
         }
@@ -220,11 +240,14 @@ __device__ void td_phase(const BfsArgs &a, int L, Range r) {
     }
 }
 
-// Long frontier rows: chunk c of big row i goes to warp (i + c) mod warps.
+// Long frontier rows, kBigChunk edges per chunk, chunks spread over all
+// warps; a chunk finds its row by binary search over the chunk bases.
 template <bool kPersist>
 __device__ void td_big_phase(const BfsArgs &a, int L, Range r) {
-    const int64_t nbig = (int64_t)ld_state<kPersist>(&a.ctl->nbig[L % 3]);
-    if (nbig == 0) return;
+    const unsigned long long ctr = ld_state<kPersist>(&a.ctl->nbig[L % 3]);
+    if (ctr == 0) return;
+    const int64_t nbig = (int64_t)(ctr >> kBigShift);
+    const int64_t total = (int64_t)(ctr & kBigMask);
     int32_t *NQ = (L & 1) ? a.q0 : a.q1;
     uint32_t *N = (L & 1) ? a.bm0 : a.bm1;
     unsigned long long *nq_slot = &a.ctl->qn[(L + 1) % 3];
@@ -234,23 +257,27 @@ __device__ void td_big_phase(const BfsArgs &a, int L, Range r) {
     const int64_t nwarps = (int64_t)r.nblk * wpb;
     const uint32_t lvl = (uint32_t)(L + 1);
     unsigned long long cn = 0, cmo = 0, cmi = 0;
-    for (int64_t i = 0; i < nbig; i++) {
-        const int32_t u = ld_state<kPersist>(a.big + i);
+    for (int64_t k = gw; k < total; k += nwarps) {
+        int64_t lo = 0, hi = nbig - 1;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi + 1) >> 1;
+            if (ld_state<kPersist>(a.big_base + mid) <= k) lo = mid;
+            else hi = mid - 1;
+        }
+        const int32_t u = ld_state<kPersist>(a.big + lo);
+        const int64_t c = k - ld_state<kPersist>(a.big_base + lo);
         const int64_t st = __ldg(a.prow + u);
         const int64_t d = __ldg(a.prow + u + 1) - st;
         const uint32_t ou = (uint32_t)__ldg(a.perm + u);
-        const int64_t nch = (d + kBigChunk - 1) / kBigChunk;
-        for (int64_t c = ((gw - i) % nwarps + nwarps) % nwarps; c < nch; c += nwarps) {
-            const int64_t e1 = min(d, (c + 1) * kBigChunk);
-            for (int64_t e = c * kBigChunk + lane; e - lane < e1; e += 32) {
-                bool claimed = false;
-                int32_t v = 0;
-                if (e < e1) {
-                    v = __ldg(a.pcol + st + e);
-                    claimed = push_edge(a, N, v, ou, kPersist);
-                }
-                append_claims(a, NQ, nq_slot, claimed, v, lvl, cn, cmo, cmi);
+        const int64_t e1 = min(d, (c + 1) * kBigChunk);
+        for (int64_t e = c * kBigChunk + lane; e - lane < e1; e += 32) {
+            bool claimed = false;
+            int32_t v = 0;
+            if (e < e1) {
+                v = __ldg(a.pcol + st + e);
+                claimed = push_edge(a, N, v, ou, kPersist);
             }
+            append_claims(a, NQ, nq_slot, claimed, v, lvl, cn, cmo, cmi);
         }
     }
     cn = warp_sum(cn);
@@ -318,12 +345,17 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r) {
             cp = a.col4 + (__ldg(a.slice_off + s) >> 2) + (p & (C - 1));
         }
         int32_t found = -1;
+        // group j+1 is requested before group j's frontier tests, so each lane
+        // keeps one column load in flight while it waits on the bitmap
+        int4 c = make_int4(p, p, p, p);
+        if (active && ng > 0) c = ld_nc(cp);
         for (int32_t j = 0;; j++) {
             active = active && (j < ng);
             if (!__any_sync(kFull, active)) break;
             bytes += 16ull * 32;  // one int4 group for the warp's 32 rows
             if (!active) continue;
-            const int4 c = ld_nc(cp + (int64_t)j * C);
+            int4 nx = make_int4(p, p, p, p);
+            if (j + 1 < ng) nx = ld_nc(cp + (int64_t)(j + 1) * C);
             const uint32_t f0 = ld_bits<kPersist>(F + (c.x >> 5));
             const uint32_t f1 = ld_bits<kPersist>(F + (c.y >> 5));
             const uint32_t f2 = ld_bits<kPersist>(F + (c.z >> 5));
@@ -340,6 +372,7 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r) {
                     if (kEarly) active = false;
                 }
             }
+            c = nx;
         }
         const unsigned nm = __ballot_sync(kFull, found >= 0);
         if (lane == 0) {
@@ -740,6 +773,7 @@ alb_status bfs_scratch_alloc(alb_graph *g) {
     ALB_TRY(dmalloc((void **)&b.q0, sizeof(int32_t) * n, "frontier queue"));
     ALB_TRY(dmalloc((void **)&b.q1, sizeof(int32_t) * n, "frontier queue"));
     ALB_TRY(dmalloc((void **)&b.big, sizeof(int32_t) * n, "long-row list"));
+    ALB_TRY(dmalloc((void **)&b.big_base, sizeof(int64_t) * n, "long-row chunk bases"));
     ALB_TRY(dmalloc((void **)&b.level_pos, sizeof(int32_t) * n, "levels"));
     ALB_TRY(dmalloc((void **)&b.parent_pos, sizeof(uint32_t) * n, "parents"));
     ALB_TRY(dmalloc((void **)&b.ctl, sizeof(BfsCtl), "level control"));
@@ -758,6 +792,7 @@ void bfs_scratch_free(alb_graph *g) {
     dfree(b.q0);
     dfree(b.q1);
     dfree(b.big);
+    dfree(b.big_base);
     dfree(b.level_pos);
     dfree(b.parent_pos);
     dfree(b.out_level);
@@ -814,6 +849,7 @@ BfsArgs make_args(alb_graph *g) {
     a.q0 = b.q0;
     a.q1 = b.q1;
     a.big = b.big;
+    a.big_base = b.big_base;
     a.level_pos = b.level_pos;
     a.parent_pos = b.parent_pos;
     a.ctl = b.ctl;

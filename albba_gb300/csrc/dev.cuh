@@ -11,7 +11,7 @@ namespace alb {
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 // Top-down: rows longer than kBigRow are pushed in kBigChunk-edge chunks
 // shared by every warp instead of by the one warp that dequeued them.
-constexpr int64_t kBigRow = 1024;
+constexpr int64_t kBigRow = 256;
 constexpr int64_t kBigChunk = 128;
 
 // ---------------------------------------------------------------- loads
@@ -114,6 +114,7 @@ struct BfsArgs {
     uint32_t *vis;             // visited bitmap
     int32_t *q0, *q1;          // frontier queues (by level parity)
     int32_t *big;              // frontier rows split across all warps (top-down)
+    int64_t *big_base;         // their first chunk index
     int32_t *level_pos;        // depth by position
     uint32_t *parent_pos;      // parent original id by position
     BfsCtl *ctl;

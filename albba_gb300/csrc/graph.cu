@@ -549,7 +549,8 @@ alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma, int32_t long_
             k_long_flags<<<grid_for(n, T), T, 0, st>>>(n, long_row, s.ideg, flag);
             ALB_CK(cudaGetLastError());
             ALB_TRY(exclusive_scan(flag, idx, n, st));
-            ALB_CK(cudaMemcpy(&s.nlong, idx + n, sizeof(int64_t), cudaMemcpyDeviceToHost));
+            ALB_CK(cudaMemcpyAsync(&s.nlong, idx + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+            ALB_CK(cudaStreamSynchronize(st));
             ALB_TRY(dmalloc((void **)&s.lrow, sizeof(int32_t) * std::max<int64_t>(s.nlong, 1),
                             "long rows"));
             ALB_TRY(dmalloc((void **)&llen, sizeof(int32_t) * std::max<int64_t>(s.nlong, 1),
@@ -559,7 +560,8 @@ alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma, int32_t long_
             ALB_CK(cudaGetLastError());
             ALB_TRY(exclusive_scan(llen, s.lptr, s.nlong, st));
             int64_t nent = 0;
-            ALB_CK(cudaMemcpy(&nent, s.lptr + s.nlong, sizeof(int64_t), cudaMemcpyDeviceToHost));
+            ALB_CK(cudaMemcpyAsync(&nent, s.lptr + s.nlong, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+            ALB_CK(cudaStreamSynchronize(st));
             ALB_TRY(dmalloc((void **)&s.lcol, sizeof(int32_t) * std::max<int64_t>(nent, 1),
                             "long-row sources"));
             if (s.nlong)

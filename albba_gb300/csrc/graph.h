@@ -62,6 +62,7 @@ struct BfsScratch {
     uint32_t *bm0 = nullptr, *bm1 = nullptr, *vis = nullptr;
     int32_t *q0 = nullptr, *q1 = nullptr;
     int32_t *big = nullptr;
+    int64_t *big_base = nullptr;
     int32_t *level_pos = nullptr;
     uint32_t *parent_pos = nullptr;
     int32_t *out_level = nullptr, *out_parent = nullptr;  // staging for host outputs

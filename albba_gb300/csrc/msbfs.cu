@@ -58,6 +58,7 @@ struct MsArgs {
     uint32_t *D;
     int32_t *q0, *q1;
     int32_t *big;  // frontier rows longer than kBigRow (top-down)
+    int64_t *big_base;
     MsCtl *ctl;
     const float *mlp;
 };
@@ -105,10 +106,11 @@ __global__ void k_ms_roots(MsArgs a, MsInit in) {
             a.q0[atomicAdd(&s_nf, 1ull)] = p;
             atomicAdd(&s_mf, (unsigned long long)a.odeg[p]);
         }
-        if (!(oldv & bit)) {
-            atomicAdd(&s_pairs, 1ull);
-            atomicAdd(&s_edges, (unsigned long long)a.odeg[p]);
-        }
+        // bit i belongs to root i alone, so every root counts once (its bit
+        // may already be set in V when p has no sources: V starts full there)
+        (void)oldv;
+        atomicAdd(&s_pairs, 1ull);
+        atomicAdd(&s_edges, (unsigned long long)a.odeg[p]);
     }
     __syncthreads();
     // positions whose every root bit is now set
@@ -341,6 +343,9 @@ __device__ __forceinline__ void ms_append(int32_t *NQ, unsigned long long *nq_sl
     if (claimed) NQ[base + __popc(cm & lanemask_lt())] = v;
 }
 
+constexpr int kMsBigShift = 38;
+constexpr unsigned long long kMsBigMask = (1ull << kMsBigShift) - 1;
+
 __global__ void k_ms_td(MsArgs a, int j) {
     const uint64_t *F = slot(a, j);
     uint64_t *N = slot(a, j + 1);
@@ -355,18 +360,25 @@ __global__ void k_ms_td(MsArgs a, int j) {
     __shared__ uint64_t s_f[32][32];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int64_t wpb = blockDim.x >> 5;
-    const int64_t stride = (int64_t)gridDim.x * wpb * 32;
-    for (int64_t cb = (blockIdx.x * wpb + wib) * 32; cb < qlen; cb += stride) {
+    const int64_t nwarps = (int64_t)gridDim.x * wpb;
+    int G = 32;  // frontier rows per warp: enough to keep every warp busy
+    while (G > 1 && (int64_t)(G >> 1) * nwarps >= qlen) G >>= 1;
+    const int64_t stride = nwarps * G;
+    for (int64_t cb = (blockIdx.x * wpb + wib) * G; cb < qlen; cb += stride) {
         const int64_t i = cb + lane;
-        const int32_t u = i < qlen ? Q[i] : -1;
+        const int32_t u = (lane < G && i < qlen) ? Q[i] : -1;
         int64_t st = 0, d = 0;
         uint64_t f = 0;
         if (u >= 0) {
             st = __ldg(a.prow + u);
             d = __ldg(a.prow + u + 1) - st;
             f = __ldg(F + u);
-            if (d > kBigRow) {  // pushed by all warps in k_ms_td_big
-                a.big[atomicAdd(big_slot, 1ull)] = u;
+            if (d > kBigRow) {  // pushed in chunks by all warps in k_ms_td_big
+                const unsigned long long nch = (unsigned long long)((d + kBigChunk - 1) / kBigChunk);
+                const unsigned long long old = atomicAdd(big_slot, (1ull << kMsBigShift) | nch);
+                const int64_t idx = (int64_t)(old >> kMsBigShift);
+                a.big[idx] = u;
+                a.big_base[idx] = (int64_t)(old & kMsBigMask);
                 d = 0;
             }
         }
@@ -394,11 +406,14 @@ __global__ void k_ms_td(MsArgs a, int j) {
     }
 }
 
-// Long frontier rows: chunk c of big row i goes to warp (i + c) mod warps.
+// Long frontier rows in kBigChunk-edge chunks over all warps; a chunk finds
+// its row by binary search over the chunk bases (monotone in the index).
 __global__ void k_ms_td_big(MsArgs a, int j) {
     const int L = a.ctl->level;
-    const int64_t nbig = (int64_t)a.ctl->nbig[L % 3];
-    if (nbig == 0) return;
+    const unsigned long long ctr = a.ctl->nbig[L % 3];
+    if (ctr == 0) return;
+    const int64_t nbig = (int64_t)(ctr >> kMsBigShift);
+    const int64_t total = (int64_t)(ctr & kMsBigMask);
     const uint64_t *F = slot(a, j);
     uint64_t *N = slot(a, j + 1);
     int32_t *NQ = (L & 1) ? a.q0 : a.q1;
@@ -407,23 +422,27 @@ __global__ void k_ms_td_big(MsArgs a, int j) {
     const int64_t wpb = blockDim.x >> 5;
     const int64_t gw = blockIdx.x * wpb + (threadIdx.x >> 5);
     const int64_t nwarps = (int64_t)gridDim.x * wpb;
-    for (int64_t i = 0; i < nbig; i++) {
-        const int32_t u = a.big[i];
+    for (int64_t k = gw; k < total; k += nwarps) {
+        int64_t lo = 0, hi = nbig - 1;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi + 1) >> 1;
+            if (a.big_base[mid] <= k) lo = mid;
+            else hi = mid - 1;
+        }
+        const int32_t u = a.big[lo];
+        const int64_t c = k - a.big_base[lo];
         const int64_t st = __ldg(a.prow + u);
         const int64_t d = __ldg(a.prow + u + 1) - st;
         const uint64_t f = __ldg(F + u);
-        const int64_t nch = (d + kBigChunk - 1) / kBigChunk;
-        for (int64_t c = ((gw - i) % nwarps + nwarps) % nwarps; c < nch; c += nwarps) {
-            const int64_t e1 = min(d, (c + 1) * kBigChunk);
-            for (int64_t e = c * kBigChunk + lane; e - lane < e1; e += 32) {
-                bool claimed = false;
-                int32_t v = 0;
-                if (e < e1) {
-                    v = __ldg(a.pcol + st + e);
-                    claimed = ms_push(a, N, v, f);
-                }
-                ms_append(NQ, nq_slot, claimed, v);
+        const int64_t e1 = min(d, (c + 1) * kBigChunk);
+        for (int64_t e = c * kBigChunk + lane; e - lane < e1; e += 32) {
+            bool claimed = false;
+            int32_t v = 0;
+            if (e < e1) {
+                v = __ldg(a.pcol + st + e);
+                claimed = ms_push(a, N, v, f);
             }
+            ms_append(NQ, nq_slot, claimed, v);
         }
     }
 }
@@ -572,6 +591,7 @@ struct MsScratch {
     uint64_t *V = nullptr, *S = nullptr;
     uint32_t *D = nullptr;
     int32_t *q0 = nullptr, *q1 = nullptr, *big = nullptr;
+    int64_t *big_base = nullptr;
     MsCtl *ctl = nullptr, *h_ctl = nullptr;
     int32_t *out = nullptr;
 };
@@ -594,6 +614,7 @@ void ms_scratch_free(alb_graph *g) {
     dfree(m.q0);
     dfree(m.q1);
     dfree(m.big);
+    dfree(m.big_base);
     dfree(m.ctl);
     dfree(m.out);
     if (m.h_ctl) cudaFreeHost(m.h_ctl);
@@ -614,6 +635,7 @@ alb_status ms_alloc(alb_graph *g, MsScratch &m) {
     ALB_TRY(dmalloc((void **)&m.q0, sizeof(int32_t) * npad, "msbfs queue"));
     ALB_TRY(dmalloc((void **)&m.q1, sizeof(int32_t) * npad, "msbfs queue"));
     ALB_TRY(dmalloc((void **)&m.big, sizeof(int32_t) * npad, "msbfs long-row list"));
+    ALB_TRY(dmalloc((void **)&m.big_base, sizeof(int64_t) * npad, "msbfs long-row chunk bases"));
     ALB_TRY(dmalloc((void **)&m.ctl, sizeof(MsCtl), "msbfs control"));
     ALB_CK(cudaMallocHost((void **)&m.h_ctl, sizeof(MsCtl)));
     m.ready = true;
@@ -649,6 +671,7 @@ MsArgs ms_args(alb_graph *g, MsScratch &m) {
     a.q0 = m.q0;
     a.q1 = m.q1;
     a.big = m.big;
+    a.big_base = m.big_base;
     a.ctl = m.ctl;
     return a;
 }

@@ -79,6 +79,7 @@ alb_status exclusive_scan(const Tin *in, int64_t *out, int64_t count, cudaStream
     const int64_t ntiles = (count + kScanTile - 1) / kScanTile;
     if (ntiles == 0) {
         ALB_CK(cudaMemsetAsync(out, 0, sizeof(int64_t), st));
+        ALB_CK(cudaStreamSynchronize(st));
         return ALB_OK;
     }
     int64_t *bsum = nullptr;

@@ -168,9 +168,10 @@ def regret(us: np.ndarray, choice: np.ndarray) -> dict:
             "chosen_us": float(chosen.sum()), "best_us": float(best.sum())}
 
 
-def save(params: np.ndarray, form: str, meta: dict) -> Path:
-    WEIGHTS.mkdir(exist_ok=True)
-    p = WEIGHTS / f"{form}.json"
+def save(params: np.ndarray, form: str, meta: dict, out_dir: Path | None = None) -> Path:
+    d = Path(out_dir) if out_dir else WEIGHTS
+    d.mkdir(parents=True, exist_ok=True)
+    p = d / f"{form}.json"
     p.write_text(json.dumps({"form": form, "nparam": int(params.size),
                              "params": [float(x) for x in params], "meta": meta}))
     return p
@@ -195,7 +196,8 @@ def install(forms=("plain", "batched")) -> dict:
     return done
 
 
-def run(full: bool, forms, roots: int, steps: int, heldout_scale: int, log=print) -> dict:
+def run(full: bool, forms, roots: int, steps: int, heldout_scale: int, log=print,
+        out_dir: Path | None = None) -> dict:
     report = {}
     specs = training_specs(full)
     for form in forms:
@@ -223,7 +225,7 @@ def run(full: bool, forms, roots: int, steps: int, heldout_scale: int, log=print
                 "train_loss": loss, "steps": steps, "profile_s": t1 - t0, "train_s": t2 - t1,
                 "train_regret": tr, "heldout": {"graph": f"rmat s{heldout_scale} ef16",
                                                 "regret": held}}
-        save(params, form, meta)
+        save(params, form, meta, out_dir)
         report[form] = meta
         log(json.dumps({form: meta}))
     return report
@@ -236,8 +238,9 @@ def main():
     ap.add_argument("--roots", type=int, default=4)
     ap.add_argument("--steps", type=int, default=4000)
     ap.add_argument("--heldout-scale", type=int, default=22)
+    ap.add_argument("--out-dir", default=None, help="where to write <form>.json")
     a = ap.parse_args()
-    run(a.full, a.forms.split(","), a.roots, a.steps, a.heldout_scale)
+    run(a.full, a.forms.split(","), a.roots, a.steps, a.heldout_scale, out_dir=a.out_dir)
 
 
 if __name__ == "__main__":

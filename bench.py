@@ -199,14 +199,33 @@ def run_reference(args, rank: int, world: int) -> None:
 
 
 # ----------------------------------------------------------------- GPU side
+def timed(stream, fn, steps, sync, dist, torch):
+    """CUDA events on the launching stream around `steps` calls of fn (max over ranks)."""
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sync()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    out = [fn() for _ in range(steps)]
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    sync()
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, out
+
+
 def run_ours(args, rank: int, world: int, dist) -> None:
     import torch
 
     import albba_gb300 as ab
+    from albba_gb300 import selector
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
+    loaded = selector.install()
     g, roots, gen_s = make_graph(args)
-    deg = g.degrees()
     stream = torch.cuda.current_stream()
     dg = ab.Graph(g, flags=ab.CSR_SYMMETRIC | ab.CSR_SORTED)
     dg.set_stream(stream.cuda_stream)
@@ -214,61 +233,60 @@ def run_ours(args, rank: int, world: int, dist) -> None:
     n = g.n
     d_lv = torch.empty(n, dtype=torch.int32, device="cuda")
     d_pa = torch.empty(n, dtype=torch.int32, device="cuda")
-    opts = ab.bfs_opts("beamer", args.loop)
+    d_ms = torch.empty((n, 64), dtype=torch.int32, device="cuda")
+    policy = "learned" if loaded.get("batched") else "beamer"
+    bopts = ab.bfs_opts(policy)
+    popts = ab.bfs_opts("learned" if loaded.get("plain") else "beamer", args.loop)
+    sync = (lambda: dist.barrier()) if dist else (lambda: None)
+
+    def batched_step():
+        st = dg.msbfs64_device(roots, d_ms, bopts)
+        return st.edges // 2, st.kernels
 
     def plain_step():
-        e = 0
-        k = 0
-        per_root = []
+        e = k = 0
+        per = []
         for r in roots:
-            st = dg.bfs_device(int(r), d_lv, d_pa, opts)
+            st = dg.bfs_device(int(r), d_lv, d_pa, popts)
             e += st.edges // 2
             k += st.kernels
-            per_root.append((st.edges // 2, st.ms))
-        return e, k, per_root
+            per.append((st.edges // 2, st.ms))
+        return e, k, per
 
-    # warm-up
     for _ in range(args.warmup):
+        batched_step()
         plain_step()
-    sync = (lambda: dist.barrier()) if dist else (lambda: None)
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with Clocks(dev) as clk:
-        sync()
-        torch.cuda.synchronize()
-        ev0.record(stream)
-        edges, launches, per_root = 0, 0, []
-        for _ in range(args.steps):
-            e, k, pr = plain_step()
-            edges += e
-            launches += k
-            per_root += pr
-        ev1.record(stream)
-        torch.cuda.synchronize()
-        sync()
-    ms = ev0.elapsed_time(ev1)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    steps = args.steps
+        ms, outs = timed(stream, batched_step, args.steps, sync, dist, torch)
+    edges = sum(e for e, _ in outs)
+    launches = sum(k for _, k in outs)
     value = world * edges / ms / 1e6
-    hm = len(per_root) / sum(ms_r / (e_r / 1e6) for e_r, ms_r in per_root if e_r > 0) \
-        if per_root else None
+    pms, pouts = timed(stream, plain_step, args.steps, sync, dist, torch)
+    pedges = sum(o[0] for o in pouts)
+    per_root = [x for o in pouts for x in o[2]]
+    plain = world * pedges / pms / 1e6
+    hm = len(per_root) / sum(m / (e / 1e6) for e, m in per_root if e > 0) if per_root else None
 
-    # roofline: bottom-up launches timed with CUDA events (host-driven loop)
     roof = None if args.no_roofline else roofline(dg, roots[:8])
-    e2e = None if args.no_e2e else e2e_plain(args, g, roots, ab, torch)
+    e2e = None if args.no_e2e else e2e_batched(args, g, roots, ab, torch, bopts)
     cpu = cpu_baseline(g, roots, args.cpu_roots) if rank == 0 and args.cpu_roots > 0 else None
     if rank != 0:
         return
-    line = {"metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": world, "steps": steps,
-            "warmup": args.warmup, "ms_per_step": ms / steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+    meta = {f: (json.loads((selector.WEIGHTS / f"{f}.json").read_text()).get("meta", {})
+                if loaded.get(f) else None) for f in ("plain", "batched")}
+    line = {"metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic RMAT (seeded generator, no dataset)",
-            "config": config(args, g, {"form": "plain direction-optimising single-root BFS x 64 "
-                                               "(CUDA-graph level loop)",
-                                       "parallelism": f"replicas x{world}"}),
-            "plain_gteps_harmonic_mean": hm,
+            "config": config(args, g, {
+                "form": f"64-root bit-parallel batched BFS, {policy} direction selector",
+                "parallelism": f"replicas x{world}"}),
+            "plain": {"gteps": plain, "gteps_harmonic_mean": hm, "ms_per_step": pms / args.steps,
+                      "form": "64 single-root direction-optimising BFS "
+                              f"({'learned' if loaded.get('plain') else 'beamer'}, {args.loop} loop)"},
+            "batched_over_plain": value / plain if plain else None,
+            "selector": {"batched": policy, "weights": {f: bool(loaded.get(f)) for f in loaded},
+                         "heldout": {f: (m or {}).get("heldout") for f, m in meta.items()}},
             "sell_build_ms": build_ms, "graph_gen_s": gen_s,
             "gpu_launches": launches, "clocks": clk.summary(), "roofline": roof,
             "e2e": e2e, "cpu_baseline": cpu}
@@ -276,6 +294,8 @@ def run_ours(args, rank: int, world: int, dist) -> None:
 
 
 def roofline(dg, roots) -> dict:
+    """Bottom-up slice kernel (k_bu): bytes counted by the kernel, CUDA-event
+    time of its launches in the host-driven loop on the graph's stream."""
     import albba_gb300 as ab
     peak, kind = peaks()
     byts, us, launches = 0, 0.0, 0
@@ -288,40 +308,45 @@ def roofline(dg, roots) -> dict:
                 us += t.step_us
                 launches += 1
     gbs = byts / us / 1e3 if us > 0 else 0.0
-    return {"bound": "hbm", "kernel": "k_bu (bottom-up pull, bypass + early exit)",
+    return {"bound": "hbm", "kernel": "k_bu + k_bu_long (bottom-up pull: slices, then long rows)",
             "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
             "peak_kind": f"{kind} HBM copy bandwidth (burst)",
             "bytes_per_launch": byts / max(launches, 1), "us_per_launch": us / max(launches, 1),
-            "launches": launches, "traffic": None}
+            "launches": launches, "roots": len(roots), "traffic": None}
 
 
-def e2e_plain(args, g, roots, ab, torch) -> dict:
-    n = g.n
-    lv = np.empty(n, np.int32)
-    pa = np.empty(n, np.int32)
+def e2e_batched(args, g, roots, ab, torch, opts) -> dict:
+    """Host CSR in, host levels out, through the C ABI: alb_graph_create +
+    alb_sell_build + alb_msbfs64 (n x 64 int32 levels copied back)."""
+    levels = np.empty((g.n, 64), np.int32)
     h2d = g.rowptr.nbytes + g.col.nbytes
-    d2h = len(roots) * (lv.nbytes + pa.nbytes)
+    d2h = levels.nbytes
 
     def step():
-        e = 0
         with ab.Graph(g, flags=ab.CSR_SYMMETRIC | ab.CSR_SORTED) as dg:
             dg.sell_build(32, args.sigma)
-            for r in roots:
-                _, _, st = dg.bfs(int(r), ab.bfs_opts("beamer", "graph"))
-                e += st.edges // 2
-        return e
+            st = ab.check(ab.lib().alb_msbfs64(dg.handle, roots.ctypes.data, len(roots),
+                                                ab.C.byref(opts), levels.ctypes.data,
+                                                ab.C.byref(ab.Stats())))
+            del st
+        return 0
 
     step()
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
     k = 2
-    e = sum(step() for _ in range(k))
+    t0 = time.perf_counter()
+    for _ in range(k):
+        step()
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
-    return {"value": e / dt / 1e9, "unit": "GTEPS", "h2d_bytes_per_step": h2d,
+    deg = g.degrees()
+    edges = 0
+    for i in range(len(roots)):
+        edges += int(deg[levels[:, i] >= 0].sum()) // 2
+    return {"value": k * edges / dt / 1e9, "unit": "GTEPS", "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h, "steps": k,
-            "path": "alb_graph_create (host CSR) + alb_sell_build + alb_bfs x roots "
-                    "(host level+parent), wall clock"}
+            "path": "alb_graph_create (host CSR) + alb_sell_build + alb_msbfs64 (host n x 64 "
+                    "levels), wall clock"}
 
 
 def emit(line: dict, args) -> None:

@@ -205,6 +205,29 @@ alb_status alb_msbfs64(alb_graph *g, const int32_t *roots, int32_t nroots,
 alb_status alb_msbfs64_device(alb_graph *g, const int32_t *roots, int32_t nroots,
                               const alb_bfs_opts *o, int32_t *d_levels, alb_stats *st);
 
+/* ---------------------------------------------------------------- work list */
+
+/* Many (graph, root) traversals of small graphs in one persistent launch:
+ * each CTA runs one traversal at a time with its frontier, next-frontier and
+ * visited bitmaps in shared memory, popping the next item from a global
+ * counter (longest graphs first). Graphs keep their own SELL build (C, sigma,
+ * long rows) and Beamer thresholds. Levels only (no parents). A graph added
+ * to a work list must outlive the list's runs and must fit the shared-memory
+ * budget (3 bits per vertex: up to about 600K vertices). */
+typedef struct alb_worklist alb_worklist;
+alb_status alb_worklist_create(alb_worklist **out);
+void alb_worklist_destroy(alb_worklist *w);
+alb_status alb_worklist_add(alb_worklist *w, alb_graph *g, const int32_t *roots, int32_t nroots,
+                            float alpha, float beta);
+/* Total int32 level entries (sum over items of n) and item count. */
+alb_status alb_worklist_size(const alb_worklist *w, int64_t *level_entries, int32_t *items);
+/* levels: host buffer of alb_worklist_size entries; item k (in the order
+ * added, roots in order) occupies n_g consecutive entries, original ids.
+ * block: threads per CTA (128, 256, 512 or 1024). stats.ms = kernel time. */
+alb_status alb_worklist_run(alb_worklist *w, int32_t block, int32_t *levels, alb_stats *st);
+alb_status alb_worklist_run_device(alb_worklist *w, int32_t block, int32_t *d_levels,
+                                   alb_stats *st);
+
 /* --------------------------------------------------------------- selector */
 
 /* Load the 1,443 fp32 parameters of a direction-selector MLP
