@@ -9,8 +9,8 @@ step time; the cheapest prediction wins. Training runs on the GPU through the
 library's own forward/backward/Adam kernels (alb_selector_train). The Beamer
 alpha/beta rule stays as the fallback when no weights are loaded.
 
-Weights are stored as JSON next to this file (selector/plain.json for the
-single-root BFS, selector/batched.json for the 64-root batched BFS) with the
+Weights are stored as JSON next to this file (selector_weights/plain.json for the
+single-root BFS, selector_weights/batched.json for the 64-root batched BFS) with the
 metadata of the run that produced them.
 
 The reference (scalbba/albba) switches kernels on a fixed frontier-size
@@ -29,7 +29,7 @@ import numpy as np
 
 import albba_gb300 as ab
 
-WEIGHTS = Path(__file__).resolve().parent / "selector"
+WEIGHTS = Path(__file__).resolve().parent / "selector_weights"
 FORMS = {"plain": 0, "batched": 1}
 
 
