@@ -328,6 +328,7 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r) {
     const int32_t C = a.C, log2C = a.log2C;
     const int32_t lvl = L + 1;
     unsigned long long cn = 0, cmo = 0, cmi = 0, full = 0, bytes = 0;
+    const uint64_t pol = l2_evict_first();
     for (int64_t w = gw; w < a.nwords; w += stride) {
         const uint32_t vis = ld_bits<kPersist>(a.vis + w);
         if (kBypass && vis == kFull) {
@@ -348,14 +349,14 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r) {
         // group j+1 is requested before group j's frontier tests, so each lane
         // keeps one column load in flight while it waits on the bitmap
         int4 c = make_int4(p, p, p, p);
-        if (active && ng > 0) c = ld_nc(cp);
+        if (active && ng > 0) c = ld_stream(cp, pol);
         for (int32_t j = 0;; j++) {
             active = active && (j < ng);
             if (!__any_sync(kFull, active)) break;
             bytes += 16ull * 32;  // one int4 group for the warp's 32 rows
             if (!active) continue;
             int4 nx = make_int4(p, p, p, p);
-            if (j + 1 < ng) nx = ld_nc(cp + (int64_t)(j + 1) * C);
+            if (j + 1 < ng) nx = ld_stream(cp + (int64_t)(j + 1) * C, pol);
             const uint32_t f0 = ld_bits<kPersist>(F + (c.x >> 5));
             const uint32_t f1 = ld_bits<kPersist>(F + (c.y >> 5));
             const uint32_t f2 = ld_bits<kPersist>(F + (c.z >> 5));

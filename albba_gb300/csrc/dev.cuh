@@ -29,6 +29,22 @@ __device__ __forceinline__ int4 ld_nc(const int4 *p) {
 template <class T>
 __device__ __forceinline__ T ld_ro(const T *p) { return __ldg(p); }
 
+// L2 eviction policies (PTX createpolicy): the column stream of a level is
+// read once and marked evict-first so that the bitmaps it is tested against
+// keep their L2 lines.
+__device__ __forceinline__ uint64_t l2_evict_first() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ int4 ld_stream(const int4 *ptr, uint64_t pol) {
+    int4 r;
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.s32 {%0,%1,%2,%3}, [%4], %5;"
+                 : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+                 : "l"(ptr), "l"(pol));
+    return r;
+}
+
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 __device__ __forceinline__ unsigned lanemask_lt() {
     unsigned m;
