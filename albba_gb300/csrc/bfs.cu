@@ -131,7 +131,13 @@ __device__ __forceinline__ bool push_edge(const BfsArgs &a, uint32_t *N, int32_t
     const uint32_t bit = 1u << (v & 31);
     const uint32_t w = persist ? __ldcg(a.vis + (v >> 5)) : __ldg(a.vis + (v >> 5));
     if (w & bit) return false;
-    atomicMin(a.parent_pos + v, ou);
+    // read before writing: a hub target receives thousands of pushes in one
+    // level, and atomics on one address serialise in L2, so the atomics are
+    // issued only when they can still change something
+    const uint32_t cur_parent = __ldcg(a.parent_pos + v);
+    const uint32_t cur_n = __ldcg(N + (v >> 5));
+    if (ou < cur_parent) atomicMin(a.parent_pos + v, ou);
+    if (cur_n & bit) return false;
     return !(atomicOr(N + (v >> 5), bit) & bit);
 }
 
@@ -335,7 +341,6 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r) {
             if (lane == 0) N[w] = 0;
             continue;
         }
-        bytes += 16;
         const int32_t p = (int32_t)(w * 32 + lane);
         const int64_t s = (int64_t)p >> log2C;
         bool active = !((vis >> lane) & 1u);
@@ -350,11 +355,14 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r) {
         // keeps one column load in flight while it waits on the bitmap
         int4 c = make_int4(p, p, p, p);
         if (active && ng > 0) c = ld_stream(cp, pol);
+        // an unvisited row whose first entry is padding is a long row (rows
+        // without sources start visited): the long-row pass has run already
+        const bool long_cand = active && c.x == p;
         for (int32_t j = 0;; j++) {
             active = active && (j < ng);
             if (!__any_sync(kFull, active)) break;
-            bytes += 16ull * 32;  // one int4 group for the warp's 32 rows
             if (!active) continue;
+            bytes += 32;  // four columns and the four frontier words they select
             int4 nx = make_int4(p, p, p, p);
             if (j + 1 < ng) nx = ld_stream(cp + (int64_t)(j + 1) * C, pol);
             const uint32_t f0 = ld_bits<kPersist>(F + (c.x >> 5));
@@ -375,7 +383,11 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r) {
             }
             c = nx;
         }
-        const unsigned nm = __ballot_sync(kFull, found >= 0);
+        bool reached = found >= 0;
+        bool by_long = false;
+        if (long_cand && !reached && a.nlong)
+            by_long = reached = ld_state<kPersist>(a.parent_pos + p) != kFull;
+        const unsigned nm = __ballot_sync(kFull, reached);
         if (lane == 0) {
             N[w] = nm;
             if (nm) {
@@ -383,9 +395,10 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r) {
                 full += (vis != kFull && (vis | nm) == kFull);
             }
         }
-        if (found >= 0) {
+        if (reached) {
             a.level_pos[p] = lvl;
-            a.parent_pos[p] = (uint32_t)__ldg(a.perm + found);
+            if (!by_long) a.parent_pos[p] = (uint32_t)__ldg(a.perm + found);
+            bytes += 20;  // level, parent, the parent's id, two degrees
             cn++;
             cmo += (unsigned long long)__ldg(a.odeg + p);
             cmi += (unsigned long long)__ldg(a.ideg + p);
@@ -394,6 +407,7 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r) {
     cn = warp_sum(cn);
     cmo = warp_sum(cmo);
     cmi = warp_sum(cmi);
+    bytes = warp_sum(bytes);
     if (lane == 0 && (cn || full || bytes)) {
         const int k = (L + 1) % 3;
         if (cn) {
@@ -406,55 +420,96 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r) {
     }
 }
 
-// Bottom-up pull of the long rows (kept out of the slices): one warp per row,
-// 32 sources per step; the lowest lane with a frontier hit in the first
-// step that has one is the earliest, i.e. smallest-id, source.
+// Bottom-up pull of the long rows (kept out of the slices). Rows are in
+// source-id order, so a row's parent is its first frontier source.
+// Head pass: one warp per unvisited long row scans its first kLongChunk
+// sources, 32 per step; a hit there is the row's first frontier source. A row
+// with no hit in its head and more sources left goes on the continuation list
+// (packed counter in nbig[L % 3]: rows << kBigShift | chunks), whose
+// kLongChunk-source chunks the tail pass spreads over all warps; their hits
+// meet in parent_pos[p] by atomicMin. The slice pass that follows sees
+// parent_pos[p] set and records the row as reached. Both run before bu_phase.
 template <bool kPersist, bool kEarly>
 __device__ void bu_long_phase(const BfsArgs &a, int L, Range r) {
     if (a.nlong == 0) return;
     const uint32_t *F = (L & 1) ? a.bm1 : a.bm0;
-    uint32_t *N = (L & 1) ? a.bm0 : a.bm1;
     const int lane = threadIdx.x & 31;
     const int64_t wpb = blockDim.x >> 5;
     const int64_t nwarps = (int64_t)r.nblk * wpb;
-    unsigned long long cn = 0, cmo = 0, cmi = 0, full = 0, bytes = 0;
+    unsigned long long *cont = &a.ctl->nbig[L % 3];
+    unsigned long long bytes = 0;
     for (int64_t i = (int64_t)r.bid * wpb + (threadIdx.x >> 5); i < a.nlong; i += nwarps) {
         const int32_t p = __ldg(a.lrow + i);
-        const uint32_t bit = 1u << (p & 31);
-        if (ld_bits<kPersist>(a.vis + (p >> 5)) & bit) continue;
+        if ((ld_bits<kPersist>(a.vis + (p >> 5)) >> (p & 31)) & 1u) continue;
         const int64_t st = __ldg(a.lptr + i), en = __ldg(a.lptr + i + 1);
-        bytes += 16;
+        const int64_t hen = min(en, st + kLongChunk);
+        bytes += 24;
         int32_t found = -1;
-        for (int64_t e0 = st; e0 < en; e0 += 32) {
+        for (int64_t e0 = st; e0 < hen; e0 += 32) {
             const int64_t e = e0 + lane;
-            const int32_t c = e < en ? __ldg(a.lcol + e) : p;
+            const int32_t c = e < hen ? __ldg(a.lcol + e) : p;
             const bool hit = (ld_bits<kPersist>(F + (c >> 5)) >> (c & 31)) & 1u;
             const unsigned m = __ballot_sync(kFull, hit);
-            bytes += 128;
+            bytes += 8 * (unsigned long long)min((int64_t)32, hen - e0);
             if (m && found < 0) found = __shfl_sync(kFull, c, __ffs(m) - 1);
             if (kEarly && found >= 0) break;
         }
-        if (found >= 0 && lane == 0) {
-            a.level_pos[p] = L + 1;
-            a.parent_pos[p] = (uint32_t)__ldg(a.perm + found);
-            atomicOr(N + (p >> 5), bit);
-            const uint32_t old = atomicOr(a.vis + (p >> 5), bit);
-            full += (old != kFull && (old | bit) == kFull);
-            cn++;
-            cmo += (unsigned long long)__ldg(a.odeg + p);
-            cmi += (unsigned long long)__ldg(a.ideg + p);
+        if (lane == 0) {
+            if (found >= 0) {
+                atomicMin(a.parent_pos + p, (uint32_t)__ldg(a.perm + found));
+            } else if (hen < en) {
+                const unsigned long long nch =
+                    (unsigned long long)((en - hen + kLongChunk - 1) / kLongChunk);
+                const unsigned long long old = atomicAdd(cont, (1ull << kBigShift) | nch);
+                const int64_t idx = (int64_t)(old >> kBigShift);
+                a.big[idx] = (int32_t)i;
+                a.big_base[idx] = (int64_t)(old & kBigMask);
+            }
         }
     }
-    if (lane == 0 && (cn || full || bytes)) {
-        const int k = (L + 1) % 3;
-        if (cn) {
-            atomicAdd(&a.ctl->acc_n[k], cn);
-            atomicAdd(&a.ctl->acc_mo[k], cmo);
-            atomicAdd(&a.ctl->acc_mi[k], cmi);
+    if (lane == 0 && bytes) atomicAdd(&a.ctl->acc_bytes[(L + 1) % 3], bytes);
+}
+
+// Tail pass over the continuation list: chunk k of list entry j covers
+// sources [lptr[i] + (1 + k - big_base[j]) * kLongChunk, ...) of long row
+// i = big[j]; the entry is found by binary search over big_base.
+template <bool kPersist, bool kEarly>
+__device__ void bu_long_tail_phase(const BfsArgs &a, int L, Range r) {
+    const unsigned long long ctr = ld_state<kPersist>(&a.ctl->nbig[L % 3]);
+    if (ctr == 0) return;
+    const int64_t nrows = (int64_t)(ctr >> kBigShift);
+    const int64_t total = (int64_t)(ctr & kBigMask);
+    const uint32_t *F = (L & 1) ? a.bm1 : a.bm0;
+    const int lane = threadIdx.x & 31;
+    const int64_t wpb = blockDim.x >> 5;
+    const int64_t nwarps = (int64_t)r.nblk * wpb;
+    unsigned long long bytes = 0;
+    for (int64_t k = (int64_t)r.bid * wpb + (threadIdx.x >> 5); k < total; k += nwarps) {
+        int64_t lo = 0, hi = nrows - 1;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi + 1) >> 1;
+            if (ld_state<kPersist>(a.big_base + mid) <= k) lo = mid;
+            else hi = mid - 1;
         }
-        if (full) atomicAdd(&a.ctl->acc_full[k], full);
-        if (bytes) atomicAdd(&a.ctl->acc_bytes[k], bytes);
+        const int32_t i = ld_state<kPersist>(a.big + lo);
+        const int32_t p = __ldg(a.lrow + i);
+        const int64_t c = k - ld_state<kPersist>(a.big_base + lo);
+        const int64_t st = __ldg(a.lptr + i) + (1 + c) * kLongChunk;
+        const int64_t en = min(__ldg(a.lptr + i + 1), st + kLongChunk);
+        bytes += 24;
+        int32_t found = -1;
+        for (int64_t e0 = st; e0 < en; e0 += 32) {
+            const int64_t e = e0 + lane;
+            const int32_t cc = e < en ? __ldg(a.lcol + e) : p;
+            const bool hit = (ld_bits<kPersist>(F + (cc >> 5)) >> (cc & 31)) & 1u;
+            const unsigned m = __ballot_sync(kFull, hit);
+            bytes += 8 * (unsigned long long)min((int64_t)32, en - e0);
+            if (m && found < 0) found = __shfl_sync(kFull, cc, __ffs(m) - 1);
+            if (kEarly && found >= 0) break;
+        }
+        if (found >= 0 && lane == 0) atomicMin(a.parent_pos + p, (uint32_t)__ldg(a.perm + found));
     }
+    if (lane == 0 && bytes) atomicAdd(&a.ctl->acc_bytes[(L + 1) % 3], bytes);
 }
 
 // Algorithmic bytes of the level that just ran (see alb_level_rec).
@@ -603,13 +658,18 @@ __global__ void k_bu_long(BfsArgs a) {
     bu_long_phase<false, kEarly>(a, a.ctl->level, Range{(int)blockIdx.x, (int)gridDim.x});
 }
 
+template <bool kEarly>
+__global__ void k_bu_long_tail(BfsArgs a) {
+    bu_long_tail_phase<false, kEarly>(a, a.ctl->level, Range{(int)blockIdx.x, (int)gridDim.x});
+}
+
 __global__ void k_end(BfsArgs a, cudaGraphConditionalHandle wh) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     BfsCtl c = *a.ctl;
     const int k = (c.level + 1) % 3;
     if (a.trace && c.level < c.trace_cap)
         a.trace[c.level].bytes = level_bytes(c, c.dir, c.acc_n[k], c.acc_bytes[k]);
-    c.launches += 2 + (c.branch == 1 ? 4 : c.branch == 0 ? 3 : 2);  // decide, end, steps
+    c.launches += 2 + (c.branch == 1 ? 4 : 3);  // decide, end, steps
     roll(c, c.dir, c.acc_n[k], c.acc_mo[k], c.acc_mi[k], c.acc_full[k]);
     if (c.level < c.trace_cap) c.trace_len = c.level;
     else c.trace_len = c.trace_cap;
@@ -703,17 +763,29 @@ __global__ void __launch_bounds__(256) k_persistent(BfsArgs a) {
                 ok = grid_sync(a.ctl, nb);
             }
         } else if (dir == ALB_DIR_BOTTOMUP) {
-            bu_phase<true, true, true>(a, L, r);
-            ok = grid_sync(a.ctl, nb);
-            if (ok && a.nlong) {
+            if (a.nlong) {
                 bu_long_phase<true, true>(a, L, r);
+                ok = grid_sync(a.ctl, nb);
+                if (ok && *(volatile unsigned long long *)&a.ctl->nbig[L % 3]) {
+                    bu_long_tail_phase<true, true>(a, L, r);
+                    ok = grid_sync(a.ctl, nb);
+                }
+            }
+            if (ok) {
+                bu_phase<true, true, true>(a, L, r);
                 ok = grid_sync(a.ctl, nb);
             }
         } else {
-            bu_phase<true, false, false>(a, L, r);
-            ok = grid_sync(a.ctl, nb);
-            if (ok && a.nlong) {
+            if (a.nlong) {
                 bu_long_phase<true, false>(a, L, r);
+                ok = grid_sync(a.ctl, nb);
+                if (ok && *(volatile unsigned long long *)&a.ctl->nbig[L % 3]) {
+                    bu_long_tail_phase<true, false>(a, L, r);
+                    ok = grid_sync(a.ctl, nb);
+                }
+            }
+            if (ok) {
+                bu_phase<true, false, false>(a, L, r);
                 ok = grid_sync(a.ctl, nb);
             }
         }
@@ -933,19 +1005,23 @@ alb_status build_loop_graph(alb_graph *g, int block) {
         ALB_TRY(add_kernel_node(b1, &bg, &t, 1, (void *)k_td_big, wide, aargs));
         ALB_TRY(add_kernel_node(b1, &f, &bg, 1, (void *)k_td_finish, wide, aargs));
     }
-    {  // 2: bottom-up with bypass, then the long rows
-        cudaGraphNode_t b, l;
-        ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[2], &b, nullptr, 0,
-                                (void *)k_bu<true, true>, wide, aargs));
-        ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[2], &l, &b, 1,
+    {  // 2: the long rows (head, tail), then bottom-up with bypass
+        cudaGraphNode_t b, l, t;
+        ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[2], &l, nullptr, 0,
                                 (void *)k_bu_long<true>, wide, aargs));
+        ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[2], &t, &l, 1,
+                                (void *)k_bu_long_tail<true>, wide, aargs));
+        ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[2], &b, &t, 1,
+                                (void *)k_bu<true, true>, wide, aargs));
     }
-    {  // 3: bottom-up without bypass, then the long rows
-        cudaGraphNode_t b, l;
-        ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[3], &b, nullptr, 0,
-                                (void *)k_bu<false, false>, wide, aargs));
-        ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[3], &l, &b, 1,
+    {  // 3: the long rows (head, tail), then bottom-up without bypass
+        cudaGraphNode_t b, l, t;
+        ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[3], &l, nullptr, 0,
                                 (void *)k_bu_long<false>, wide, aargs));
+        ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[3], &t, &l, 1,
+                                (void *)k_bu_long_tail<false>, wide, aargs));
+        ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[3], &b, &t, 1,
+                                (void *)k_bu<false, false>, wide, aargs));
     }
     void *eargs[] = {&a, &wh};
     cudaGraphNode_t nend;
@@ -988,11 +1064,13 @@ alb_status run_host_loop(alb_graph *g, const BfsArgs &a, const alb_bfs_opts &o,
             k_td_big<<<wide.grid, wide.block, 0, st>>>(a);
             k_td_finish<<<wide.grid, wide.block, 0, st>>>(a);
         } else if (dir == ALB_DIR_BOTTOMUP) {
-            k_bu<true, true><<<wide.grid, wide.block, 0, st>>>(a);
             k_bu_long<true><<<wide.grid, wide.block, 0, st>>>(a);
+            k_bu_long_tail<true><<<wide.grid, wide.block, 0, st>>>(a);
+            k_bu<true, true><<<wide.grid, wide.block, 0, st>>>(a);
         } else {
-            k_bu<false, false><<<wide.grid, wide.block, 0, st>>>(a);
             k_bu_long<false><<<wide.grid, wide.block, 0, st>>>(a);
+            k_bu_long_tail<false><<<wide.grid, wide.block, 0, st>>>(a);
+            k_bu<false, false><<<wide.grid, wide.block, 0, st>>>(a);
         }
         if (e1) cudaEventRecord(e1, st);
         k_end<<<1, 32, 0, st>>>(a, 0);
@@ -1099,11 +1177,13 @@ void launch_step(const BfsArgs &a, const Launch &wide, cudaStream_t st, int dir,
         k_td_big<<<wide.grid, wide.block, 0, st>>>(a);
         k_td_finish<<<wide.grid, wide.block, 0, st>>>(a);
     } else if (dir == ALB_DIR_BOTTOMUP) {
-        k_bu<true, true><<<wide.grid, wide.block, 0, st>>>(a);
         k_bu_long<true><<<wide.grid, wide.block, 0, st>>>(a);
+        k_bu_long_tail<true><<<wide.grid, wide.block, 0, st>>>(a);
+        k_bu<true, true><<<wide.grid, wide.block, 0, st>>>(a);
     } else {
-        k_bu<false, false><<<wide.grid, wide.block, 0, st>>>(a);
         k_bu_long<false><<<wide.grid, wide.block, 0, st>>>(a);
+        k_bu_long_tail<false><<<wide.grid, wide.block, 0, st>>>(a);
+        k_bu<false, false><<<wide.grid, wide.block, 0, st>>>(a);
     }
 }
 

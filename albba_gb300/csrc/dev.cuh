@@ -13,6 +13,12 @@ constexpr uint32_t kFull = 0xFFFFFFFFu;
 // shared by every warp instead of by the one warp that dequeued them.
 constexpr int64_t kBigRow = 256;
 constexpr int64_t kBigChunk = 128;
+// Bottom-up: a row kept out of the slices is pulled by one warp over its
+// first kLongChunk sources; what remains is split into kLongChunk-source
+// chunks spread over all warps (a hub would otherwise hold one warp).
+constexpr int64_t kLongChunk = 1024;
+// SELL build: rows with more raw entries than this are copied in chunks.
+constexpr int64_t kFillChunk = 2048;
 
 // ---------------------------------------------------------------- loads
 // Column and structure arrays are read-only for a whole traversal: read them
@@ -121,7 +127,7 @@ struct BfsArgs {
     const int4 *col4;          // SELL columns, 4-interleaved
     const int64_t *prow;       // push CSR (position space)
     const int32_t *pcol;
-    int64_t nlong;             // rows kept out of the slices (pulled per warp)
+    int64_t nlong;             // rows kept out of the slices
     const int32_t *lrow;
     const int64_t *lptr;
     const int32_t *lcol;

@@ -360,6 +360,7 @@ __global__ void k_fill_sell(int64_t n, int64_t npad, int32_t C, int32_t log2C, i
 }
 
 // Push-side CSR in position space, one warp per row.
+// Rows with more than kFillChunk raw entries are left to k_fill_chunks.
 __global__ void k_fill_push(int64_t n, const int32_t *perm, const int32_t *inv,
                             const int64_t *prow, const int64_t *rp, const int32_t *col,
                             int32_t *pcol) {
@@ -369,6 +370,7 @@ __global__ void k_fill_push(int64_t n, const int32_t *perm, const int32_t *inv,
         const int32_t v = perm[p];
         int64_t at = prow[p];
         const int64_t b = rp[v], e = rp[v + 1];
+        if (e - b > kFillChunk) continue;
         for (int64_t i = b + lane; i - lane < e; i += 32) {
             const int32_t c = i < e ? col[i] : v;
             const bool keep = c != v;
@@ -394,23 +396,82 @@ __global__ void k_long_scatter(int64_t n, const int32_t *flag, const int64_t *id
     }
 }
 
-// Sources of the long rows (pull side, position space), one warp per row.
-__global__ void k_fill_long(int64_t nlong, const int32_t *lrow, const int64_t *lptr,
-                            const int32_t *perm, const int32_t *inv, const int64_t *rp,
-                            const int32_t *col, int32_t *lcol) {
+// ------------------------------------------------ rows filled in chunks
+// Long rows (hubs, up to millions of entries) are copied in kFillChunk-entry
+// chunks spread over all warps instead of by one warp each. Rows are sorted,
+// so a row's self-loops form one run [lo, hi); the output index of input
+// entry j of row v is then (j - b) - (clamp(j, lo, hi) - lo), computable per
+// entry without a scan.
+__global__ void k_flag_raw(int64_t n, const int32_t *perm, const int64_t *rp, int64_t thr,
+                           int32_t *flag) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p < n) {
+        const int32_t v = perm[p];
+        flag[p] = (rp[v + 1] - rp[v]) > thr ? 1 : 0;
+    }
+}
+
+__global__ void k_scatter_flagged(int64_t n, const int32_t *flag, const int64_t *idx,
+                                  int32_t *rows) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p < n && flag[p]) rows[idx[p]] = (int32_t)p;
+}
+
+// Per listed row: chunk count over its raw entries and its self-loop run.
+__global__ void k_chunk_src(int64_t nr, const int32_t *rows, const int32_t *perm,
+                            const int64_t *rp, const int32_t *col, int64_t chunk, int32_t *cnt,
+                            int64_t *slo, int64_t *shi) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= nr) return;
+    const int32_t v = perm[rows[i]];
+    const int64_t b = rp[v], e = rp[v + 1];
+    cnt[i] = (int32_t)((e - b + chunk - 1) / chunk);
+    int64_t lo = b, hi = e;  // first entry >= v
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (col[mid] < v) lo = mid + 1;
+        else hi = mid;
+    }
+    int64_t lo2 = lo, hi2 = e;  // first entry > v
+    while (lo2 < hi2) {
+        const int64_t mid = (lo2 + hi2) >> 1;
+        if (col[mid] <= v) lo2 = mid + 1;
+        else hi2 = mid;
+    }
+    slo[i] = lo;
+    shi[i] = lo2;
+}
+
+// crow[cb[i] + c] = i for every chunk c of row i.
+__global__ void k_chunk_rows(int64_t nr, const int64_t *cb, int32_t *crow) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= nr) return;
+    for (int64_t k = cb[i]; k < cb[i + 1]; k++) crow[k] = (int32_t)i;
+}
+
+// One warp per chunk: out[obase + kept index] = inv[col[j]] for the chunk's
+// raw entries j, self-loops dropped. obase is indexed by position (by_pos)
+// or by list index.
+__global__ void k_fill_chunks(int64_t nchunks, const int32_t *crow, const int32_t *rows,
+                              const int64_t *cb, const int64_t *slo, const int64_t *shi,
+                              const int32_t *perm, const int32_t *inv, const int64_t *rp,
+                              const int32_t *col, const int64_t *obase, int by_pos,
+                              int32_t *out) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t i = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); i < nlong;
-         i += nw) {
-        const int32_t v = perm[lrow[i]];
-        int64_t at = lptr[i];
+    for (int64_t k = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); k < nchunks;
+         k += nw) {
+        const int32_t i = crow[k];
+        const int32_t p = rows[i];
+        const int32_t v = perm[p];
         const int64_t b = rp[v], e = rp[v + 1];
-        for (int64_t j = b + lane; j - lane < e; j += 32) {
-            const int32_t c = j < e ? col[j] : v;
-            const bool keep = c != v;
-            const unsigned m = __ballot_sync(kFull, keep);
-            if (keep) lcol[at + __popc(m & lanemask_lt())] = inv[c];
-            at += __popc(m);
+        const int64_t s0 = b + (k - cb[i]) * kFillChunk;
+        const int64_t s1 = min(e, s0 + kFillChunk);
+        const int64_t lo = slo[i], hi = shi[i];
+        const int64_t o = by_pos ? obase[p] : obase[i];
+        for (int64_t j = s0 + lane; j < s1; j += 32) {
+            const int32_t c = col[j];
+            if (c != v) out[o + (j - b) - (min(max(j, lo), hi) - lo)] = inv[c];
         }
     }
 }
@@ -444,6 +505,64 @@ __global__ void k_vinit(int64_t n, int64_t nwords, const int32_t *ideg, uint32_t
 }
 
 inline unsigned grid_for(int64_t count, int tpb) { return (unsigned)((count + tpb - 1) / tpb); }
+
+// Reads one int64 device value on stream st.
+alb_status read_i64(const int64_t *d, int64_t *h, cudaStream_t st) {
+    ALB_CK(cudaMemcpyAsync(h, d, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    ALB_CK(cudaStreamSynchronize(st));
+    return ALB_OK;
+}
+
+// Chunk list of nr rows: cb (nr + 1 first-chunk indices) from per-row counts,
+// crow (row of each chunk). cb and crow are allocated here.
+alb_status chunk_list(const int32_t *cnt, int64_t nr, int64_t **cb, int32_t **crow,
+                      int64_t *nchunks, cudaStream_t st) {
+    ALB_TRY(dmalloc((void **)cb, sizeof(int64_t) * (nr + 1), "chunk bases"));
+    ALB_TRY(exclusive_scan(cnt, *cb, nr, st));
+    ALB_TRY(read_i64(*cb + nr, nchunks, st));
+    ALB_TRY(dmalloc((void **)crow, sizeof(int32_t) * std::max<int64_t>(*nchunks, 1),
+                    "chunk rows"));
+    if (nr) k_chunk_rows<<<grid_for(nr, 256), 256, 0, st>>>(nr, *cb, *crow);
+    ALB_CK(cudaGetLastError());
+    return ALB_OK;
+}
+
+// Copies the rows listed in rows[0..nr) (positions) into out in position
+// space, kFillChunk raw entries per warp task (see k_fill_chunks).
+alb_status fill_rows_chunked(const int32_t *rows, int64_t nr, const int32_t *perm,
+                             const int32_t *inv, const int64_t *rp, const int32_t *col,
+                             const int64_t *obase, bool by_pos, int32_t *out, unsigned grid,
+                             cudaStream_t st) {
+    if (nr == 0) return ALB_OK;
+    int32_t *cnt = nullptr, *crow = nullptr;
+    int64_t *slo = nullptr, *shi = nullptr, *cb = nullptr;
+    auto cleanup = [&]() {
+        dfree(cnt);
+        dfree(crow);
+        dfree(slo);
+        dfree(shi);
+        dfree(cb);
+    };
+    alb_status rc = [&]() -> alb_status {
+        ALB_TRY(dmalloc((void **)&cnt, sizeof(int32_t) * nr, "chunk counts"));
+        ALB_TRY(dmalloc((void **)&slo, sizeof(int64_t) * nr, "self-loop runs"));
+        ALB_TRY(dmalloc((void **)&shi, sizeof(int64_t) * nr, "self-loop runs"));
+        k_chunk_src<<<grid_for(nr, 256), 256, 0, st>>>(nr, rows, perm, rp, col, kFillChunk, cnt,
+                                                        slo, shi);
+        ALB_CK(cudaGetLastError());
+        int64_t nchunks = 0;
+        ALB_TRY(chunk_list(cnt, nr, &cb, &crow, &nchunks, st));
+        if (nchunks)
+            k_fill_chunks<<<grid, 256, 0, st>>>(nchunks, crow, rows, cb, slo, shi, perm, inv, rp,
+                                                col, obase, by_pos ? 1 : 0, out);
+        ALB_CK(cudaGetLastError());
+        // the temporaries are freed below: finish with them first
+        ALB_CK(cudaStreamSynchronize(st));
+        return ALB_OK;
+    }();
+    cleanup();
+    return rc;
+}
 
 alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma, int32_t long_row) {
     const int64_t n = g->n;
@@ -531,6 +650,35 @@ alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma, int32_t long_
                                              s.width, s.slice_off, g->rp_in, g->col_in, s.col);
         k_fill_push<<<fill_grid, T, 0, st>>>(n, s.perm, s.inv, s.prow, g->rp_out, g->col_out,
                                              s.pcol);
+        ALB_CK(cudaGetLastError());
+        // push rows too long for one warp: listed, then copied in chunks
+        {
+            int32_t *flag = nullptr, *rows = nullptr;
+            int64_t *idx = nullptr;
+            struct Tmp {
+                int32_t *&a, *&b;
+                int64_t *&c;
+                ~Tmp() {
+                    dfree(a);
+                    dfree(b);
+                    dfree(c);
+                }
+            } tmp{flag, rows, idx};
+            ALB_TRY(dmalloc((void **)&flag, sizeof(int32_t) * n, "long push-row flags"));
+            ALB_TRY(dmalloc((void **)&idx, sizeof(int64_t) * (n + 1), "long push-row index"));
+            k_flag_raw<<<grid_for(n, T), T, 0, st>>>(n, s.perm, g->rp_out, kFillChunk, flag);
+            ALB_CK(cudaGetLastError());
+            ALB_TRY(exclusive_scan(flag, idx, n, st));
+            int64_t nr = 0;
+            ALB_TRY(read_i64(idx + n, &nr, st));
+            if (nr) {
+                ALB_TRY(dmalloc((void **)&rows, sizeof(int32_t) * nr, "long push rows"));
+                k_scatter_flagged<<<grid_for(n, T), T, 0, st>>>(n, flag, idx, rows);
+                ALB_CK(cudaGetLastError());
+                ALB_TRY(fill_rows_chunked(rows, nr, s.perm, s.inv, g->rp_out, g->col_out, s.prow,
+                                          true, s.pcol, fill_grid, st));
+            }
+        }
         // long rows: flags -> scan -> scatter -> offsets -> fill
         {
             int32_t *flag = nullptr, *llen = nullptr;
@@ -564,10 +712,8 @@ alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma, int32_t long_
             ALB_CK(cudaStreamSynchronize(st));
             ALB_TRY(dmalloc((void **)&s.lcol, sizeof(int32_t) * std::max<int64_t>(nent, 1),
                             "long-row sources"));
-            if (s.nlong)
-                k_fill_long<<<fill_grid, T, 0, st>>>(s.nlong, s.lrow, s.lptr, s.perm, s.inv,
-                                                     g->rp_in, g->col_in, s.lcol);
-            ALB_CK(cudaGetLastError());
+            ALB_TRY(fill_rows_chunked(s.lrow, s.nlong, s.perm, s.inv, g->rp_in, g->col_in, s.lptr,
+                                      false, s.lcol, fill_grid, st));
         }
         k_vinit<<<grid_for(s.nwords, T), T, 0, st>>>(n, s.nwords, s.ideg, s.vinit, dcnt);
         ALB_CK(cudaGetLastError());

@@ -9,6 +9,9 @@
 //            p is the l whose S[l][p] holds its bit, so the int32 output is
 //            written once, at the end, as full 256-byte rows.
 //   D        one bit per position: V[p] == ~0 (the bypass test)
+//   A[l & 1] one bit per position: S[l][p] != 0. The 2 MB-per-2^24-vertex
+//            bitmap stays in L2 where the 8-byte frontier words do not, and a
+//            bottom-up gather fetches S[l][c] only when c's bit is set.
 //
 // bottom-up (k_ms_bu): warp per 32 positions; a full D word is skipped; each
 //   lane ORs S[l] over its row with 16-byte column loads and stops when every
@@ -27,6 +30,9 @@
 namespace alb {
 
 constexpr uint64_t kAll = ~0ull;
+// Packed list counters (rows << kMsBigShift | chunks), as in bfs.cu.
+constexpr int kMsBigShift = 38;
+constexpr unsigned long long kMsBigMask = (1ull << kMsBigShift) - 1;
 
 struct MsCtl {
     int32_t level, dir, prev_dir, q_valid, done, err, policy, base;  // base: level of S[0]
@@ -49,19 +55,24 @@ struct MsArgs {
     const int4 *col4;
     const int64_t *prow;
     const int32_t *pcol;
-    int64_t nlong;  // rows kept out of the slices, pulled one warp each
+    int64_t nlong;  // rows kept out of the slices, pulled in chunks
     const int32_t *lrow;
     const int64_t *lptr;
     const int32_t *lcol;
     uint64_t *V;
     uint64_t *S;  // K slots of npad words
     uint32_t *D;
+    uint32_t *A;  // 2 x nwords: frontier-nonzero bitmaps by level parity
     int32_t *q0, *q1;
     int32_t *big;  // frontier rows longer than kBigRow (top-down)
     int64_t *big_base;
     MsCtl *ctl;
     const float *mlp;
 };
+
+__device__ __forceinline__ uint32_t *nz_bits(const MsArgs &a, int L) {
+    return a.A + (int64_t)(L & 1) * a.nwords;
+}
 
 __device__ __forceinline__ uint64_t *slot(const MsArgs &a, int j) { return a.S + (int64_t)j * a.npad; }
 
@@ -81,6 +92,8 @@ __global__ void k_ms_init(MsArgs a, uint64_t unused) {
             if (!(p < a.n && a.ideg[p] > 0)) d |= 1u << b;
         }
         a.D[w] = d;
+        a.A[w] = 0;
+        a.A[a.nwords + w] = 0;
     }
 }
 
@@ -105,6 +118,7 @@ __global__ void k_ms_roots(MsArgs a, MsInit in) {
         if (olds == 0) {
             a.q0[atomicAdd(&s_nf, 1ull)] = p;
             atomicAdd(&s_mf, (unsigned long long)a.odeg[p]);
+            atomicOr(a.A + (p >> 5), 1u << (p & 31));  // level 0: A[0]
         }
         // bit i belongs to root i alone, so every root counts once (its bit
         // may already be set in V when p has no sources: V starts full there)
@@ -153,8 +167,16 @@ __global__ void k_ms_roots(MsArgs a, MsInit in) {
 
 // Bottom-up over S[j] -> S[j+1]. kBypass: skip words whose 32 positions are
 // done; kEarly: stop a row once every root is accounted for, or at padding.
-template <bool kBypass, bool kEarly>
-__global__ void k_ms_bu(MsArgs a, int j) {
+// kFilt: test the nonzero bitmap before each 8-byte frontier fetch. It pays
+// when few sources are in the frontier (the fetches it saves miss L2) and
+// costs a dependent round trip per group when most are, so the host picks it
+// from the frontier's share of all entries.
+// Launched with kMsBuBlock threads; the bound keeps it at 48 registers
+// (5 blocks, 40 warps per SM) without spills.
+constexpr int kMsBuBlock = 256;
+
+template <bool kBypass, bool kEarly, bool kFilt>
+__global__ void __launch_bounds__(kMsBuBlock, 5) k_ms_bu(MsArgs a, int j) {
     const uint64_t *F = slot(a, j);
     uint64_t *N = slot(a, j + 1);
     const int lane = threadIdx.x & 31;
@@ -162,16 +184,20 @@ __global__ void k_ms_bu(MsArgs a, int j) {
     const int64_t stride = (int64_t)gridDim.x * wpb;
     const int L = a.ctl->level;
     const int k = (L + 1) % 3;
+    const uint32_t *Az = nz_bits(a, L);
+    uint32_t *An = nz_bits(a, L + 1);
     unsigned long long cn = 0, cbits = 0, cmo = 0, cmi = 0, cfull = 0, cedges = 0, bytes = 0;
     unsigned long long cdone = 0;
+    const uint64_t pol = l2_evict_first();
     for (int64_t w = blockIdx.x * wpb + (threadIdx.x >> 5); w < a.nwords; w += stride) {
         const uint32_t d = __ldg(a.D + w);
         const int64_t p = w * 32 + lane;
         if (kBypass && d == kFull) {
             N[p] = 0;
+            if (lane == 0) An[w] = 0;
             continue;
         }
-        bytes += 16;
+        bytes += 8;  // V[p]
         const uint64_t vis = __ldg(a.V + p);
         bool active = vis != kAll;
         int32_t ng = 0;
@@ -182,25 +208,48 @@ __global__ void k_ms_bu(MsArgs a, int j) {
             cp = a.col4 + (__ldg(a.slice_off + s) >> 2) + (p & (a.C - 1));
         }
         uint64_t acc = 0;
+        // group g+1 is requested before group g's frontier fetches, so each
+        // lane keeps a column load in flight while it waits on the gathers
+        const int32_t pp = (int32_t)p;
+        int4 c = make_int4(pp, pp, pp, pp);
+        if (active && ng > 0) c = ld_stream(cp, pol);
         for (int32_t g = 0;; g++) {
             active = active && g < ng;
             if (!__any_sync(kFull, active)) break;
-            bytes += 16ull * 32;
             if (!active) continue;
-            const int4 c = ld_nc(cp + (int64_t)g * a.C);
+            int4 nx = make_int4(pp, pp, pp, pp);
+            if (g + 1 < ng) nx = ld_stream(cp + (int64_t)(g + 1) * a.C, pol);
             // padding entries hold p itself: S[j][p] only has bits already in
             // V[p], so OR-ing it changes nothing
-            acc |= __ldg(F + c.x) | __ldg(F + c.y) | __ldg(F + c.z) | __ldg(F + c.w);
-            if (kEarly && (c.w == (int32_t)p || (acc | vis) == kAll)) active = false;
+            if (kFilt) {
+                const uint32_t z0 = __ldg(Az + (c.x >> 5)), z1 = __ldg(Az + (c.y >> 5)),
+                               z2 = __ldg(Az + (c.z >> 5)), z3 = __ldg(Az + (c.w >> 5));
+                const bool h0 = (z0 >> (c.x & 31)) & 1u, h1 = (z1 >> (c.y & 31)) & 1u,
+                           h2 = (z2 >> (c.z & 31)) & 1u, h3 = (z3 >> (c.w & 31)) & 1u;
+                if (h0) acc |= __ldg(F + c.x);
+                if (h1) acc |= __ldg(F + c.y);
+                if (h2) acc |= __ldg(F + c.z);
+                if (h3) acc |= __ldg(F + c.w);
+                // four columns, four bitmap words, the frontier words fetched
+                bytes += 32 + 8 * (h0 + h1 + h2 + h3);
+            } else {
+                acc |= __ldg(F + c.x) | __ldg(F + c.y) | __ldg(F + c.z) | __ldg(F + c.w);
+                bytes += 48;  // four columns and their four frontier words
+            }
+            if (kEarly && (c.w == pp || (acc | vis) == kAll)) active = false;
+            c = nx;
         }
         const uint64_t nb = acc & ~vis;
         N[p] = nb;
+        const unsigned nzm = __ballot_sync(kFull, nb != 0);
+        if (lane == 0) An[w] = nzm;
         bool done_now = false;
         if (nb) {
             const uint64_t nv = vis | nb;
             a.V[p] = nv;
             const int pc = __popcll(nb);
             const int32_t od = __ldg(a.odeg + p);
+            bytes += 12;  // V[p] written, push degree
             cn++;
             cbits += pc;
             cmo += od;
@@ -223,6 +272,7 @@ __global__ void k_ms_bu(MsArgs a, int j) {
     cmi = warp_sum(cmi);
     cedges = warp_sum(cedges);
     cdone = warp_sum(cdone);
+    bytes = warp_sum(bytes);
     if (lane == 0) {
         if (cn) {
             atomicAdd(&a.ctl->acc_n[k], cn);
@@ -243,10 +293,39 @@ __device__ __forceinline__ uint64_t warp_or64(uint64_t v) {
     return v;
 }
 
-// Long rows (kept out of the slices): one warp per row ORs the frontier
-// words of 32 sources per step and stops once every root is accounted for.
+// Long rows (kept out of the slices), head pass: one warp per long row some
+// root has not visited ORs the frontier words of its first kLongChunk
+// sources, 32 per step (fetched where the nonzero bitmap has a bit when filt
+// is set), and stops once every root is accounted for. New bits go into N[p]
+// by atomicOr (the slice pass wrote 0 there). A row still missing roots with
+// sources left joins the continuation list (nbig[L % 3], big, big_base) for
+// k_ms_bu_long_tail; k_ms_bu_long_fin folds N[p] into the state.
 template <bool kEarly>
-__global__ void k_ms_bu_long(MsArgs a, int j) {
+__device__ __forceinline__ uint64_t ms_long_scan(const MsArgs &a, const uint64_t *F,
+                                                 const uint32_t *Az, int filt, int64_t st,
+                                                 int64_t en, uint64_t acc, uint64_t vis,
+                                                 unsigned long long &bytes) {
+    const int lane = threadIdx.x & 31;
+    for (int64_t e0 = st; e0 < en; e0 += 32) {
+        const int64_t e = e0 + lane;
+        uint64_t f = 0;
+        bool fetched = false;
+        if (e < en) {
+            const int32_t c = __ldg(a.lcol + e);
+            fetched = !filt || ((__ldg(Az + (c >> 5)) >> (c & 31)) & 1u);
+            if (fetched) f = __ldg(F + c);
+        }
+        acc |= warp_or64(f);
+        // columns (and bitmap words when filtering), frontier words fetched
+        const int64_t ne = min((int64_t)32, en - e0);
+        bytes += (filt ? 8 : 4) * ne + 8 * __popc(__ballot_sync(kFull, fetched));
+        if (kEarly && (acc | vis) == kAll) break;
+    }
+    return acc;
+}
+
+template <bool kEarly>
+__global__ void k_ms_bu_long(MsArgs a, int j, int filt) {
     if (a.nlong == 0) return;
     const uint64_t *F = slot(a, j);
     uint64_t *N = slot(a, j + 1);
@@ -254,81 +333,162 @@ __global__ void k_ms_bu_long(MsArgs a, int j) {
     const int64_t wpb = blockDim.x >> 5;
     const int64_t nwarps = (int64_t)gridDim.x * wpb;
     const int L = a.ctl->level;
-    const int k = (L + 1) % 3;
-    unsigned long long cn = 0, cbits = 0, cmo = 0, cmi = 0, cfull = 0, cedges = 0, bytes = 0;
-    unsigned long long cdone = 0;
+    const uint32_t *Az = nz_bits(a, L);
+    unsigned long long *cont = &a.ctl->nbig[L % 3];
+    unsigned long long bytes = 0;
     for (int64_t i = blockIdx.x * wpb + (threadIdx.x >> 5); i < a.nlong; i += nwarps) {
         const int32_t p = __ldg(a.lrow + i);
         const uint64_t vis = __ldg(a.V + p);
         if (vis == kAll) continue;
         const int64_t st = __ldg(a.lptr + i), en = __ldg(a.lptr + i + 1);
+        const int64_t hen = min(en, st + kLongChunk);
         bytes += 24;
-        uint64_t acc = 0;
-        for (int64_t e0 = st; e0 < en; e0 += 32) {
-            const int64_t e = e0 + lane;
-            const uint64_t f = e < en ? __ldg(F + __ldg(a.lcol + e)) : 0ull;
-            acc |= warp_or64(f);
-            bytes += 128;
-            if (kEarly && (acc | vis) == kAll) break;
-        }
+        const uint64_t acc = ms_long_scan<kEarly>(a, F, Az, filt, st, hen, 0ull, vis, bytes);
         const uint64_t nb = acc & ~vis;
-        if (lane == 0 && nb) {
-            N[p] = nb;  // the slice pass wrote 0 here
-            const uint64_t nv = vis | nb;
-            a.V[p] = nv;
-            const int pc = __popcll(nb);
-            const int32_t od = __ldg(a.odeg + p);
-            cn++;
-            cbits += pc;
-            cmo += od;
-            cedges += (unsigned long long)pc * od;
-            if (nv == kAll) {
-                cdone++;
-                cmi += __ldg(a.ideg + p);
-                const uint32_t bit = 1u << (p & 31);
-                const uint32_t od2 = atomicOr(a.D + (p >> 5), bit);
-                cfull += (od2 != kFull && (od2 | bit) == kFull);
+        if (lane == 0) {
+            if (nb) atomicOr((unsigned long long *)N + p, (unsigned long long)nb);
+            if ((acc | vis) != kAll && hen < en) {
+                const unsigned long long nch =
+                    (unsigned long long)((en - hen + kLongChunk - 1) / kLongChunk);
+                const unsigned long long old = atomicAdd(cont, (1ull << kMsBigShift) | nch);
+                const int64_t idx = (int64_t)(old >> kMsBigShift);
+                a.big[idx] = (int32_t)i;
+                a.big_base[idx] = (int64_t)(old & kMsBigMask);
             }
         }
     }
-    if (lane == 0 && (cn || bytes)) {
-        if (cn) {
-            atomicAdd(&a.ctl->acc_n[k], cn);
-            atomicAdd(&a.ctl->acc_bits[k], cbits);
-            atomicAdd(&a.ctl->acc_mo[k], cmo);
-            atomicAdd(&a.ctl->acc_mi[k], cmi);
-            atomicAdd(&a.ctl->acc_edges[k], cedges);
-            if (cdone) atomicAdd(&a.ctl->acc_done[k], cdone);
+    if (lane == 0 && bytes) atomicAdd(&a.ctl->acc_bytes[(L + 1) % 3], bytes);
+}
+
+// Tail pass: chunk k of continuation entry jj covers sources
+// [lptr[i] + (1 + k - big_base[jj]) * kLongChunk, ...) of long row i = big[jj];
+// the scan starts from the bits N[p] already holds so it can stop early.
+template <bool kEarly>
+__global__ void k_ms_bu_long_tail(MsArgs a, int j, int filt) {
+    const int L = a.ctl->level;
+    const unsigned long long ctr = a.ctl->nbig[L % 3];
+    if (ctr == 0) return;
+    const int64_t nrows = (int64_t)(ctr >> kMsBigShift);
+    const int64_t total = (int64_t)(ctr & kMsBigMask);
+    const uint64_t *F = slot(a, j);
+    uint64_t *N = slot(a, j + 1);
+    const int lane = threadIdx.x & 31;
+    const int64_t wpb = blockDim.x >> 5;
+    const int64_t nwarps = (int64_t)gridDim.x * wpb;
+    const uint32_t *Az = nz_bits(a, L);
+    unsigned long long bytes = 0;
+    for (int64_t k = blockIdx.x * wpb + (threadIdx.x >> 5); k < total; k += nwarps) {
+        int64_t lo = 0, hi = nrows - 1;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi + 1) >> 1;
+            if (a.big_base[mid] <= k) lo = mid;
+            else hi = mid - 1;
         }
+        const int32_t i = a.big[lo];
+        const int32_t p = __ldg(a.lrow + i);
+        const uint64_t vis = __ldg(a.V + p);
+        const uint64_t have = __ldcg((const unsigned long long *)N + p);
+        if ((have | vis) == kAll) continue;
+        const int64_t st = __ldg(a.lptr + i) + (1 + k - a.big_base[lo]) * kLongChunk;
+        const int64_t en = min(__ldg(a.lptr + i + 1), st + kLongChunk);
+        bytes += 24;
+        const uint64_t acc = ms_long_scan<kEarly>(a, F, Az, filt, st, en, have, vis, bytes);
+        const uint64_t nb = acc & ~vis & ~have;
+        if (lane == 0 && nb) atomicOr((unsigned long long *)N + p, (unsigned long long)nb);
+    }
+    if (lane == 0 && bytes) atomicAdd(&a.ctl->acc_bytes[(L + 1) % 3], bytes);
+}
+
+// Long rows, second half: thread per long row folds N[p] into V, the
+// nonzero and done bitmaps and the level counters.
+__global__ void k_ms_bu_long_fin(MsArgs a, int j) {
+    if (a.nlong == 0) return;
+    const uint64_t *N = slot(a, j + 1);
+    const int L = a.ctl->level;
+    const int k = (L + 1) % 3;
+    uint32_t *An = nz_bits(a, L + 1);
+    unsigned long long cn = 0, cbits = 0, cmo = 0, cmi = 0, cfull = 0, cedges = 0, cdone = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.nlong;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t p = __ldg(a.lrow + i);
+        const uint64_t nb = N[p];
+        if (!nb) continue;
+        const uint64_t vis = a.V[p];
+        const uint64_t nv = vis | nb;
+        a.V[p] = nv;
+        const uint32_t bit = 1u << (p & 31);
+        atomicOr(An + (p >> 5), bit);
+        const int pc = __popcll(nb);
+        const int32_t od = __ldg(a.odeg + p);
+        cn++;
+        cbits += pc;
+        cmo += od;
+        cedges += (unsigned long long)pc * od;
+        if (nv == kAll) {
+            cdone++;
+            cmi += __ldg(a.ideg + p);
+            const uint32_t od2 = atomicOr(a.D + (p >> 5), bit);
+            cfull += (od2 != kFull && (od2 | bit) == kFull);
+        }
+    }
+    cn = warp_sum(cn);
+    cbits = warp_sum(cbits);
+    cmo = warp_sum(cmo);
+    cmi = warp_sum(cmi);
+    cfull = warp_sum(cfull);
+    cedges = warp_sum(cedges);
+    cdone = warp_sum(cdone);
+    if ((threadIdx.x & 31) == 0 && cn) {
+        atomicAdd(&a.ctl->acc_n[k], cn);
+        atomicAdd(&a.ctl->acc_bits[k], cbits);
+        atomicAdd(&a.ctl->acc_mo[k], cmo);
+        atomicAdd(&a.ctl->acc_mi[k], cmi);
+        atomicAdd(&a.ctl->acc_edges[k], cedges);
+        if (cdone) atomicAdd(&a.ctl->acc_done[k], cdone);
         if (cfull) atomicAdd(&a.ctl->acc_full[k], cfull);
-        atomicAdd(&a.ctl->acc_bytes[k], bytes);
     }
 }
 
-// S[j] -> queue (positions with a non-empty frontier word).
+// Frontier-nonzero bitmap A[L & 1] -> queue of level L: thread per bitmap
+// word, ballot/popc prefix sums within the warp, one atomic per warp.
 __global__ void k_ms_compact(MsArgs a, int j) {
-    const uint64_t *F = slot(a, j);
+    (void)j;
     const int L = a.ctl->level;
+    const uint32_t *Az = nz_bits(a, L);
     int32_t *Q = (L & 1) ? a.q1 : a.q0;
     unsigned long long *qslot = &a.ctl->qn[L % 3];
     const int lane = threadIdx.x & 31;
-    const int64_t wpb = blockDim.x >> 5;
-    const int64_t stride = (int64_t)gridDim.x * wpb;
-    for (int64_t w = blockIdx.x * wpb + (threadIdx.x >> 5); w < a.nwords; w += stride) {
-        const int64_t p = w * 32 + lane;
-        const bool f = __ldg(F + p) != 0;
-        const unsigned m = __ballot_sync(kFull, f);
-        if (!m) continue;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    // warp-uniform bound: every lane reaches the shuffles
+    for (int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) & ~31ll; w0 < a.nwords;
+         w0 += stride) {
+        const int64_t w = w0 + lane;
+        uint32_t m = w < a.nwords ? __ldg(Az + w) : 0u;
+        const int64_t cnt = __popc(m);
+        const int64_t inc = warp_inclusive_scan(cnt);
+        const int64_t total = __shfl_sync(kFull, inc, 31);
+        if (total == 0) continue;
         unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(qslot, (unsigned long long)__popc(m));
-        base = __shfl_sync(kFull, base, 0);
-        if (f) Q[base + __popc(m & lanemask_lt())] = (int32_t)p;
+        if (lane == 31) base = atomicAdd(qslot, (unsigned long long)total);
+        base = __shfl_sync(kFull, base, 31);
+        int64_t o = (int64_t)base + inc - cnt;
+        while (m) {
+            const int b = __ffs(m) - 1;
+            m &= m - 1;
+            Q[o++] = (int32_t)(w * 32 + b);
+        }
     }
 }
 
+// One pushed edge: the roots f reaching v this level; true when this push
+// made N[v] nonzero (v joins the next queue). N[v] is read first so that the
+// many pushes into a hub stop issuing atomics once its word holds their bits.
 __device__ __forceinline__ bool ms_push(const MsArgs &a, uint64_t *N, int32_t v, uint64_t f) {
-    const uint64_t nb = f & ~__ldg(a.V + v);
-    return nb && atomicOr((unsigned long long *)N + v, nb) == 0;
+    const uint64_t vis = __ldg(a.V + v);
+    const uint64_t cur = __ldcg((const unsigned long long *)N + v);
+    const uint64_t nb = f & ~vis;
+    if (!nb || !(nb & ~cur)) return false;  // nothing new (cur != 0: already queued)
+    return atomicOr((unsigned long long *)N + v, nb) == 0;
 }
 
 __device__ __forceinline__ void ms_append(int32_t *NQ, unsigned long long *nq_slot, bool claimed,
@@ -343,8 +503,6 @@ __device__ __forceinline__ void ms_append(int32_t *NQ, unsigned long long *nq_sl
     if (claimed) NQ[base + __popc(cm & lanemask_lt())] = v;
 }
 
-constexpr int kMsBigShift = 38;
-constexpr unsigned long long kMsBigMask = (1ull << kMsBigShift) - 1;
 
 __global__ void k_ms_td(MsArgs a, int j) {
     const uint64_t *F = slot(a, j);
@@ -454,11 +612,13 @@ __global__ void k_ms_td_finish(MsArgs a, int j) {
     const int32_t *NQ = (L & 1) ? a.q0 : a.q1;
     const int64_t nqlen = (int64_t)a.ctl->qn[(L + 1) % 3];
     const int k = (L + 1) % 3;
+    uint32_t *An = nz_bits(a, L + 1);  // zeroed before the level
     unsigned long long cn = 0, cbits = 0, cmo = 0, cmi = 0, cfull = 0, cedges = 0, cdone = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nqlen;
          i += (int64_t)gridDim.x * blockDim.x) {
         const int32_t v = NQ[i];
         const uint64_t nb = N[v];
+        atomicOr(An + (v >> 5), 1u << (v & 31));
         const uint64_t old = a.V[v];  // only this thread writes V[v] in this kernel
         const uint64_t nv = old | nb;
         a.V[v] = nv;
@@ -560,28 +720,80 @@ __global__ void k_ms_end(MsArgs a, int dir) {
     }
 }
 
-// Levels of every (vertex, root) pair from the snapshots S[0..nslots):
-// thread (p, i) finds the slot holding bit i of p. Rows of 64 int32 per
-// vertex (original id), written whole.
-__global__ void k_ms_expand(MsArgs a, int nslots, int base, int first, int nroots, int32_t *out) {
-    const int64_t total = a.n * 64;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
-         t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t p = t >> 6;
-        const int i = (int)(t & 63);
-        const uint64_t bit = 1ull << i;
-        int32_t lvl = -1;
-        for (int jj = 0; jj < nslots; jj++)
-            if (__ldg(a.S + (int64_t)jj * a.npad + p) & bit) {
-                lvl = base + jj;
-                break;
+// Writes the levels held by snapshot slots [0, nslots) (levels base ..) into
+// the vertex-major n x 64 output. Half a warp per position: lane q of the
+// half owns roots 4q .. 4q+3 and writes them as one 16-byte store, so a
+// position's 256-byte output row is one contiguous burst. The slots are read
+// once per position (lane q loads slot q and q+16) and shared with shuffles.
+// Each warp takes kExpandUnroll pairs of positions per step and issues all
+// their loads before the first shuffle, to keep enough bytes in flight.
+// A root's bit is set in exactly one slot, so the slots can be scanned in any
+// order. kFirst: the first flush writes every entry (-1 where unreached and
+// for root columns >= nroots); later flushes write only the levels found.
+constexpr int kExpandUnroll = 4;
+
+template <bool kFirst, bool kVec>
+__global__ void k_ms_expand(MsArgs a, int nslots, int base, int nroots, int32_t *out) {
+    const int lane = threadIdx.x & 31, q = lane & 15;
+    const int64_t total = a.n * 16;
+    const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int first_cnt = min(16, nslots);
+    // the loop bound is warp-uniform so that every lane reaches the shuffles
+    for (int64_t t0 = gw * 32 * kExpandUnroll; t0 < total; t0 += nw * 32 * kExpandUnroll) {
+        uint64_t mine[kExpandUnroll];
+        int32_t vid[kExpandUnroll];
+#pragma unroll
+        for (int u = 0; u < kExpandUnroll; u++) {
+            const int64_t t = t0 + u * 32 + lane;
+            const bool ok = t < total;
+            const int64_t p = ok ? t >> 4 : 0;
+            mine[u] = (ok && q < nslots) ? __ldcs(a.S + (int64_t)q * a.npad + p) : 0ull;
+            vid[u] = ok ? __ldg(a.perm + p) : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < kExpandUnroll; u++) {
+            const int64_t t = t0 + u * 32 + lane;
+            const bool ok = t < total;
+            const int64_t p = ok ? t >> 4 : 0;
+            int32_t l[4] = {-1, -1, -1, -1};
+            for (int k = 0; k < first_cnt; k++) {
+                const uint64_t sv = __shfl_sync(kFull, mine[u], k, 16);
+                const uint32_t b = (uint32_t)(sv >> (4 * q)) & 0xFu;
+                if (b) {
+#pragma unroll
+                    for (int r = 0; r < 4; r++)
+                        if ((b >> r) & 1u) l[r] = base + k;
+                }
             }
-        int32_t *o = out + (int64_t)__ldg(a.perm + p) * 64 + i;
-        if (i >= nroots) lvl = -1;
-        if (first)
-            *o = lvl;
-        else if (lvl >= 0)
-            *o = lvl;
+            for (int c0 = 16; c0 < nslots; c0 += 16) {  // more than 16 levels held
+                const int js = c0 + q;
+                const uint64_t m2 =
+                    (ok && js < nslots) ? __ldcs(a.S + (int64_t)js * a.npad + p) : 0ull;
+                const int cnt = min(16, nslots - c0);
+                for (int k = 0; k < cnt; k++) {
+                    const uint64_t sv = __shfl_sync(kFull, m2, k, 16);
+                    const uint32_t b = (uint32_t)(sv >> (4 * q)) & 0xFu;
+                    if (b) {
+#pragma unroll
+                        for (int r = 0; r < 4; r++)
+                            if ((b >> r) & 1u) l[r] = base + c0 + k;
+                    }
+                }
+            }
+            if (!ok) continue;
+#pragma unroll
+            for (int r = 0; r < 4; r++)
+                if (4 * q + r >= nroots) l[r] = -1;
+            int32_t *o = out + (int64_t)vid[u] * 64 + 4 * q;
+            if (kFirst && kVec) {
+                __stcs(reinterpret_cast<int4 *>(o), make_int4(l[0], l[1], l[2], l[3]));
+            } else {
+#pragma unroll
+                for (int r = 0; r < 4; r++)
+                    if (kFirst || l[r] >= 0) o[r] = l[r];
+            }
+        }
     }
 }
 
@@ -589,7 +801,7 @@ struct MsScratch {
     bool ready = false;
     int32_t K = 0;
     uint64_t *V = nullptr, *S = nullptr;
-    uint32_t *D = nullptr;
+    uint32_t *D = nullptr, *A = nullptr;
     int32_t *q0 = nullptr, *q1 = nullptr, *big = nullptr;
     int64_t *big_base = nullptr;
     MsCtl *ctl = nullptr, *h_ctl = nullptr;
@@ -611,6 +823,7 @@ void ms_scratch_free(alb_graph *g) {
     dfree(m.V);
     dfree(m.S);
     dfree(m.D);
+    dfree(m.A);
     dfree(m.q0);
     dfree(m.q1);
     dfree(m.big);
@@ -624,6 +837,17 @@ void ms_scratch_free(alb_graph *g) {
 
 namespace {
 
+void launch_expand(const MsArgs &a, int nslots, int base, bool first, int nroots, int32_t *out,
+                   unsigned grid, cudaStream_t st) {
+    const bool vec = ((uintptr_t)out & 15) == 0;
+    if (first && vec)
+        k_ms_expand<true, true><<<grid, 256, 0, st>>>(a, nslots, base, nroots, out);
+    else if (first)
+        k_ms_expand<true, false><<<grid, 256, 0, st>>>(a, nslots, base, nroots, out);
+    else
+        k_ms_expand<false, false><<<grid, 256, 0, st>>>(a, nslots, base, nroots, out);
+}
+
 alb_status ms_alloc(alb_graph *g, MsScratch &m) {
     if (m.ready) return ALB_OK;
     const Sell &s = g->sell;
@@ -632,6 +856,7 @@ alb_status ms_alloc(alb_graph *g, MsScratch &m) {
     ALB_TRY(dmalloc((void **)&m.V, sizeof(uint64_t) * npad, "msbfs visited"));
     ALB_TRY(dmalloc((void **)&m.S, sizeof(uint64_t) * npad * m.K, "msbfs frontier snapshots"));
     ALB_TRY(dmalloc((void **)&m.D, sizeof(uint32_t) * s.nwords, "msbfs done bitmap"));
+    ALB_TRY(dmalloc((void **)&m.A, sizeof(uint32_t) * 2 * s.nwords, "msbfs frontier-nonzero bitmaps"));
     ALB_TRY(dmalloc((void **)&m.q0, sizeof(int32_t) * npad, "msbfs queue"));
     ALB_TRY(dmalloc((void **)&m.q1, sizeof(int32_t) * npad, "msbfs queue"));
     ALB_TRY(dmalloc((void **)&m.big, sizeof(int32_t) * npad, "msbfs long-row list"));
@@ -668,6 +893,7 @@ MsArgs ms_args(alb_graph *g, MsScratch &m) {
     a.V = m.V;
     a.S = m.S;
     a.D = m.D;
+    a.A = m.A;
     a.q0 = m.q0;
     a.q1 = m.q1;
     a.big = m.big;
@@ -714,6 +940,7 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
     cudaStream_t stream = g->stream;
     const int block = o.block;
     const unsigned wide = (unsigned)(g->num_sms * std::max(1, 2048 / block));
+    const unsigned bu_grid = (unsigned)(g->num_sms * (2048 / kMsBuBlock));
     MsInit in;
     std::memset(&in, 0, sizeof(in));
     for (int i = 0; i < nroots; i++) in.roots[i] = roots[i];
@@ -774,8 +1001,7 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
             // snapshot store full: write out levels [base, base + K - 1) and
             // restart the store from the current frontier
             if (d_levels) {
-                k_ms_expand<<<wide, 256, 0, stream>>>(a, m.K - 1, base, first_flush ? 1 : 0,
-                                                      nroots, d_levels);
+                launch_expand(a, m.K - 1, base, first_flush, nroots, d_levels, wide, stream);
                 launches++;
             }
             first_flush = false;
@@ -796,6 +1022,8 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
         rec.active_slices = h->active_words;
         rec.step_us = -1.f;
         const bool q_valid = h->q_valid != 0;
+        // nonzero-bitmap filter when under 1/8 of all entries point into the frontier
+        const int filt = (h->mf < s.m_in / 8) ? 1 : 0;
         auto launch_step = [&](int d) -> alb_status {
             if (d == ALB_DIR_TOPDOWN) {
                 if (!q_valid) {
@@ -804,18 +1032,30 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
                 }
                 ALB_CK(cudaMemsetAsync(a.S + (int64_t)(j + 1) * a.npad, 0,
                                        sizeof(uint64_t) * a.npad, stream));
+                ALB_CK(cudaMemsetAsync(a.A + (int64_t)((L + 1) & 1) * a.nwords, 0,
+                                       sizeof(uint32_t) * a.nwords, stream));
                 k_ms_td<<<wide, block, 0, stream>>>(a, j);
                 k_ms_td_big<<<wide, block, 0, stream>>>(a, j);
                 k_ms_td_finish<<<wide, block, 0, stream>>>(a, j);
                 launches += 3;
             } else if (d == ALB_DIR_BOTTOMUP) {
-                k_ms_bu<true, true><<<wide, block, 0, stream>>>(a, j);
-                k_ms_bu_long<true><<<wide, block, 0, stream>>>(a, j);
-                launches += 2;
+                if (filt)
+                    k_ms_bu<true, true, true><<<bu_grid, kMsBuBlock, 0, stream>>>(a, j);
+                else
+                    k_ms_bu<true, true, false><<<bu_grid, kMsBuBlock, 0, stream>>>(a, j);
+                k_ms_bu_long<true><<<wide, block, 0, stream>>>(a, j, filt);
+                k_ms_bu_long_tail<true><<<wide, block, 0, stream>>>(a, j, filt);
+                k_ms_bu_long_fin<<<wide, block, 0, stream>>>(a, j);
+                launches += 4;
             } else {
-                k_ms_bu<false, false><<<wide, block, 0, stream>>>(a, j);
-                k_ms_bu_long<false><<<wide, block, 0, stream>>>(a, j);
-                launches += 2;
+                if (filt)
+                    k_ms_bu<false, false, true><<<bu_grid, kMsBuBlock, 0, stream>>>(a, j);
+                else
+                    k_ms_bu<false, false, false><<<bu_grid, kMsBuBlock, 0, stream>>>(a, j);
+                k_ms_bu_long<false><<<wide, block, 0, stream>>>(a, j, filt);
+                k_ms_bu_long_tail<false><<<wide, block, 0, stream>>>(a, j, filt);
+                k_ms_bu_long_fin<<<wide, block, 0, stream>>>(a, j);
+                launches += 4;
             }
             return ALB_OK;
         };
@@ -874,7 +1114,7 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
             const int k = (L + 1) % 3;
             rec.bytes = dir == ALB_DIR_TOPDOWN
                             ? (int64_t)(20 * rec.nf + 16 * rec.mf + 16 * (int64_t)h->acc_n[k])
-                            : (int64_t)h->acc_bytes[k] + 8 * 3 * a.npad;
+                            : (int64_t)h->acc_bytes[k] + 8 * a.npad + 8 * a.nwords;
             trace->push_back(rec);
         }
     }
@@ -883,8 +1123,8 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
     if (!h->done) return fail(ALB_ERR_DEVICE, "msbfs: level cap reached");
     if (d_levels) {
         const int nslots = h->level - base;  // slots 0 .. level-base-1 hold levels
-        k_ms_expand<<<wide, 256, 0, stream>>>(a, std::min(nslots, m.K), base,
-                                              first_flush ? 1 : 0, nroots, d_levels);
+        launch_expand(a, std::min(nslots, m.K), base, first_flush, nroots, d_levels, wide,
+                      stream);
         launches++;
     }
     ALB_CK(cudaGetLastError());

@@ -179,11 +179,17 @@ typedef struct {
                               only; -1 otherwise) */
     int32_t pad_;
 } alb_level_rec;
-/* Algorithmic bytes: bottom-up = sum over non-bypassed 32-row words of
- * 16 + 16*C*K (K = int4 column groups the warp loaded) + 12*nwords (visited
- * read, next-frontier write, frontier read once); top-down = 20*|F| +
- * 8*sum(deg F) + 12*|F_next| (queue + offsets, adjacency + visited probes,
- * level/parent/queue writes). */
+/* Algorithmic bytes (the elements the step reads or writes, counted by the
+ * kernels themselves): bottom-up = 12*nwords (visited read and write, next
+ * frontier write) + 32 per row per 4-column group scanned (four int32
+ * columns, the four frontier words they select) + 20 per row reached (level,
+ * parent, the parent's id, two degrees) + 8 per long-row source scanned;
+ * top-down = 20*|F| + 8*sum(deg F) + 12*|F_next| (queue + offsets, adjacency
+ * + visited probes, level/parent/queue writes). The 64-root batched BFS
+ * counts the same way with 8-byte frontier and visited words: 8 per row
+ * pulled, 48 per 4-column group (32 + 8 per frontier word fetched when the
+ * nonzero bitmap is consulted), 12 per row reached, 8*npad + 8*nwords for the
+ * next-frontier, done and nonzero-bitmap words. */
 
 /* Per-level records of the last traversal on g (requires opts.trace). */
 alb_status alb_level_trace(const alb_graph *g, int32_t cap, alb_level_rec *out,
