@@ -328,28 +328,36 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r) {
     const uint32_t *F = (L & 1) ? a.bm1 : a.bm0;
     uint32_t *N = (L & 1) ? a.bm0 : a.bm1;
     const int lane = threadIdx.x & 31;
-    const int64_t wpb = blockDim.x >> 5;
-    const int64_t gw = (int64_t)r.bid * wpb + (threadIdx.x >> 5);
-    const int64_t stride = (int64_t)r.nblk * wpb;
+    (void)r;  // words are handed out by the level's counter, not by block index
     const int32_t C = a.C, log2C = a.log2C;
     const int32_t lvl = L + 1;
-    unsigned long long cn = 0, cmo = 0, cmi = 0, full = 0, bytes = 0;
+    unsigned cn = 0, full = 0;
+    unsigned long long cmo = 0, cmi = 0, bytes = 0;
     const uint64_t pol = l2_evict_first();
-    for (int64_t w = gw; w < a.nwords; w += stride) {
-        const uint32_t vis = ld_bits<kPersist>(a.vis + w);
+    // words come in runs from the level's counter; the next word's visited
+    // mask is requested one iteration ahead (only the warp that takes a word
+    // writes it during the level), and a word's slice geometry is requested
+    // without waiting for its mask
+    unsigned long long *ctr = &a.ctl->work[L % 3];
+    WordRuns runs;
+    int64_t w = runs.first(ctr, a.nwords);
+    uint32_t vis_next = w < a.nwords ? ld_bits<kPersist>(a.vis + w) : kFull;
+    for (int64_t wn; w < a.nwords; w = wn) {
+        const uint32_t vis = vis_next;
+        wn = runs.after(w, ctr, a.nwords);
+        if (wn < a.nwords) vis_next = ld_bits<kPersist>(a.vis + wn);
         if (kBypass && vis == kFull) {
             if (lane == 0) N[w] = 0;
             continue;
         }
         const int32_t p = (int32_t)(w * 32 + lane);
-        const int64_t s = (int64_t)p >> log2C;
+        // rows past n are preset visited; clamp their slice index
+        const int64_t s = (int64_t)(p < a.n ? p : a.n - 1) >> log2C;
+        const int32_t wd = __ldg(a.width + s);
+        const int64_t so = __ldg(a.slice_off + s);
         bool active = !((vis >> lane) & 1u);
-        int32_t ng = 0;
-        const int4 *cp = nullptr;
-        if (active) {
-            ng = (__ldg(a.width + s) + 3) >> 2;
-            cp = a.col4 + (__ldg(a.slice_off + s) >> 2) + (p & (C - 1));
-        }
+        const int32_t ng = active ? (wd + 3) >> 2 : 0;
+        const int4 *cp = a.col4 + (so >> 2) + (p & (C - 1));
         int32_t found = -1;
         // group j+1 is requested before group j's frontier tests, so each lane
         // keeps one column load in flight while it waits on the bitmap
@@ -411,11 +419,11 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r) {
     if (lane == 0 && (cn || full || bytes)) {
         const int k = (L + 1) % 3;
         if (cn) {
-            atomicAdd(&a.ctl->acc_n[k], cn);
+            atomicAdd(&a.ctl->acc_n[k], (unsigned long long)cn);
             atomicAdd(&a.ctl->acc_mo[k], cmo);
             atomicAdd(&a.ctl->acc_mi[k], cmi);
         }
-        if (full) atomicAdd(&a.ctl->acc_full[k], full);
+        if (full) atomicAdd(&a.ctl->acc_full[k], (unsigned long long)full);
         if (bytes) atomicAdd(&a.ctl->acc_bytes[k], bytes);
     }
 }
@@ -619,6 +627,7 @@ __global__ void k_decide(BfsArgs a, int forced, cudaGraphConditionalHandle sw) {
         a.ctl->acc_full[k] = 0;
         a.ctl->acc_bytes[k] = 0;
         a.ctl->nbig[k] = 0;
+        a.ctl->work[k] = 0;
         a.ctl->qn[k] = 0;
         unsigned branch;
         if (dir == ALB_DIR_TOPDOWN)
@@ -648,8 +657,12 @@ __global__ void k_td_finish(BfsArgs a) {
     td_finish_phase<false>(a, a.ctl->level, Range{(int)blockIdx.x, (int)gridDim.x});
 }
 
+// The slice pass runs with kBuBlock threads whatever the loop's block size:
+// the bound holds it at 48 registers (5 blocks, 40 warps per SM).
+constexpr unsigned kBuBlock = 256;
+
 template <bool kBypass, bool kEarly>
-__global__ void k_bu(BfsArgs a) {
+__global__ void __launch_bounds__(kBuBlock, 5) k_bu(BfsArgs a) {
     bu_phase<false, kBypass, kEarly>(a, a.ctl->level, Range{(int)blockIdx.x, (int)gridDim.x});
 }
 
@@ -737,6 +750,7 @@ __global__ void __launch_bounds__(256) k_persistent(BfsArgs a) {
                     a.ctl->acc_full[k] = 0;
                     a.ctl->acc_bytes[k] = 0;
                     a.ctl->nbig[k] = 0;
+                    a.ctl->work[k] = 0;
                     a.ctl->qn[k] = 0;
                 }
             }
@@ -936,12 +950,24 @@ namespace {
 struct Launch {
     unsigned grid;
     unsigned block;
+    int sms;
 };
 
 Launch level_launch(const alb_graph *g, int block) {
     // every level kernel is a grid-stride loop: fill the GPU once
     const int per_sm = std::max(1, 2048 / block);
-    return Launch{(unsigned)(g->num_sms * per_sm), (unsigned)block};
+    return Launch{(unsigned)(g->num_sms * per_sm), (unsigned)block, g->num_sms};
+}
+
+Launch with_block(const Launch &w, unsigned block) { return Launch{w.grid, block, w.sms}; }
+
+// The same launch with as many blocks as are resident at once for func (its
+// registers can allow fewer than 2048 threads per SM): a grid-stride kernel
+// then runs in one wave instead of leaving a partial second wave.
+Launch fit(const void *func, const Launch &w) {
+    const int per = resident_blocks(func, (int)w.block);
+    if (per <= 0) return w;
+    return Launch{(unsigned)(w.sms * per), w.block, w.sms};
 }
 
 alb_status add_kernel_node(cudaGraph_t graph, cudaGraphNode_t *node, const cudaGraphNode_t *deps,
@@ -993,35 +1019,35 @@ alb_status build_loop_graph(alb_graph *g, int block) {
     {  // 0: top-down, queue ready
         cudaGraph_t b0 = sp.conditional.phGraph_out[0];
         cudaGraphNode_t t, bg, f;
-        ALB_TRY(add_kernel_node(b0, &t, nullptr, 0, (void *)k_td, wide, aargs));
-        ALB_TRY(add_kernel_node(b0, &bg, &t, 1, (void *)k_td_big, wide, aargs));
+        ALB_TRY(add_kernel_node(b0, &t, nullptr, 0, (void *)k_td, fit((const void *)k_td, wide), aargs));
+        ALB_TRY(add_kernel_node(b0, &bg, &t, 1, (void *)k_td_big, fit((const void *)k_td_big, wide), aargs));
         ALB_TRY(add_kernel_node(b0, &f, &bg, 1, (void *)k_td_finish, wide, aargs));
     }
     {  // 1: compaction / clear, then top-down
         cudaGraph_t b1 = sp.conditional.phGraph_out[1];
         cudaGraphNode_t pr, t, bg, f;
         ALB_TRY(add_kernel_node(b1, &pr, nullptr, 0, (void *)k_prep, wide, aargs));
-        ALB_TRY(add_kernel_node(b1, &t, &pr, 1, (void *)k_td, wide, aargs));
-        ALB_TRY(add_kernel_node(b1, &bg, &t, 1, (void *)k_td_big, wide, aargs));
+        ALB_TRY(add_kernel_node(b1, &t, &pr, 1, (void *)k_td, fit((const void *)k_td, wide), aargs));
+        ALB_TRY(add_kernel_node(b1, &bg, &t, 1, (void *)k_td_big, fit((const void *)k_td_big, wide), aargs));
         ALB_TRY(add_kernel_node(b1, &f, &bg, 1, (void *)k_td_finish, wide, aargs));
     }
     {  // 2: the long rows (head, tail), then bottom-up with bypass
         cudaGraphNode_t b, l, t;
         ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[2], &l, nullptr, 0,
-                                (void *)k_bu_long<true>, wide, aargs));
+                                (void *)k_bu_long<true>, fit((const void *)k_bu_long<true>, wide), aargs));
         ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[2], &t, &l, 1,
-                                (void *)k_bu_long_tail<true>, wide, aargs));
+                                (void *)k_bu_long_tail<true>, fit((const void *)k_bu_long_tail<true>, wide), aargs));
         ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[2], &b, &t, 1,
-                                (void *)k_bu<true, true>, wide, aargs));
+                                (void *)k_bu<true, true>, fit((const void *)k_bu<true, true>, with_block(wide, kBuBlock)), aargs));
     }
     {  // 3: the long rows (head, tail), then bottom-up without bypass
         cudaGraphNode_t b, l, t;
         ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[3], &l, nullptr, 0,
-                                (void *)k_bu_long<false>, wide, aargs));
+                                (void *)k_bu_long<false>, fit((const void *)k_bu_long<false>, wide), aargs));
         ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[3], &t, &l, 1,
-                                (void *)k_bu_long_tail<false>, wide, aargs));
+                                (void *)k_bu_long_tail<false>, fit((const void *)k_bu_long_tail<false>, wide), aargs));
         ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[3], &b, &t, 1,
-                                (void *)k_bu<false, false>, wide, aargs));
+                                (void *)k_bu<false, false>, fit((const void *)k_bu<false, false>, with_block(wide, kBuBlock)), aargs));
     }
     void *eargs[] = {&a, &wh};
     cudaGraphNode_t nend;
@@ -1060,17 +1086,17 @@ alb_status run_host_loop(alb_graph *g, const BfsArgs &a, const alb_bfs_opts &o,
         if (e0) cudaEventRecord(e0, st);
         if (dir == ALB_DIR_TOPDOWN) {
             if (!h->q_valid || h->n_dirty) k_prep<<<wide.grid, wide.block, 0, st>>>(a);
-            k_td<<<wide.grid, wide.block, 0, st>>>(a);
-            k_td_big<<<wide.grid, wide.block, 0, st>>>(a);
+            { const Launch l = fit((const void *)k_td, wide); k_td<<<l.grid, l.block, 0, st>>>(a); }
+            { const Launch l = fit((const void *)k_td_big, wide); k_td_big<<<l.grid, l.block, 0, st>>>(a); }
             k_td_finish<<<wide.grid, wide.block, 0, st>>>(a);
         } else if (dir == ALB_DIR_BOTTOMUP) {
-            k_bu_long<true><<<wide.grid, wide.block, 0, st>>>(a);
-            k_bu_long_tail<true><<<wide.grid, wide.block, 0, st>>>(a);
-            k_bu<true, true><<<wide.grid, wide.block, 0, st>>>(a);
+            { const Launch l = fit((const void *)k_bu_long<true>, wide); k_bu_long<true><<<l.grid, l.block, 0, st>>>(a); }
+            { const Launch l = fit((const void *)k_bu_long_tail<true>, wide); k_bu_long_tail<true><<<l.grid, l.block, 0, st>>>(a); }
+            { const Launch l = fit((const void *)k_bu<true, true>, with_block(wide, kBuBlock)); k_bu<true, true><<<l.grid, l.block, 0, st>>>(a); }
         } else {
-            k_bu_long<false><<<wide.grid, wide.block, 0, st>>>(a);
-            k_bu_long_tail<false><<<wide.grid, wide.block, 0, st>>>(a);
-            k_bu<false, false><<<wide.grid, wide.block, 0, st>>>(a);
+            { const Launch l = fit((const void *)k_bu_long<false>, wide); k_bu_long<false><<<l.grid, l.block, 0, st>>>(a); }
+            { const Launch l = fit((const void *)k_bu_long_tail<false>, wide); k_bu_long_tail<false><<<l.grid, l.block, 0, st>>>(a); }
+            { const Launch l = fit((const void *)k_bu<false, false>, with_block(wide, kBuBlock)); k_bu<false, false><<<l.grid, l.block, 0, st>>>(a); }
         }
         if (e1) cudaEventRecord(e1, st);
         k_end<<<1, 32, 0, st>>>(a, 0);
@@ -1173,17 +1199,17 @@ alb_status bfs_impl(alb_graph *g, int32_t root, const alb_bfs_opts &o, int32_t *
 void launch_step(const BfsArgs &a, const Launch &wide, cudaStream_t st, int dir, const BfsCtl &h) {
     if (dir == ALB_DIR_TOPDOWN) {
         if (!h.q_valid || h.n_dirty) k_prep<<<wide.grid, wide.block, 0, st>>>(a);
-        k_td<<<wide.grid, wide.block, 0, st>>>(a);
-        k_td_big<<<wide.grid, wide.block, 0, st>>>(a);
+        { const Launch l = fit((const void *)k_td, wide); k_td<<<l.grid, l.block, 0, st>>>(a); }
+        { const Launch l = fit((const void *)k_td_big, wide); k_td_big<<<l.grid, l.block, 0, st>>>(a); }
         k_td_finish<<<wide.grid, wide.block, 0, st>>>(a);
     } else if (dir == ALB_DIR_BOTTOMUP) {
-        k_bu_long<true><<<wide.grid, wide.block, 0, st>>>(a);
-        k_bu_long_tail<true><<<wide.grid, wide.block, 0, st>>>(a);
-        k_bu<true, true><<<wide.grid, wide.block, 0, st>>>(a);
+        { const Launch l = fit((const void *)k_bu_long<true>, wide); k_bu_long<true><<<l.grid, l.block, 0, st>>>(a); }
+        { const Launch l = fit((const void *)k_bu_long_tail<true>, wide); k_bu_long_tail<true><<<l.grid, l.block, 0, st>>>(a); }
+        { const Launch l = fit((const void *)k_bu<true, true>, with_block(wide, kBuBlock)); k_bu<true, true><<<l.grid, l.block, 0, st>>>(a); }
     } else {
-        k_bu_long<false><<<wide.grid, wide.block, 0, st>>>(a);
-        k_bu_long_tail<false><<<wide.grid, wide.block, 0, st>>>(a);
-        k_bu<false, false><<<wide.grid, wide.block, 0, st>>>(a);
+        { const Launch l = fit((const void *)k_bu_long<false>, wide); k_bu_long<false><<<l.grid, l.block, 0, st>>>(a); }
+        { const Launch l = fit((const void *)k_bu_long_tail<false>, wide); k_bu_long_tail<false><<<l.grid, l.block, 0, st>>>(a); }
+        { const Launch l = fit((const void *)k_bu<false, false>, with_block(wide, kBuBlock)); k_bu<false, false><<<l.grid, l.block, 0, st>>>(a); }
     }
 }
 

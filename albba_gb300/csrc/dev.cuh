@@ -63,6 +63,38 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
     return t;
 }
 
+// Dynamic distribution of bitmap words to warps. Rows sorted by degree
+// inside each sigma window make a word's cost depend on its offset in the
+// window, so a fixed grid stride (a multiple of 32 warps) would hand one warp
+// the heavy offset of every window; instead each warp takes kGrabWords
+// consecutive words at a time from a counter shared by the launch, asking
+// for its next run one run ahead. Call from all lanes of a warp.
+constexpr int64_t kGrabWords = 8;
+
+__device__ __forceinline__ int64_t grab_words(unsigned long long *ctr) {
+    unsigned long long v = 0;
+    if ((threadIdx.x & 31) == 0) v = atomicAdd(ctr, (unsigned long long)kGrabWords);
+    return (int64_t)__shfl_sync(0xFFFFFFFFu, v, 0);
+}
+
+struct WordRuns {
+    int64_t end, next;  // end of the current run; start of the one after it
+    __device__ __forceinline__ int64_t first(unsigned long long *ctr, int64_t nwords) {
+        const int64_t cur = grab_words(ctr);
+        next = grab_words(ctr);
+        end = min(cur + kGrabWords, nwords);
+        return cur;
+    }
+    // the word after w (>= nwords when the launch's words are exhausted)
+    __device__ __forceinline__ int64_t after(int64_t w, unsigned long long *ctr, int64_t nwords) {
+        if (w + 1 < end) return w + 1;
+        const int64_t cur = next;
+        next = grab_words(ctr);
+        end = min(cur + kGrabWords, nwords);
+        return cur;
+    }
+};
+
 template <class T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
@@ -106,6 +138,7 @@ struct BfsCtl {
     int64_t reached, edges;  // running totals
     unsigned long long acc_n[3], acc_mo[3], acc_mi[3], acc_full[3], qn[3], acc_bytes[3];
     unsigned long long nbig[3];  // rows too long for one warp, per level slot
+    unsigned long long work[3];  // bottom-up word counter (grab_words), per level slot
     unsigned int bar_count, bar_gen;  // persistent-kernel grid barrier
     int32_t trace_cap, trace_len;
     int32_t level_cap;       // safety bound on the number of levels

@@ -17,6 +17,8 @@
 //   Self-loops are dropped, so the padding value doubles as an end marker.
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -47,6 +49,21 @@ alb_status dmalloc(void **p, size_t bytes, const char *what) {
 
 void dfree(void *p) {
     if (p) cudaFree(p);
+}
+
+int resident_blocks(const void *func, int block) {
+    static std::mutex mu;
+    static std::map<std::pair<const void *, int>, int> cache;
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find({func, block});
+    if (it != cache.end()) return it->second;
+    int per = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, func, block, 0) != cudaSuccess) {
+        cudaGetLastError();
+        per = 0;
+    }
+    cache[{func, block}] = per;
+    return per;
 }
 
 namespace {

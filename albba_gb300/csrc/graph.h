@@ -14,6 +14,9 @@ namespace alb {
 // Device allocation with host fault injection; returns ALB_OK or ALB_ERR_OOM.
 alb_status dmalloc(void **p, size_t bytes, const char *what);
 void dfree(void *p);
+// Blocks of `block` threads of func resident on one SM at once (cached per
+// function and block size; 0 if the query fails).
+int resident_blocks(const void *func, int block);
 
 // CUDA error check that records the failing call and returns ALB_ERR_CUDA.
 #define ALB_CK(call)                                                                 \

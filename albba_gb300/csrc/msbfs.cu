@@ -42,7 +42,7 @@ struct MsCtl {
     int64_t nf, mf, prev_nf, nu, mu, active_words;
     int64_t pairs, edges;  // (vertex, root) pairs reached; sum of their push degrees
     unsigned long long acc_n[3], acc_mo[3], acc_mi[3], acc_full[3], acc_bits[3], acc_edges[3],
-        qn[3], acc_bytes[3], acc_done[3], nbig[3];
+        qn[3], acc_bytes[3], acc_done[3], nbig[3], work[3];
     int64_t launches;
     float feat_mean_deg, feat_skew;
 };
@@ -180,17 +180,25 @@ __global__ void __launch_bounds__(kMsBuBlock, 5) k_ms_bu(MsArgs a, int j) {
     const uint64_t *F = slot(a, j);
     uint64_t *N = slot(a, j + 1);
     const int lane = threadIdx.x & 31;
-    const int64_t wpb = blockDim.x >> 5;
-    const int64_t stride = (int64_t)gridDim.x * wpb;
     const int L = a.ctl->level;
     const int k = (L + 1) % 3;
     const uint32_t *Az = nz_bits(a, L);
     uint32_t *An = nz_bits(a, L + 1);
-    unsigned long long cn = 0, cbits = 0, cmo = 0, cmi = 0, cfull = 0, cedges = 0, bytes = 0;
-    unsigned long long cdone = 0;
+    // per-thread counts fit 32 bits; degree sums and bytes need 64
+    unsigned cn = 0, cbits = 0, cfull = 0, cdone = 0;
+    unsigned long long cmo = 0, cmi = 0, cedges = 0, bytes = 0;
     const uint64_t pol = l2_evict_first();
-    for (int64_t w = blockIdx.x * wpb + (threadIdx.x >> 5); w < a.nwords; w += stride) {
-        const uint32_t d = __ldg(a.D + w);
+    // words come in runs from the level's counter; the next word's done mask
+    // is requested one iteration ahead, and a word's visited words and slice
+    // geometry are requested together
+    unsigned long long *ctr = &a.ctl->work[L % 3];
+    WordRuns runs;
+    int64_t w = runs.first(ctr, a.nwords);
+    uint32_t d_next = w < a.nwords ? __ldg(a.D + w) : kFull;
+    for (int64_t wn; w < a.nwords; w = wn) {
+        const uint32_t d = d_next;
+        wn = runs.after(w, ctr, a.nwords);
+        if (wn < a.nwords) d_next = __ldg(a.D + wn);
         const int64_t p = w * 32 + lane;
         if (kBypass && d == kFull) {
             N[p] = 0;
@@ -198,15 +206,15 @@ __global__ void __launch_bounds__(kMsBuBlock, 5) k_ms_bu(MsArgs a, int j) {
             continue;
         }
         bytes += 8;  // V[p]
+        // rows past n (padding of the last word) are preset visited; their
+        // slice index is clamped so the geometry loads stay in bounds
+        const int64_t s = (p < a.n ? p : a.n - 1) >> a.log2C;
         const uint64_t vis = __ldg(a.V + p);
+        const int32_t wd = __ldg(a.width + s);
+        const int64_t so = __ldg(a.slice_off + s);
         bool active = vis != kAll;
-        int32_t ng = 0;
-        const int4 *cp = nullptr;
-        if (active) {
-            const int64_t s = p >> a.log2C;
-            ng = (__ldg(a.width + s) + 3) >> 2;
-            cp = a.col4 + (__ldg(a.slice_off + s) >> 2) + (p & (a.C - 1));
-        }
+        const int32_t ng = active ? (wd + 3) >> 2 : 0;
+        const int4 *cp = a.col4 + (so >> 2) + (p & (a.C - 1));
         uint64_t acc = 0;
         // group g+1 is requested before group g's frontier fetches, so each
         // lane keeps a column load in flight while it waits on the gathers
@@ -275,14 +283,14 @@ __global__ void __launch_bounds__(kMsBuBlock, 5) k_ms_bu(MsArgs a, int j) {
     bytes = warp_sum(bytes);
     if (lane == 0) {
         if (cn) {
-            atomicAdd(&a.ctl->acc_n[k], cn);
-            atomicAdd(&a.ctl->acc_bits[k], cbits);
+            atomicAdd(&a.ctl->acc_n[k], (unsigned long long)cn);
+            atomicAdd(&a.ctl->acc_bits[k], (unsigned long long)cbits);
             atomicAdd(&a.ctl->acc_mo[k], cmo);
             atomicAdd(&a.ctl->acc_mi[k], cmi);
             atomicAdd(&a.ctl->acc_edges[k], cedges);
-            if (cdone) atomicAdd(&a.ctl->acc_done[k], cdone);
+            if (cdone) atomicAdd(&a.ctl->acc_done[k], (unsigned long long)cdone);
         }
-        if (cfull) atomicAdd(&a.ctl->acc_full[k], cfull);
+        if (cfull) atomicAdd(&a.ctl->acc_full[k], (unsigned long long)cfull);
         if (bytes) atomicAdd(&a.ctl->acc_bytes[k], bytes);
     }
 }
@@ -449,14 +457,17 @@ __global__ void k_ms_bu_long_fin(MsArgs a, int j) {
     }
 }
 
-// Frontier-nonzero bitmap A[L & 1] -> queue of level L: thread per bitmap
-// word, ballot/popc prefix sums within the warp, one atomic per warp.
-__global__ void k_ms_compact(MsArgs a, int j) {
-    (void)j;
-    const int L = a.ctl->level;
-    const uint32_t *Az = nz_bits(a, L);
-    int32_t *Q = (L & 1) ? a.q1 : a.q0;
-    unsigned long long *qslot = &a.ctl->qn[L % 3];
+// Frontier-nonzero bitmap A[M & 1] -> queue of level M (M = L + ahead):
+// thread per bitmap word, prefix sums within the warp, one atomic per warp.
+// ahead = 0 rebuilds the current queue before a top-down level that follows
+// a bottom-up one; ahead = 1 builds the next queue after a top-down level
+// (whose pushes only mark the bitmap, so no atomic counter is shared by
+// every claim).
+__global__ void k_ms_compact(MsArgs a, int ahead) {
+    const int M = a.ctl->level + ahead;
+    const uint32_t *Az = nz_bits(a, M);
+    int32_t *Q = (M & 1) ? a.q1 : a.q0;
+    unsigned long long *qslot = &a.ctl->qn[M % 3];
     const int lane = threadIdx.x & 31;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     // warp-uniform bound: every lane reaches the shuffles
@@ -480,27 +491,17 @@ __global__ void k_ms_compact(MsArgs a, int j) {
     }
 }
 
-// One pushed edge: the roots f reaching v this level; true when this push
-// made N[v] nonzero (v joins the next queue). N[v] is read first so that the
-// many pushes into a hub stop issuing atomics once its word holds their bits.
-__device__ __forceinline__ bool ms_push(const MsArgs &a, uint64_t *N, int32_t v, uint64_t f) {
+// One pushed edge: the roots f reaching v this level. The push that makes
+// N[v] nonzero marks v in the next nonzero bitmap An (the next queue is
+// compacted from it afterwards). N[v] is read first so that the many pushes
+// into a hub stop issuing atomics once its word holds their bits.
+__device__ __forceinline__ void ms_push(const MsArgs &a, uint64_t *N, uint32_t *An, int32_t v,
+                                        uint64_t f) {
     const uint64_t vis = __ldg(a.V + v);
     const uint64_t cur = __ldcg((const unsigned long long *)N + v);
     const uint64_t nb = f & ~vis;
-    if (!nb || !(nb & ~cur)) return false;  // nothing new (cur != 0: already queued)
-    return atomicOr((unsigned long long *)N + v, nb) == 0;
-}
-
-__device__ __forceinline__ void ms_append(int32_t *NQ, unsigned long long *nq_slot, bool claimed,
-                                          int32_t v) {
-    const unsigned cm = __ballot_sync(kFull, claimed);
-    if (!cm) return;
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(cm) - 1;
-    unsigned long long base = 0;
-    if (lane == leader) base = atomicAdd(nq_slot, (unsigned long long)__popc(cm));
-    base = __shfl_sync(kFull, base, leader);
-    if (claimed) NQ[base + __popc(cm & lanemask_lt())] = v;
+    if (!nb || !(nb & ~cur)) return;  // nothing new (cur != 0: already marked)
+    if (atomicOr((unsigned long long *)N + v, nb) == 0) atomicOr(An + (v >> 5), 1u << (v & 31));
 }
 
 
@@ -509,9 +510,8 @@ __global__ void k_ms_td(MsArgs a, int j) {
     uint64_t *N = slot(a, j + 1);
     const int L = a.ctl->level;
     const int32_t *Q = (L & 1) ? a.q1 : a.q0;
-    int32_t *NQ = (L & 1) ? a.q0 : a.q1;
     const int64_t qlen = (int64_t)a.ctl->qn[L % 3];
-    unsigned long long *nq_slot = &a.ctl->qn[(L + 1) % 3];
+    uint32_t *An = nz_bits(a, L + 1);
     unsigned long long *big_slot = &a.ctl->nbig[L % 3];
     __shared__ int64_t s_ex[32][32];
     __shared__ int64_t s_st[32][32];
@@ -546,26 +546,22 @@ __global__ void k_ms_td(MsArgs a, int j) {
         s_st[wib][lane] = st;
         s_f[wib][lane] = f;
         __syncwarp();
-        for (int64_t eb = 0; eb < T; eb += 32) {
-            const int64_t e = eb + lane;
-            bool claimed = false;
-            int32_t v = 0;
-            if (e < T) {
-                int jj = 0;
+        for (int64_t e = lane; e < T; e += 32) {
+            int jj = 0;
 #pragma unroll
-                for (int step = 16; step > 0; step >>= 1)
-                    if (s_ex[wib][jj + step] <= e) jj += step;
-                v = __ldg(a.pcol + s_st[wib][jj] + (e - s_ex[wib][jj]));
-                claimed = ms_push(a, N, v, s_f[wib][jj]);
-            }
-            ms_append(NQ, nq_slot, claimed, v);
+            for (int step = 16; step > 0; step >>= 1)
+                if (s_ex[wib][jj + step] <= e) jj += step;
+            const int32_t v = __ldg(a.pcol + s_st[wib][jj] + (e - s_ex[wib][jj]));
+            ms_push(a, N, An, v, s_f[wib][jj]);
         }
         __syncwarp();
     }
 }
 
-// Long frontier rows in kBigChunk-edge chunks over all warps; a chunk finds
-// its row by binary search over the chunk bases (monotone in the index).
+// Long frontier rows in kBigChunk-edge chunks over all warps. Each warp
+// takes a contiguous run of chunks: it finds the row of its first chunk by
+// binary search over the chunk bases (monotone in the list index) and walks
+// forward from there.
 __global__ void k_ms_td_big(MsArgs a, int j) {
     const int L = a.ctl->level;
     const unsigned long long ctr = a.ctl->nbig[L % 3];
@@ -574,34 +570,39 @@ __global__ void k_ms_td_big(MsArgs a, int j) {
     const int64_t total = (int64_t)(ctr & kMsBigMask);
     const uint64_t *F = slot(a, j);
     uint64_t *N = slot(a, j + 1);
-    int32_t *NQ = (L & 1) ? a.q0 : a.q1;
-    unsigned long long *nq_slot = &a.ctl->qn[(L + 1) % 3];
+    uint32_t *An = nz_bits(a, L + 1);
     const int lane = threadIdx.x & 31;
     const int64_t wpb = blockDim.x >> 5;
     const int64_t gw = blockIdx.x * wpb + (threadIdx.x >> 5);
     const int64_t nwarps = (int64_t)gridDim.x * wpb;
-    for (int64_t k = gw; k < total; k += nwarps) {
-        int64_t lo = 0, hi = nbig - 1;
-        while (lo < hi) {
-            const int64_t mid = (lo + hi + 1) >> 1;
-            if (a.big_base[mid] <= k) lo = mid;
-            else hi = mid - 1;
+    const int64_t per = (total + nwarps - 1) / nwarps;
+    const int64_t k0 = gw * per, k1 = min(total, k0 + per);
+    if (k0 >= k1) return;
+    int64_t lo = 0, hi = nbig - 1;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) >> 1;
+        if (a.big_base[mid] <= k0) lo = mid;
+        else hi = mid - 1;
+    }
+    int64_t base = a.big_base[lo];
+    int64_t next = lo + 1 < nbig ? a.big_base[lo + 1] : total;
+    int32_t u = a.big[lo];
+    int64_t st = __ldg(a.prow + u), d = __ldg(a.prow + u + 1) - st;
+    uint64_t f = __ldg(F + u);
+    for (int64_t k = k0; k < k1; k++) {
+        while (k >= next) {  // the run crosses into the next long row
+            lo++;
+            base = next;
+            next = lo + 1 < nbig ? a.big_base[lo + 1] : total;
+            u = a.big[lo];
+            st = __ldg(a.prow + u);
+            d = __ldg(a.prow + u + 1) - st;
+            f = __ldg(F + u);
         }
-        const int32_t u = a.big[lo];
-        const int64_t c = k - a.big_base[lo];
-        const int64_t st = __ldg(a.prow + u);
-        const int64_t d = __ldg(a.prow + u + 1) - st;
-        const uint64_t f = __ldg(F + u);
+        const int64_t c = k - base;
         const int64_t e1 = min(d, (c + 1) * kBigChunk);
-        for (int64_t e = c * kBigChunk + lane; e - lane < e1; e += 32) {
-            bool claimed = false;
-            int32_t v = 0;
-            if (e < e1) {
-                v = __ldg(a.pcol + st + e);
-                claimed = ms_push(a, N, v, f);
-            }
-            ms_append(NQ, nq_slot, claimed, v);
-        }
+        for (int64_t e = c * kBigChunk + lane; e < e1; e += 32)
+            ms_push(a, N, An, __ldg(a.pcol + st + e), f);
     }
 }
 
@@ -612,13 +613,11 @@ __global__ void k_ms_td_finish(MsArgs a, int j) {
     const int32_t *NQ = (L & 1) ? a.q0 : a.q1;
     const int64_t nqlen = (int64_t)a.ctl->qn[(L + 1) % 3];
     const int k = (L + 1) % 3;
-    uint32_t *An = nz_bits(a, L + 1);  // zeroed before the level
     unsigned long long cn = 0, cbits = 0, cmo = 0, cmi = 0, cfull = 0, cedges = 0, cdone = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nqlen;
          i += (int64_t)gridDim.x * blockDim.x) {
         const int32_t v = NQ[i];
         const uint64_t nb = N[v];
-        atomicOr(An + (v >> 5), 1u << (v & 31));
         const uint64_t old = a.V[v];  // only this thread writes V[v] in this kernel
         const uint64_t nv = old | nb;
         a.V[v] = nv;
@@ -699,7 +698,7 @@ __global__ void k_ms_end(MsArgs a, int dir) {
         // zero the slots level L+1 accumulates into after the next rollover
         const int z = (c.level + 1) % 3;
         c.acc_n[z] = c.acc_mo[z] = c.acc_mi[z] = c.acc_full[z] = c.acc_bits[z] = 0;
-        c.acc_edges[z] = c.qn[z] = c.acc_bytes[z] = c.acc_done[z] = c.nbig[z] = 0;
+        c.acc_edges[z] = c.qn[z] = c.acc_bytes[z] = c.acc_done[z] = c.nbig[z] = c.work[z] = 0;
         s = c;
     }
     __syncwarp();
@@ -838,14 +837,21 @@ void ms_scratch_free(alb_graph *g) {
 namespace {
 
 void launch_expand(const MsArgs &a, int nslots, int base, bool first, int nroots, int32_t *out,
-                   unsigned grid, cudaStream_t st) {
+                   int num_sms, cudaStream_t st) {
     const bool vec = ((uintptr_t)out & 15) == 0;
+    auto grid = [&](const void *f) {
+        const int per = resident_blocks(f, 256);
+        return (unsigned)(num_sms * (per > 0 ? per : 8));
+    };
     if (first && vec)
-        k_ms_expand<true, true><<<grid, 256, 0, st>>>(a, nslots, base, nroots, out);
+        k_ms_expand<true, true><<<grid((const void *)k_ms_expand<true, true>), 256, 0, st>>>(
+            a, nslots, base, nroots, out);
     else if (first)
-        k_ms_expand<true, false><<<grid, 256, 0, st>>>(a, nslots, base, nroots, out);
+        k_ms_expand<true, false><<<grid((const void *)k_ms_expand<true, false>), 256, 0, st>>>(
+            a, nslots, base, nroots, out);
     else
-        k_ms_expand<false, false><<<grid, 256, 0, st>>>(a, nslots, base, nroots, out);
+        k_ms_expand<false, false><<<grid((const void *)k_ms_expand<false, false>), 256, 0, st>>>(
+            a, nslots, base, nroots, out);
 }
 
 alb_status ms_alloc(alb_graph *g, MsScratch &m) {
@@ -940,7 +946,11 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
     cudaStream_t stream = g->stream;
     const int block = o.block;
     const unsigned wide = (unsigned)(g->num_sms * std::max(1, 2048 / block));
-    const unsigned bu_grid = (unsigned)(g->num_sms * (2048 / kMsBuBlock));
+    // grid-stride kernels get as many blocks as are resident at once (one wave)
+    auto rg = [&](const void *f, int b) -> unsigned {
+        const int per = resident_blocks(f, b);
+        return (unsigned)(g->num_sms * (per > 0 ? per : std::max(1, 2048 / b)));
+    };
     MsInit in;
     std::memset(&in, 0, sizeof(in));
     for (int i = 0; i < nroots; i++) in.roots[i] = roots[i];
@@ -1001,7 +1011,7 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
             // snapshot store full: write out levels [base, base + K - 1) and
             // restart the store from the current frontier
             if (d_levels) {
-                launch_expand(a, m.K - 1, base, first_flush, nroots, d_levels, wide, stream);
+                launch_expand(a, m.K - 1, base, first_flush, nroots, d_levels, g->num_sms, stream);
                 launches++;
             }
             first_flush = false;
@@ -1027,34 +1037,35 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
         auto launch_step = [&](int d) -> alb_status {
             if (d == ALB_DIR_TOPDOWN) {
                 if (!q_valid) {
-                    k_ms_compact<<<wide, block, 0, stream>>>(a, j);
+                    k_ms_compact<<<wide, block, 0, stream>>>(a, 0);
                     launches++;
                 }
                 ALB_CK(cudaMemsetAsync(a.S + (int64_t)(j + 1) * a.npad, 0,
                                        sizeof(uint64_t) * a.npad, stream));
                 ALB_CK(cudaMemsetAsync(a.A + (int64_t)((L + 1) & 1) * a.nwords, 0,
                                        sizeof(uint32_t) * a.nwords, stream));
-                k_ms_td<<<wide, block, 0, stream>>>(a, j);
-                k_ms_td_big<<<wide, block, 0, stream>>>(a, j);
-                k_ms_td_finish<<<wide, block, 0, stream>>>(a, j);
-                launches += 3;
+                k_ms_td<<<rg((const void *)k_ms_td, block), block, 0, stream>>>(a, j);
+                k_ms_td_big<<<rg((const void *)k_ms_td_big, block), block, 0, stream>>>(a, j);
+                k_ms_compact<<<wide, block, 0, stream>>>(a, 1);
+                k_ms_td_finish<<<rg((const void *)k_ms_td_finish, block), block, 0, stream>>>(a, j);
+                launches += 4;
             } else if (d == ALB_DIR_BOTTOMUP) {
                 if (filt)
-                    k_ms_bu<true, true, true><<<bu_grid, kMsBuBlock, 0, stream>>>(a, j);
+                    k_ms_bu<true, true, true><<<rg((const void *)k_ms_bu<true, true, true>, kMsBuBlock), kMsBuBlock, 0, stream>>>(a, j);
                 else
-                    k_ms_bu<true, true, false><<<bu_grid, kMsBuBlock, 0, stream>>>(a, j);
-                k_ms_bu_long<true><<<wide, block, 0, stream>>>(a, j, filt);
-                k_ms_bu_long_tail<true><<<wide, block, 0, stream>>>(a, j, filt);
-                k_ms_bu_long_fin<<<wide, block, 0, stream>>>(a, j);
+                    k_ms_bu<true, true, false><<<rg((const void *)k_ms_bu<true, true, false>, kMsBuBlock), kMsBuBlock, 0, stream>>>(a, j);
+                k_ms_bu_long<true><<<rg((const void *)k_ms_bu_long<true>, block), block, 0, stream>>>(a, j, filt);
+                k_ms_bu_long_tail<true><<<rg((const void *)k_ms_bu_long_tail<true>, block), block, 0, stream>>>(a, j, filt);
+                k_ms_bu_long_fin<<<rg((const void *)k_ms_bu_long_fin, block), block, 0, stream>>>(a, j);
                 launches += 4;
             } else {
                 if (filt)
-                    k_ms_bu<false, false, true><<<bu_grid, kMsBuBlock, 0, stream>>>(a, j);
+                    k_ms_bu<false, false, true><<<rg((const void *)k_ms_bu<false, false, true>, kMsBuBlock), kMsBuBlock, 0, stream>>>(a, j);
                 else
-                    k_ms_bu<false, false, false><<<bu_grid, kMsBuBlock, 0, stream>>>(a, j);
-                k_ms_bu_long<false><<<wide, block, 0, stream>>>(a, j, filt);
-                k_ms_bu_long_tail<false><<<wide, block, 0, stream>>>(a, j, filt);
-                k_ms_bu_long_fin<<<wide, block, 0, stream>>>(a, j);
+                    k_ms_bu<false, false, false><<<rg((const void *)k_ms_bu<false, false, false>, kMsBuBlock), kMsBuBlock, 0, stream>>>(a, j);
+                k_ms_bu_long<false><<<rg((const void *)k_ms_bu_long<false>, block), block, 0, stream>>>(a, j, filt);
+                k_ms_bu_long_tail<false><<<rg((const void *)k_ms_bu_long_tail<false>, block), block, 0, stream>>>(a, j, filt);
+                k_ms_bu_long_fin<<<rg((const void *)k_ms_bu_long_fin, block), block, 0, stream>>>(a, j);
                 launches += 4;
             }
             return ALB_OK;
@@ -1123,7 +1134,7 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
     if (!h->done) return fail(ALB_ERR_DEVICE, "msbfs: level cap reached");
     if (d_levels) {
         const int nslots = h->level - base;  // slots 0 .. level-base-1 hold levels
-        launch_expand(a, std::min(nslots, m.K), base, first_flush, nroots, d_levels, wide,
+        launch_expand(a, std::min(nslots, m.K), base, first_flush, nroots, d_levels, g->num_sms,
                       stream);
         launches++;
     }
