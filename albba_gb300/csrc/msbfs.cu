@@ -50,6 +50,7 @@ struct MsCtl {
 struct MsArgs {
     int64_t n, nwords, npad;
     int32_t C, log2C, K;
+    int32_t sigma;  // sort window: perm maps each aligned window of sigma rows to itself
     const int32_t *perm, *inv, *ideg, *odeg, *width;
     const int64_t *slice_off;
     const int4 *col4;
@@ -796,6 +797,54 @@ __global__ void k_ms_expand(MsArgs a, int nslots, int base, int nroots, int32_t 
     }
 }
 
+// The same output, one CTA per aligned tile of kExpandTile rows. The sort
+// permutes rows only inside sigma windows, so when sigma divides the tile the
+// positions of the tile's original ids are the tile's own positions: the CTA
+// stages the tile's slot words in shared memory (coalesced), then writes the
+// tile's 256-byte output rows in original-id order, a sequential stream.
+// First flush, 16-byte aligned output, at most kExpandMaxSlots slots.
+constexpr int kExpandTile = 1024;
+constexpr int kExpandMaxSlots = 16;
+
+constexpr int kExpandThreads = 512;
+
+__global__ void __launch_bounds__(kExpandThreads) k_ms_expand_tile(MsArgs a, int nslots, int base,
+                                                                   int nroots, int32_t *out) {
+    extern __shared__ uint64_t s_slots[];  // nslots x kExpandTile, then kExpandTile positions
+    int32_t *s_pos = reinterpret_cast<int32_t *>(s_slots + (size_t)nslots * kExpandTile);
+    const int64_t t0 = (int64_t)blockIdx.x * kExpandTile;
+    const int rows = (int)min((int64_t)kExpandTile, a.n - t0);
+    for (int i = threadIdx.x; i < nslots * kExpandTile; i += blockDim.x) {
+        const int jj = i / kExpandTile, r = i % kExpandTile;
+        s_slots[i] = r < rows ? __ldcs(a.S + (int64_t)jj * a.npad + t0 + r) : 0ull;
+    }
+    for (int r = threadIdx.x; r < rows; r += blockDim.x)
+        s_pos[r] = (int32_t)((int64_t)__ldg(a.inv + t0 + r) - t0);  // position in the tile
+    __syncthreads();
+    const int q = threadIdx.x & 15;
+    for (int r = threadIdx.x >> 4; r < rows; r += blockDim.x >> 4) {
+        const int64_t v = t0 + r;  // original id
+        const int pl = s_pos[r];
+        if ((unsigned)pl >= (unsigned)rows) {  // not a window permutation: refuse, loudly
+            a.ctl->err = ALB_ERR_DEVICE;
+            continue;
+        }
+        int32_t l[4] = {-1, -1, -1, -1};
+        for (int jj = 0; jj < nslots; jj++) {
+            const uint32_t b = (uint32_t)(s_slots[jj * kExpandTile + pl] >> (4 * q)) & 0xFu;
+            if (b) {
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    if ((b >> k) & 1u) l[k] = base + jj;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (4 * q + k >= nroots) l[k] = -1;
+        __stcs(reinterpret_cast<int4 *>(out + v * 64 + 4 * q), make_int4(l[0], l[1], l[2], l[3]));
+    }
+}
+
 struct MsScratch {
     bool ready = false;
     int32_t K = 0;
@@ -843,7 +892,17 @@ void launch_expand(const MsArgs &a, int nslots, int base, bool first, int nroots
         const int per = resident_blocks(f, 256);
         return (unsigned)(num_sms * (per > 0 ? per : 8));
     };
-    if (first && vec)
+    const bool tiled = first && vec && nslots <= kExpandMaxSlots && a.sigma >= 1 &&
+                       a.sigma <= kExpandTile && kExpandTile % a.sigma == 0;
+    if (tiled) {
+        const size_t sm = (sizeof(uint64_t) * (size_t)std::max(nslots, 1) + sizeof(int32_t)) *
+                          kExpandTile;
+        cudaFuncSetAttribute(k_ms_expand_tile, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)((sizeof(uint64_t) * kExpandMaxSlots + sizeof(int32_t)) *
+                                   kExpandTile));
+        const unsigned tiles = (unsigned)((a.n + kExpandTile - 1) / kExpandTile);
+        k_ms_expand_tile<<<tiles, kExpandThreads, sm, st>>>(a, nslots, base, nroots, out);
+    } else if (first && vec)
         k_ms_expand<true, true><<<grid((const void *)k_ms_expand<true, true>), 256, 0, st>>>(
             a, nslots, base, nroots, out);
     else if (first)
@@ -883,6 +942,7 @@ MsArgs ms_args(alb_graph *g, MsScratch &m) {
     a.C = s.C;
     a.log2C = s.log2C;
     a.K = m.K;
+    a.sigma = s.sigma;
     a.perm = s.perm;
     a.inv = s.inv;
     a.ideg = s.ideg;
@@ -1140,7 +1200,12 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
     }
     ALB_CK(cudaGetLastError());
     ALB_CK(cudaEventRecord(g->ev1, stream));
+    int32_t dev_err = 0;
+    if (d_levels)
+        ALB_CK(cudaMemcpyAsync(&dev_err, &a.ctl->err, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                               stream));
     ALB_CK(cudaStreamSynchronize(stream));
+    if (dev_err) return fail(dev_err, "msbfs: level output saw a position outside its tile");
     float ms = 0;
     ALB_CK(cudaEventElapsedTime(&ms, g->ev0, g->ev1));
     if (st) {
