@@ -125,41 +125,22 @@ __device__ void prep_phase(const BfsArgs &a, int L, bool compact, bool zero_next
     }
 }
 
-// One pushed edge u -> v (u's original id ou); returns true when v is claimed.
-__device__ __forceinline__ bool push_edge(const BfsArgs &a, uint32_t *N, int32_t v, uint32_t ou,
+// One pushed edge u -> v (u's original id ou): the smallest source wins the
+// parent, and v's bit goes into the next-frontier bitmap N (the next queue,
+// levels and counters are made from N by td_finish_phase, so no counter is
+// shared by every claim).
+__device__ __forceinline__ void push_edge(const BfsArgs &a, uint32_t *N, int32_t v, uint32_t ou,
                                           bool persist) {
     const uint32_t bit = 1u << (v & 31);
     const uint32_t w = persist ? __ldcg(a.vis + (v >> 5)) : __ldg(a.vis + (v >> 5));
-    if (w & bit) return false;
+    if (w & bit) return;
     // read before writing: a hub target receives thousands of pushes in one
     // level, and atomics on one address serialise in L2, so the atomics are
     // issued only when they can still change something
     const uint32_t cur_parent = __ldcg(a.parent_pos + v);
     const uint32_t cur_n = __ldcg(N + (v >> 5));
     if (ou < cur_parent) atomicMin(a.parent_pos + v, ou);
-    if (cur_n & bit) return false;
-    return !(atomicOr(N + (v >> 5), bit) & bit);
-}
-
-// Warp-aggregated append of claimed targets to the next queue.
-__device__ __forceinline__ void append_claims(const BfsArgs &a, int32_t *NQ,
-                                              unsigned long long *nq_slot, bool claimed, int32_t v,
-                                              uint32_t lvl, unsigned long long &cn,
-                                              unsigned long long &cmo, unsigned long long &cmi) {
-    const unsigned cm = __ballot_sync(kFull, claimed);
-    if (!cm) return;
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(cm) - 1;
-    unsigned long long base = 0;
-    if (lane == leader) base = atomicAdd(nq_slot, (unsigned long long)__popc(cm));
-    base = __shfl_sync(kFull, base, leader);
-    if (claimed) {
-        NQ[base + __popc(cm & lanemask_lt())] = v;
-        a.level_pos[v] = (int32_t)lvl;
-        cn++;
-        cmo += (unsigned long long)__ldg(a.odeg + v);
-        cmi += (unsigned long long)__ldg(a.ideg + v);
-    }
+    if (!(cur_n & bit)) atomicOr(N + (v >> 5), bit);
 }
 
 // Rows per warp for the short-row pass: as many frontier rows as keep every
@@ -179,10 +160,8 @@ constexpr unsigned long long kBigMask = (1ull << kBigShift) - 1;
 template <bool kPersist>
 __device__ void td_phase(const BfsArgs &a, int L, Range r) {
     const int32_t *Q = (L & 1) ? a.q1 : a.q0;
-    int32_t *NQ = (L & 1) ? a.q0 : a.q1;
     uint32_t *N = (L & 1) ? a.bm0 : a.bm1;
     const int64_t qlen = (int64_t)ld_state<kPersist>(&a.ctl->qn[L % 3]);
-    unsigned long long *nq_slot = &a.ctl->qn[(L + 1) % 3];
     unsigned long long *big_slot = &a.ctl->nbig[L % 3];
     __shared__ int64_t s_ex[kMaxBlock / 32][32];
     __shared__ int64_t s_st[kMaxBlock / 32][32];
@@ -193,8 +172,6 @@ __device__ void td_phase(const BfsArgs &a, int L, Range r) {
     const int64_t nwarps = (int64_t)r.nblk * wpb;
     const int G = rows_per_warp(qlen, nwarps);
     const int64_t stride = nwarps * G;
-    unsigned long long cn = 0, cmo = 0, cmi = 0;
-    const uint32_t lvl = (uint32_t)(L + 1);
     for (int64_t cb = gw * G; cb < qlen; cb += stride) {
         const int64_t i = cb + lane;
         int32_t u = (lane < G && i < qlen) ? ld_state<kPersist>(Q + i) : -1;
@@ -219,113 +196,143 @@ __device__ void td_phase(const BfsArgs &a, int L, Range r) {
         s_st[wib][lane] = st;
         s_ou[wib][lane] = ou;
         __syncwarp();
-        for (int64_t eb = 0; eb < T; eb += 32) {
-            const int64_t e = eb + lane;
-            bool claimed = false;
-            int32_t v = 0;
-            if (e < T) {
-                int j = 0;
+        for (int64_t e = lane; e < T; e += 32) {
+            int j = 0;
 #pragma unroll
-                for (int step = 16; step > 0; step >>= 1)
-                    if (s_ex[wib][j + step] <= e) j += step;
-                v = __ldg(a.pcol + s_st[wib][j] + (e - s_ex[wib][j]));
-                claimed = push_edge(a, N, v, (uint32_t)s_ou[wib][j], kPersist);
-            }
-            append_claims(a, NQ, nq_slot, claimed, v, lvl, cn, cmo, cmi);
+            for (int step = 16; step > 0; step >>= 1)
+                if (s_ex[wib][j + step] <= e) j += step;
+            push_edge(a, N, __ldg(a.pcol + s_st[wib][j] + (e - s_ex[wib][j])),
+                      (uint32_t)s_ou[wib][j], kPersist);
         }
         __syncwarp();
-    }
-    cn = warp_sum(cn);
-    cmo = warp_sum(cmo);
-    cmi = warp_sum(cmi);
-    if (lane == 0 && cn) {
-        const int k = (L + 1) % 3;
-        atomicAdd(&a.ctl->acc_n[k], cn);
-        atomicAdd(&a.ctl->acc_mo[k], cmo);
-        atomicAdd(&a.ctl->acc_mi[k], cmi);
     }
 }
 
 // Long frontier rows, kBigChunk edges per chunk, chunks spread over all
-// warps; a chunk finds its row by binary search over the chunk bases.
+// warps. Each warp takes a contiguous run of chunks: it finds the row of its
+// first chunk by binary search over the chunk bases (monotone in the list
+// index) and walks forward from there.
 template <bool kPersist>
 __device__ void td_big_phase(const BfsArgs &a, int L, Range r) {
     const unsigned long long ctr = ld_state<kPersist>(&a.ctl->nbig[L % 3]);
     if (ctr == 0) return;
     const int64_t nbig = (int64_t)(ctr >> kBigShift);
     const int64_t total = (int64_t)(ctr & kBigMask);
-    int32_t *NQ = (L & 1) ? a.q0 : a.q1;
     uint32_t *N = (L & 1) ? a.bm0 : a.bm1;
-    unsigned long long *nq_slot = &a.ctl->qn[(L + 1) % 3];
     const int lane = threadIdx.x & 31;
     const int64_t wpb = blockDim.x >> 5;
     const int64_t gw = (int64_t)r.bid * wpb + (threadIdx.x >> 5);
     const int64_t nwarps = (int64_t)r.nblk * wpb;
-    const uint32_t lvl = (uint32_t)(L + 1);
-    unsigned long long cn = 0, cmo = 0, cmi = 0;
-    for (int64_t k = gw; k < total; k += nwarps) {
-        int64_t lo = 0, hi = nbig - 1;
-        while (lo < hi) {
-            const int64_t mid = (lo + hi + 1) >> 1;
-            if (ld_state<kPersist>(a.big_base + mid) <= k) lo = mid;
-            else hi = mid - 1;
-        }
-        const int32_t u = ld_state<kPersist>(a.big + lo);
-        const int64_t c = k - ld_state<kPersist>(a.big_base + lo);
-        const int64_t st = __ldg(a.prow + u);
-        const int64_t d = __ldg(a.prow + u + 1) - st;
-        const uint32_t ou = (uint32_t)__ldg(a.perm + u);
-        const int64_t e1 = min(d, (c + 1) * kBigChunk);
-        for (int64_t e = c * kBigChunk + lane; e - lane < e1; e += 32) {
-            bool claimed = false;
-            int32_t v = 0;
-            if (e < e1) {
-                v = __ldg(a.pcol + st + e);
-                claimed = push_edge(a, N, v, ou, kPersist);
-            }
-            append_claims(a, NQ, nq_slot, claimed, v, lvl, cn, cmo, cmi);
-        }
+    const int64_t per = (total + nwarps - 1) / nwarps;
+    const int64_t k0 = gw * per, k1 = min(total, k0 + per);
+    if (k0 >= k1) return;
+    int64_t lo = 0, hi = nbig - 1;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) >> 1;
+        if (ld_state<kPersist>(a.big_base + mid) <= k0) lo = mid;
+        else hi = mid - 1;
     }
-    cn = warp_sum(cn);
-    cmo = warp_sum(cmo);
-    cmi = warp_sum(cmi);
-    if (lane == 0 && cn) {
-        const int k = (L + 1) % 3;
-        atomicAdd(&a.ctl->acc_n[k], cn);
-        atomicAdd(&a.ctl->acc_mo[k], cmo);
-        atomicAdd(&a.ctl->acc_mi[k], cmi);
+    int64_t base = ld_state<kPersist>(a.big_base + lo);
+    int64_t next = lo + 1 < nbig ? ld_state<kPersist>(a.big_base + lo + 1) : total;
+    int32_t u = ld_state<kPersist>(a.big + lo);
+    int64_t st = __ldg(a.prow + u), d = __ldg(a.prow + u + 1) - st;
+    uint32_t ou = (uint32_t)__ldg(a.perm + u);
+    for (int64_t k = k0; k < k1; k++) {
+        while (k >= next) {  // the run crosses into the next long row
+            lo++;
+            base = next;
+            next = lo + 1 < nbig ? ld_state<kPersist>(a.big_base + lo + 1) : total;
+            u = ld_state<kPersist>(a.big + lo);
+            st = __ldg(a.prow + u);
+            d = __ldg(a.prow + u + 1) - st;
+            ou = (uint32_t)__ldg(a.perm + u);
+        }
+        const int64_t c = k - base;
+        const int64_t e1 = min(d, (c + 1) * kBigChunk);
+        for (int64_t e = c * kBigChunk + lane; e < e1; e += 32)
+            push_edge(a, N, __ldg(a.pcol + st + e), ou, kPersist);
     }
 }
 
-// After a top-down level: mark the new frontier visited, clear the old one.
+// After a top-down level: clear the old frontier over its queue; compact the
+// new frontier bitmap N into the next queue (thread per word, prefix sums in
+// the warp, one atomic per warp), recording levels and counters and marking
+// the new vertices visited (each word by the one thread that owns it).
 template <bool kPersist>
 __device__ void td_finish_phase(const BfsArgs &a, int L, Range r) {
     const int32_t *Q = (L & 1) ? a.q1 : a.q0;
-    const int32_t *NQ = (L & 1) ? a.q0 : a.q1;
+    int32_t *NQ = (L & 1) ? a.q0 : a.q1;
     uint32_t *F = (L & 1) ? a.bm1 : a.bm0;
+    const uint32_t *N = (L & 1) ? a.bm0 : a.bm1;
     const int64_t qlen = (int64_t)ld_state<kPersist>(&a.ctl->qn[L % 3]);
-    const int64_t nqlen = (int64_t)ld_state<kPersist>(&a.ctl->qn[(L + 1) % 3]);
-    const int64_t m = qlen > nqlen ? qlen : nqlen;
-    unsigned long long full = 0;
-    for (int64_t i = (int64_t)r.bid * blockDim.x + threadIdx.x; i < m;
-         i += (int64_t)r.nblk * blockDim.x) {
-        if (i < nqlen) {
-            const int32_t v = ld_state<kPersist>(NQ + i);
-            const uint32_t bit = 1u << (v & 31);
-            const uint32_t old = atomicOr(a.vis + (v >> 5), bit);
-            full += (old != kFull && (old | bit) == kFull);
+    unsigned long long *nq_slot = &a.ctl->qn[(L + 1) % 3];
+    const int lane = threadIdx.x & 31;
+    const int64_t tid = (int64_t)r.bid * blockDim.x + threadIdx.x;
+    const int64_t nth = (int64_t)r.nblk * blockDim.x;
+    for (int64_t i = tid; i < qlen; i += nth) F[ld_state<kPersist>(Q + i) >> 5] = 0;
+    const int32_t lvl = L + 1;
+    unsigned cn = 0, full = 0;
+    unsigned long long cmo = 0, cmi = 0;
+    // the loop bound is warp-uniform so that every lane reaches the shuffles
+    for (int64_t w0 = tid & ~31ll; w0 < a.nwords; w0 += nth) {
+        const int64_t w = w0 + lane;
+        uint32_t m = w < a.nwords ? ld_bits<kPersist>(N + w) : 0u;
+        const int cnt = __popc(m);
+        const int inc = warp_inclusive_scan(cnt);
+        const int tot = __shfl_sync(kFull, inc, 31);
+        if (tot == 0) continue;
+        unsigned long long base = 0;
+        if (lane == 31) base = atomicAdd(nq_slot, (unsigned long long)tot);
+        base = __shfl_sync(kFull, base, 31);
+        if (m) {
+            const uint32_t old = ld_bits<kPersist>(a.vis + w);
+            a.vis[w] = old | m;
+            full += (old != kFull && (old | m) == kFull);
         }
-        if (i < qlen) F[ld_state<kPersist>(Q + i) >> 5] = 0;
+        int64_t pos = (int64_t)base + inc - cnt;
+        while (m) {
+            const int b = __ffs(m) - 1;
+            m &= m - 1;
+            const int32_t v = (int32_t)(w * 32 + b);
+            NQ[pos++] = v;
+            a.level_pos[v] = lvl;
+            cn++;
+            cmo += (unsigned long long)__ldg(a.odeg + v);
+            cmi += (unsigned long long)__ldg(a.ideg + v);
+        }
     }
+    cn = warp_sum(cn);
     full = warp_sum(full);
-    if ((threadIdx.x & 31) == 0 && full) atomicAdd(&a.ctl->acc_full[(L + 1) % 3], full);
+    cmo = warp_sum(cmo);
+    cmi = warp_sum(cmi);
+    if (lane == 0 && (cn || full)) {
+        const int k = (L + 1) % 3;
+        if (cn) {
+            atomicAdd(&a.ctl->acc_n[k], (unsigned long long)cn);
+            atomicAdd(&a.ctl->acc_mo[k], cmo);
+            atomicAdd(&a.ctl->acc_mi[k], cmi);
+        }
+        if (full) atomicAdd(&a.ctl->acc_full[k], (unsigned long long)full);
+    }
+}
+
+// Frontier word read by the bottom-up pull: from the staged shared-memory
+// copy (kSmemF) or from global memory.
+template <bool kSmemF, bool kPersist>
+__device__ __forceinline__ uint32_t ld_front(const uint32_t *F, int32_t w) {
+    if constexpr (kSmemF)
+        return F[w];
+    else
+        return ld_bits<kPersist>(F + w);
 }
 
 // Bottom-up pull. kBypass: skip words whose rows are all visited.
 // kEarly: stop each row at its first frontier source or its padding.
-template <bool kPersist, bool kBypass, bool kEarly>
-__device__ void bu_phase(const BfsArgs &a, int L, Range r) {
-    const uint32_t *F = (L & 1) ? a.bm1 : a.bm0;
+// Fs: where the frontier words are read (the global bitmap, or its copy in
+// shared memory when kSmemF).
+template <bool kPersist, bool kBypass, bool kEarly, bool kSmemF = false>
+__device__ void bu_phase(const BfsArgs &a, int L, Range r, const uint32_t *Fs = nullptr) {
+    const uint32_t *F = kSmemF ? Fs : ((L & 1) ? a.bm1 : a.bm0);
     uint32_t *N = (L & 1) ? a.bm0 : a.bm1;
     const int lane = threadIdx.x & 31;
     (void)r;  // words are handed out by the level's counter, not by block index
@@ -373,10 +380,10 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r) {
             bytes += 32;  // four columns and the four frontier words they select
             int4 nx = make_int4(p, p, p, p);
             if (j + 1 < ng) nx = ld_stream(cp + (int64_t)(j + 1) * C, pol);
-            const uint32_t f0 = ld_bits<kPersist>(F + (c.x >> 5));
-            const uint32_t f1 = ld_bits<kPersist>(F + (c.y >> 5));
-            const uint32_t f2 = ld_bits<kPersist>(F + (c.z >> 5));
-            const uint32_t f3 = ld_bits<kPersist>(F + (c.w >> 5));
+            const uint32_t f0 = ld_front<kSmemF, kPersist>(F, c.x >> 5);
+            const uint32_t f1 = ld_front<kSmemF, kPersist>(F, c.y >> 5);
+            const uint32_t f2 = ld_front<kSmemF, kPersist>(F, c.z >> 5);
+            const uint32_t f3 = ld_front<kSmemF, kPersist>(F, c.w >> 5);
             const int32_t cc[4] = {c.x, c.y, c.z, c.w};
             const uint32_t ff[4] = {f0, f1, f2, f3};
 #pragma unroll
@@ -437,6 +444,37 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r) {
 // kLongChunk-source chunks the tail pass spreads over all warps; their hits
 // meet in parent_pos[p] by atomicMin. The slice pass that follows sees
 // parent_pos[p] set and records the row as reached. Both run before bu_phase.
+// First frontier source among sources [st, en) of one long row (-1 if
+// none), 128 per step: each lane loads four source ids, then their four
+// frontier words, before testing any; the earliest hit is the lowest lane of
+// the first 32-source group with one.
+template <bool kPersist, bool kEarly>
+__device__ __forceinline__ int32_t long_scan(const BfsArgs &a, const uint32_t *F, int64_t st,
+                                             int64_t en, unsigned long long &bytes) {
+    const int lane = threadIdx.x & 31;
+    int32_t found = -1;
+    for (int64_t e0 = st; e0 < en; e0 += 128) {
+        int32_t c[4];
+        uint32_t f[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int64_t e = e0 + 32 * u + lane;
+            c[u] = e < en ? __ldg(a.lcol + e) : -1;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) f[u] = c[u] >= 0 ? ld_bits<kPersist>(F + (c[u] >> 5)) : 0u;
+        bytes += 8 * (unsigned long long)min((int64_t)128, en - e0);
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const bool hit = c[u] >= 0 && ((f[u] >> (c[u] & 31)) & 1u);
+            const unsigned m = __ballot_sync(kFull, hit);
+            if (m && found < 0) found = __shfl_sync(kFull, c[u], __ffs(m) - 1);
+        }
+        if (kEarly && found >= 0) break;
+    }
+    return found;
+}
+
 template <bool kPersist, bool kEarly>
 __device__ void bu_long_phase(const BfsArgs &a, int L, Range r) {
     if (a.nlong == 0) return;
@@ -452,16 +490,7 @@ __device__ void bu_long_phase(const BfsArgs &a, int L, Range r) {
         const int64_t st = __ldg(a.lptr + i), en = __ldg(a.lptr + i + 1);
         const int64_t hen = min(en, st + kLongChunk);
         bytes += 24;
-        int32_t found = -1;
-        for (int64_t e0 = st; e0 < hen; e0 += 32) {
-            const int64_t e = e0 + lane;
-            const int32_t c = e < hen ? __ldg(a.lcol + e) : p;
-            const bool hit = (ld_bits<kPersist>(F + (c >> 5)) >> (c & 31)) & 1u;
-            const unsigned m = __ballot_sync(kFull, hit);
-            bytes += 8 * (unsigned long long)min((int64_t)32, hen - e0);
-            if (m && found < 0) found = __shfl_sync(kFull, c, __ffs(m) - 1);
-            if (kEarly && found >= 0) break;
-        }
+        const int32_t found = long_scan<kPersist, kEarly>(a, F, st, hen, bytes);
         if (lane == 0) {
             if (found >= 0) {
                 atomicMin(a.parent_pos + p, (uint32_t)__ldg(a.perm + found));
@@ -505,16 +534,7 @@ __device__ void bu_long_tail_phase(const BfsArgs &a, int L, Range r) {
         const int64_t st = __ldg(a.lptr + i) + (1 + c) * kLongChunk;
         const int64_t en = min(__ldg(a.lptr + i + 1), st + kLongChunk);
         bytes += 24;
-        int32_t found = -1;
-        for (int64_t e0 = st; e0 < en; e0 += 32) {
-            const int64_t e = e0 + lane;
-            const int32_t cc = e < en ? __ldg(a.lcol + e) : p;
-            const bool hit = (ld_bits<kPersist>(F + (cc >> 5)) >> (cc & 31)) & 1u;
-            const unsigned m = __ballot_sync(kFull, hit);
-            bytes += 8 * (unsigned long long)min((int64_t)32, en - e0);
-            if (m && found < 0) found = __shfl_sync(kFull, cc, __ffs(m) - 1);
-            if (kEarly && found >= 0) break;
-        }
+        const int32_t found = long_scan<kPersist, kEarly>(a, F, st, en, bytes);
         if (found >= 0 && lane == 0) atomicMin(a.parent_pos + p, (uint32_t)__ldg(a.perm + found));
     }
     if (lane == 0 && bytes) atomicAdd(&a.ctl->acc_bytes[(L + 1) % 3], bytes);
@@ -664,6 +684,38 @@ constexpr unsigned kBuBlock = 256;
 template <bool kBypass, bool kEarly>
 __global__ void __launch_bounds__(kBuBlock, 5) k_bu(BfsArgs a) {
     bu_phase<false, kBypass, kEarly>(a, a.ctl->level, Range{(int)blockIdx.x, (int)gridDim.x});
+}
+
+// The slice pass with the frontier bitmap staged in shared memory: one CTA
+// of kBuSmemBlock threads per SM copies the whole bitmap (nwords * 4 bytes,
+// at most kSmemFrontierMax) with one bulk copy completing on an mbarrier,
+// then gathers frontier words from shared memory. The wait is bounded: past
+// kBulkWaitNs it records ALB_ERR_TIMEOUT and the CTA leaves.
+constexpr unsigned kBuSmemBlock = 1024;
+constexpr int64_t kSmemFrontierMax = 192 * 1024;
+constexpr uint64_t kBulkWaitNs = 2ull * 1000 * 1000 * 1000;
+
+template <bool kBypass, bool kEarly>
+__global__ void __launch_bounds__(kBuSmemBlock, 1) k_bu_smem(BfsArgs a) {
+    extern __shared__ __align__(16) uint32_t s_front[];
+    __shared__ __align__(8) uint64_t s_bar;
+    const int L = a.ctl->level;
+    const uint32_t *F = (L & 1) ? a.bm1 : a.bm0;
+    const uint32_t bytes = (uint32_t)(((a.nwords * 4) + 15) & ~15ll);
+    if (threadIdx.x == 0) {
+        mbar_init(&s_bar, 1);
+        mbar_expect_tx(&s_bar, bytes);
+        bulk_g2s(s_front, F, bytes, &s_bar);
+    }
+    __syncthreads();  // the barrier is initialised before anyone waits on it
+    const uint64_t t0 = globaltimer_ns();
+    while (!mbar_try_wait(&s_bar, 0)) {
+        if (globaltimer_ns() - t0 > kBulkWaitNs) {
+            if (threadIdx.x == 0) atomicExch(&a.ctl->err, ALB_ERR_TIMEOUT);
+            return;
+        }
+    }
+    bu_phase<false, kBypass, kEarly, true>(a, L, Range{(int)blockIdx.x, (int)gridDim.x}, s_front);
 }
 
 template <bool kEarly>
@@ -854,8 +906,10 @@ alb_status bfs_scratch_alloc(alb_graph *g) {
     BfsScratch &b = g->bfs;
     if (b.ready) return ALB_OK;
     const int64_t n = g->n, nw = g->sell.nwords;
-    ALB_TRY(dmalloc((void **)&b.bm0, sizeof(uint32_t) * nw, "frontier bitmap"));
-    ALB_TRY(dmalloc((void **)&b.bm1, sizeof(uint32_t) * nw, "frontier bitmap"));
+    // frontier bitmaps padded to 16 bytes: k_bu_smem copies them whole
+    const int64_t nw16 = (nw + 3) & ~3ll;
+    ALB_TRY(dmalloc((void **)&b.bm0, sizeof(uint32_t) * nw16, "frontier bitmap"));
+    ALB_TRY(dmalloc((void **)&b.bm1, sizeof(uint32_t) * nw16, "frontier bitmap"));
     ALB_TRY(dmalloc((void **)&b.vis, sizeof(uint32_t) * nw, "visited bitmap"));
     ALB_TRY(dmalloc((void **)&b.q0, sizeof(int32_t) * n, "frontier queue"));
     ALB_TRY(dmalloc((void **)&b.q1, sizeof(int32_t) * n, "frontier queue"));
@@ -971,16 +1025,44 @@ Launch fit(const void *func, const Launch &w) {
 }
 
 alb_status add_kernel_node(cudaGraph_t graph, cudaGraphNode_t *node, const cudaGraphNode_t *deps,
-                           size_t ndeps, void *func, Launch l, void **args) {
+                           size_t ndeps, void *func, Launch l, void **args, size_t smem = 0) {
     cudaKernelNodeParams p;
     std::memset(&p, 0, sizeof(p));
     p.func = func;
     p.gridDim = dim3(l.grid);
     p.blockDim = dim3(l.block);
-    p.sharedMemBytes = 0;
+    p.sharedMemBytes = (unsigned)smem;
     p.kernelParams = args;
     ALB_CK(cudaGraphAddKernelNode(node, graph, deps, ndeps, &p));
     return ALB_OK;
+}
+
+// The bottom-up slice pass of a level: the staged-frontier kernel when the
+// bitmap fits in shared memory, else the kernel that gathers from global.
+struct BuSlices {
+    void *func;
+    Launch l;
+    size_t smem;
+};
+
+template <bool kBypass, bool kEarly>
+BuSlices bu_slices(const BfsArgs &a, const Launch &wide) {
+    if (a.nwords * 4 <= kSmemFrontierMax) {
+        void *f = (void *)k_bu_smem<kBypass, kEarly>;
+        cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kSmemFrontierMax);
+        const size_t sm = (size_t)((a.nwords * 4 + 15) & ~15ll);
+        return {f, Launch{(unsigned)wide.sms, kBuSmemBlock, wide.sms}, sm};
+    }
+    void *f = (void *)k_bu<kBypass, kEarly>;
+    return {f, fit(f, with_block(wide, kBuBlock)), 0};
+}
+
+template <bool kBypass, bool kEarly>
+void launch_bu_slices(const BfsArgs &a, const Launch &wide, cudaStream_t st) {
+    const BuSlices b = bu_slices<kBypass, kEarly>(a, wide);
+    void *args[] = {(void *)&a};
+    cudaLaunchKernel(b.func, dim3(b.l.grid), dim3(b.l.block), args, b.smem, st);
 }
 
 // while (!done) { decide; switch { td | prep+td | bu | bu-nobypass }; end }
@@ -991,7 +1073,8 @@ alb_status build_loop_graph(alb_graph *g, int block) {
     cl->block = block;
     BfsArgs a = make_args(g);
     const Launch wide = level_launch(g, block);
-    const Launch one{1, 32};
+    const Launch one{1, 32, g->num_sms};
+    const BuSlices bu2 = bu_slices<true, true>(a, wide), bu3 = bu_slices<false, false>(a, wide);
     ALB_CK(cudaGraphCreate(&cl->graph, 0));
     cudaGraphConditionalHandle wh;
     ALB_CK(cudaGraphConditionalHandleCreate(&wh, cl->graph, 1, cudaGraphCondAssignDefault));
@@ -1019,41 +1102,73 @@ alb_status build_loop_graph(alb_graph *g, int block) {
     {  // 0: top-down, queue ready
         cudaGraph_t b0 = sp.conditional.phGraph_out[0];
         cudaGraphNode_t t, bg, f;
-        ALB_TRY(add_kernel_node(b0, &t, nullptr, 0, (void *)k_td, fit((const void *)k_td, wide), aargs));
-        ALB_TRY(add_kernel_node(b0, &bg, &t, 1, (void *)k_td_big, fit((const void *)k_td_big, wide), aargs));
+        ALB_TRY(add_kernel_node(b0, &t, nullptr, 0, (void *)k_td, fit((const void *)k_td, wide),
+                                aargs));
+        ALB_TRY(add_kernel_node(b0, &bg, &t, 1, (void *)k_td_big,
+                                fit((const void *)k_td_big, wide), aargs));
         ALB_TRY(add_kernel_node(b0, &f, &bg, 1, (void *)k_td_finish, wide, aargs));
     }
     {  // 1: compaction / clear, then top-down
         cudaGraph_t b1 = sp.conditional.phGraph_out[1];
         cudaGraphNode_t pr, t, bg, f;
         ALB_TRY(add_kernel_node(b1, &pr, nullptr, 0, (void *)k_prep, wide, aargs));
-        ALB_TRY(add_kernel_node(b1, &t, &pr, 1, (void *)k_td, fit((const void *)k_td, wide), aargs));
-        ALB_TRY(add_kernel_node(b1, &bg, &t, 1, (void *)k_td_big, fit((const void *)k_td_big, wide), aargs));
+        ALB_TRY(add_kernel_node(b1, &t, &pr, 1, (void *)k_td, fit((const void *)k_td, wide),
+                                aargs));
+        ALB_TRY(add_kernel_node(b1, &bg, &t, 1, (void *)k_td_big,
+                                fit((const void *)k_td_big, wide), aargs));
         ALB_TRY(add_kernel_node(b1, &f, &bg, 1, (void *)k_td_finish, wide, aargs));
     }
     {  // 2: the long rows (head, tail), then bottom-up with bypass
         cudaGraphNode_t b, l, t;
         ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[2], &l, nullptr, 0,
-                                (void *)k_bu_long<true>, fit((const void *)k_bu_long<true>, wide), aargs));
+                                (void *)k_bu_long<true>,
+                                fit((const void *)k_bu_long<true>, wide), aargs));
         ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[2], &t, &l, 1,
-                                (void *)k_bu_long_tail<true>, fit((const void *)k_bu_long_tail<true>, wide), aargs));
+                                (void *)k_bu_long_tail<true>,
+                                fit((const void *)k_bu_long_tail<true>, wide), aargs));
         ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[2], &b, &t, 1,
-                                (void *)k_bu<true, true>, fit((const void *)k_bu<true, true>, with_block(wide, kBuBlock)), aargs));
+                                bu2.func, bu2.l, aargs, bu2.smem));
     }
     {  // 3: the long rows (head, tail), then bottom-up without bypass
         cudaGraphNode_t b, l, t;
         ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[3], &l, nullptr, 0,
-                                (void *)k_bu_long<false>, fit((const void *)k_bu_long<false>, wide), aargs));
+                                (void *)k_bu_long<false>,
+                                fit((const void *)k_bu_long<false>, wide), aargs));
         ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[3], &t, &l, 1,
-                                (void *)k_bu_long_tail<false>, fit((const void *)k_bu_long_tail<false>, wide), aargs));
+                                (void *)k_bu_long_tail<false>,
+                                fit((const void *)k_bu_long_tail<false>, wide), aargs));
         ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[3], &b, &t, 1,
-                                (void *)k_bu<false, false>, fit((const void *)k_bu<false, false>, with_block(wide, kBuBlock)), aargs));
+                                bu3.func, bu3.l, aargs, bu3.smem));
     }
     void *eargs[] = {&a, &wh};
     cudaGraphNode_t nend;
     ALB_TRY(add_kernel_node(body, &nend, &nswitch, 1, (void *)k_end, one, eargs));
     ALB_CK(cudaGraphInstantiate(&cl->exec, cl->graph, 0));
     return ALB_OK;
+}
+
+// Grid-stride level kernel launched with its resident grid.
+void launch_fit(void *f, const BfsArgs &a, const Launch &wide, cudaStream_t st) {
+    const Launch l = fit(f, wide);
+    void *args[] = {(void *)&a};
+    cudaLaunchKernel(f, dim3(l.grid), dim3(l.block), args, 0, st);
+}
+
+void launch_step(const BfsArgs &a, const Launch &wide, cudaStream_t st, int dir, const BfsCtl &h) {
+    if (dir == ALB_DIR_TOPDOWN) {
+        if (!h.q_valid || h.n_dirty) k_prep<<<wide.grid, wide.block, 0, st>>>(a);
+        launch_fit((void *)k_td, a, wide, st);
+        launch_fit((void *)k_td_big, a, wide, st);
+        k_td_finish<<<wide.grid, wide.block, 0, st>>>(a);
+    } else if (dir == ALB_DIR_BOTTOMUP) {
+        launch_fit((void *)k_bu_long<true>, a, wide, st);
+        launch_fit((void *)k_bu_long_tail<true>, a, wide, st);
+        launch_bu_slices<true, true>(a, wide, st);
+    } else {
+        launch_fit((void *)k_bu_long<false>, a, wide, st);
+        launch_fit((void *)k_bu_long_tail<false>, a, wide, st);
+        launch_bu_slices<false, false>(a, wide, st);
+    }
 }
 
 alb_status run_host_loop(alb_graph *g, const BfsArgs &a, const alb_bfs_opts &o,
@@ -1084,20 +1199,7 @@ alb_status run_host_loop(alb_graph *g, const BfsArgs &a, const alb_bfs_opts &o,
         }
         k_decide<<<1, 32, 0, st>>>(a, dir, 0);
         if (e0) cudaEventRecord(e0, st);
-        if (dir == ALB_DIR_TOPDOWN) {
-            if (!h->q_valid || h->n_dirty) k_prep<<<wide.grid, wide.block, 0, st>>>(a);
-            { const Launch l = fit((const void *)k_td, wide); k_td<<<l.grid, l.block, 0, st>>>(a); }
-            { const Launch l = fit((const void *)k_td_big, wide); k_td_big<<<l.grid, l.block, 0, st>>>(a); }
-            k_td_finish<<<wide.grid, wide.block, 0, st>>>(a);
-        } else if (dir == ALB_DIR_BOTTOMUP) {
-            { const Launch l = fit((const void *)k_bu_long<true>, wide); k_bu_long<true><<<l.grid, l.block, 0, st>>>(a); }
-            { const Launch l = fit((const void *)k_bu_long_tail<true>, wide); k_bu_long_tail<true><<<l.grid, l.block, 0, st>>>(a); }
-            { const Launch l = fit((const void *)k_bu<true, true>, with_block(wide, kBuBlock)); k_bu<true, true><<<l.grid, l.block, 0, st>>>(a); }
-        } else {
-            { const Launch l = fit((const void *)k_bu_long<false>, wide); k_bu_long<false><<<l.grid, l.block, 0, st>>>(a); }
-            { const Launch l = fit((const void *)k_bu_long_tail<false>, wide); k_bu_long_tail<false><<<l.grid, l.block, 0, st>>>(a); }
-            { const Launch l = fit((const void *)k_bu<false, false>, with_block(wide, kBuBlock)); k_bu<false, false><<<l.grid, l.block, 0, st>>>(a); }
-        }
+        launch_step(a, wide, st, dir, *h);
         if (e1) cudaEventRecord(e1, st);
         k_end<<<1, 32, 0, st>>>(a, 0);
         ALB_CK(cudaGetLastError());
@@ -1196,22 +1298,6 @@ alb_status bfs_impl(alb_graph *g, int32_t root, const alb_bfs_opts &o, int32_t *
 }
 
 // Launch the step kernels of one variant for the current level.
-void launch_step(const BfsArgs &a, const Launch &wide, cudaStream_t st, int dir, const BfsCtl &h) {
-    if (dir == ALB_DIR_TOPDOWN) {
-        if (!h.q_valid || h.n_dirty) k_prep<<<wide.grid, wide.block, 0, st>>>(a);
-        { const Launch l = fit((const void *)k_td, wide); k_td<<<l.grid, l.block, 0, st>>>(a); }
-        { const Launch l = fit((const void *)k_td_big, wide); k_td_big<<<l.grid, l.block, 0, st>>>(a); }
-        k_td_finish<<<wide.grid, wide.block, 0, st>>>(a);
-    } else if (dir == ALB_DIR_BOTTOMUP) {
-        { const Launch l = fit((const void *)k_bu_long<true>, wide); k_bu_long<true><<<l.grid, l.block, 0, st>>>(a); }
-        { const Launch l = fit((const void *)k_bu_long_tail<true>, wide); k_bu_long_tail<true><<<l.grid, l.block, 0, st>>>(a); }
-        { const Launch l = fit((const void *)k_bu<true, true>, with_block(wide, kBuBlock)); k_bu<true, true><<<l.grid, l.block, 0, st>>>(a); }
-    } else {
-        { const Launch l = fit((const void *)k_bu_long<false>, wide); k_bu_long<false><<<l.grid, l.block, 0, st>>>(a); }
-        { const Launch l = fit((const void *)k_bu_long_tail<false>, wide); k_bu_long_tail<false><<<l.grid, l.block, 0, st>>>(a); }
-        { const Launch l = fit((const void *)k_bu<false, false>, with_block(wide, kBuBlock)); k_bu<false, false><<<l.grid, l.block, 0, st>>>(a); }
-    }
-}
 
 // Device copies of the state a level step mutates (restored between variants).
 struct LevelSnapshot {

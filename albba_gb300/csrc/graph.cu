@@ -215,10 +215,22 @@ __global__ void k_row_lengths(int64_t n, const int64_t *rp, const int32_t *col, 
     int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     int32_t l = 0;
     if (v < n) {
-        int64_t b = rp[v], e = rp[v + 1];
-        int32_t self = 0;
-        for (int64_t i = b; i < e; i++) self += (col[i] == (int32_t)v);
-        l = (int32_t)(e - b) - self;
+        // rows are sorted: the self-loops are one run, found by two binary
+        // searches (a hub row costs log(deg), not deg)
+        const int64_t b = rp[v], e = rp[v + 1];
+        int64_t lo = b, hi = e;
+        while (lo < hi) {  // first entry >= v
+            const int64_t mid = (lo + hi) >> 1;
+            if (col[mid] < (int32_t)v) lo = mid + 1;
+            else hi = mid;
+        }
+        int64_t lo2 = lo, hi2 = e;
+        while (lo2 < hi2) {  // first entry > v
+            const int64_t mid = (lo2 + hi2) >> 1;
+            if (col[mid] <= (int32_t)v) lo2 = mid + 1;
+            else hi2 = mid;
+        }
+        l = (int32_t)((e - b) - (lo2 - lo));
         len[v] = l;
     }
     l = __reduce_max_sync(kFull, l);

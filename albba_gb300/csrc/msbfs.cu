@@ -309,28 +309,37 @@ __device__ __forceinline__ uint64_t warp_or64(uint64_t v) {
 // by atomicOr (the slice pass wrote 0 there). A row still missing roots with
 // sources left joins the continuation list (nbig[L % 3], big, big_base) for
 // k_ms_bu_long_tail; k_ms_bu_long_fin folds N[p] into the state.
+// Sources [st, en) of one long row, 128 per step: each lane loads four
+// source ids, then their four frontier words, all before using any of them,
+// and keeps a private OR; the warp combines the lanes once per step.
 template <bool kEarly>
 __device__ __forceinline__ uint64_t ms_long_scan(const MsArgs &a, const uint64_t *F,
                                                  const uint32_t *Az, int filt, int64_t st,
                                                  int64_t en, uint64_t acc, uint64_t vis,
                                                  unsigned long long &bytes) {
     const int lane = threadIdx.x & 31;
-    for (int64_t e0 = st; e0 < en; e0 += 32) {
-        const int64_t e = e0 + lane;
-        uint64_t f = 0;
-        bool fetched = false;
-        if (e < en) {
-            const int32_t c = __ldg(a.lcol + e);
-            fetched = !filt || ((__ldg(Az + (c >> 5)) >> (c & 31)) & 1u);
-            if (fetched) f = __ldg(F + c);
+    uint64_t mine = 0;
+    for (int64_t e0 = st; e0 < en; e0 += 128) {
+        int32_t c[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int64_t e = e0 + 32 * u + lane;
+            c[u] = e < en ? __ldg(a.lcol + e) : -1;
         }
-        acc |= warp_or64(f);
+        int fetched = 0;
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            if (c[u] >= 0 && (!filt || ((__ldg(Az + (c[u] >> 5)) >> (c[u] & 31)) & 1u))) {
+                mine |= __ldg(F + c[u]);
+                fetched++;
+            }
+        }
         // columns (and bitmap words when filtering), frontier words fetched
-        const int64_t ne = min((int64_t)32, en - e0);
-        bytes += (filt ? 8 : 4) * ne + 8 * __popc(__ballot_sync(kFull, fetched));
-        if (kEarly && (acc | vis) == kAll) break;
+        const int64_t ne = min((int64_t)128, en - e0);
+        bytes += (filt ? 8 : 4) * ne + 8 * (unsigned long long)warp_sum(fetched);
+        if (kEarly && ((acc | warp_or64(mine)) | vis) == kAll) break;
     }
-    return acc;
+    return acc | warp_or64(mine);
 }
 
 template <bool kEarly>

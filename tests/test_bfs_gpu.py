@@ -241,3 +241,21 @@ def test_scale20_levels_and_validation():
                 olv, opa, nl = oracle.bfs(g.rowptr, g.col, int(r))
                 assert np.array_equal(lv, olv) and np.array_equal(pa, opa)
             assert oracle.validate(g.rowptr, g.col, int(r), lv, pa) == 0
+
+
+@pytest.mark.parametrize("scale,staged", [(18, True), (21, False)])
+def test_frontier_staged_and_global_slice_passes(scale, staged):
+    """The bottom-up slice pass stages the frontier bitmap in shared memory
+    while it fits (192 KB: n up to 1.5M rows) and gathers from global memory
+    beyond; both kernels, on every policy that pulls, match the oracle."""
+    g = ab.gen_rmat(scale, 8, seed=1800 + scale)
+    assert (g.n <= 192 * 1024 * 8) == staged
+    roots = g.pick_roots(2, 3)
+    with ab.Graph(g) as dg:
+        dg.sell_build(32, 1024)
+        for r in roots:
+            olv, opa, _ = oracle.bfs(g.rowptr, g.col, int(r))
+            for policy in ("bottomup", "bottomup_nobypass", "beamer"):
+                for loop in ("graph", "host"):
+                    lv, pa, _ = dg.bfs(int(r), ab.bfs_opts(policy, loop))
+                    assert np.array_equal(lv, olv) and np.array_equal(pa, opa), (policy, loop)
