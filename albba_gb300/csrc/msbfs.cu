@@ -189,91 +189,117 @@ __global__ void __launch_bounds__(kMsBuBlock, 5) k_ms_bu(MsArgs a, int j) {
     unsigned cn = 0, cbits = 0, cfull = 0, cdone = 0;
     unsigned long long cmo = 0, cmi = 0, cedges = 0, bytes = 0;
     const uint64_t pol = l2_evict_first();
-    // words come in runs from the level's counter; the next word's done mask
-    // is requested one iteration ahead, and a word's visited words and slice
-    // geometry are requested together
+    // words come in runs from the level's counter. Software pipeline over
+    // words: the done mask is requested two words ahead and the visited words
+    // and slice geometry one word ahead, so their latency overlaps the
+    // current word's column loads and gathers.
     unsigned long long *ctr = &a.ctl->work[L % 3];
     WordRuns runs;
+    auto geometry = [&](int64_t ww, uint32_t dd, uint64_t &vv, int32_t &wdv, int64_t &sov) {
+        vv = kAll;
+        wdv = 0;
+        sov = 0;
+        if (ww < a.nwords && !(kBypass && dd == kFull)) {
+            const int64_t pw = ww * 32 + lane;
+            // rows past n (padding of the last word) are preset visited;
+            // their slice index is clamped so the loads stay in bounds
+            const int64_t sw = (pw < a.n ? pw : a.n - 1) >> a.log2C;
+            vv = __ldg(a.V + pw);
+            wdv = __ldg(a.width + sw);
+            sov = __ldg(a.slice_off + sw);
+        }
+    };
     int64_t w = runs.first(ctr, a.nwords);
-    uint32_t d_next = w < a.nwords ? __ldg(a.D + w) : kFull;
-    for (int64_t wn; w < a.nwords; w = wn) {
-        const uint32_t d = d_next;
-        wn = runs.after(w, ctr, a.nwords);
-        if (wn < a.nwords) d_next = __ldg(a.D + wn);
+    int64_t w1 = w < a.nwords ? runs.after(w, ctr, a.nwords) : a.nwords;
+    uint32_t d = w < a.nwords ? __ldg(a.D + w) : kFull;
+    uint32_t d1 = w1 < a.nwords ? __ldg(a.D + w1) : kFull;
+    uint64_t vis_c;
+    int32_t wd_c;
+    int64_t so_c;
+    geometry(w, d, vis_c, wd_c, so_c);
+    while (w < a.nwords) {
+        const int64_t w2 = w1 < a.nwords ? runs.after(w1, ctr, a.nwords) : a.nwords;
+        const uint32_t d2 = w2 < a.nwords ? __ldg(a.D + w2) : kFull;
+        uint64_t vis1;
+        int32_t wd1;
+        int64_t so1;
+        geometry(w1, d1, vis1, wd1, so1);
         const int64_t p = w * 32 + lane;
         if (kBypass && d == kFull) {
             N[p] = 0;
             if (lane == 0) An[w] = 0;
-            continue;
-        }
-        bytes += 8;  // V[p]
-        // rows past n (padding of the last word) are preset visited; their
-        // slice index is clamped so the geometry loads stay in bounds
-        const int64_t s = (p < a.n ? p : a.n - 1) >> a.log2C;
-        const uint64_t vis = __ldg(a.V + p);
-        const int32_t wd = __ldg(a.width + s);
-        const int64_t so = __ldg(a.slice_off + s);
-        bool active = vis != kAll;
-        const int32_t ng = active ? (wd + 3) >> 2 : 0;
-        const int4 *cp = a.col4 + (so >> 2) + (p & (a.C - 1));
-        uint64_t acc = 0;
-        // group g+1 is requested before group g's frontier fetches, so each
-        // lane keeps a column load in flight while it waits on the gathers
-        const int32_t pp = (int32_t)p;
-        int4 c = make_int4(pp, pp, pp, pp);
-        if (active && ng > 0) c = ld_stream(cp, pol);
-        for (int32_t g = 0;; g++) {
-            active = active && g < ng;
-            if (!__any_sync(kFull, active)) break;
-            if (!active) continue;
-            int4 nx = make_int4(pp, pp, pp, pp);
-            if (g + 1 < ng) nx = ld_stream(cp + (int64_t)(g + 1) * a.C, pol);
-            // padding entries hold p itself: S[j][p] only has bits already in
-            // V[p], so OR-ing it changes nothing
-            if (kFilt) {
-                const uint32_t z0 = __ldg(Az + (c.x >> 5)), z1 = __ldg(Az + (c.y >> 5)),
-                               z2 = __ldg(Az + (c.z >> 5)), z3 = __ldg(Az + (c.w >> 5));
-                const bool h0 = (z0 >> (c.x & 31)) & 1u, h1 = (z1 >> (c.y & 31)) & 1u,
-                           h2 = (z2 >> (c.z & 31)) & 1u, h3 = (z3 >> (c.w & 31)) & 1u;
-                if (h0) acc |= __ldg(F + c.x);
-                if (h1) acc |= __ldg(F + c.y);
-                if (h2) acc |= __ldg(F + c.z);
-                if (h3) acc |= __ldg(F + c.w);
-                // four columns, four bitmap words, the frontier words fetched
-                bytes += 32 + 8 * (h0 + h1 + h2 + h3);
-            } else {
-                acc |= __ldg(F + c.x) | __ldg(F + c.y) | __ldg(F + c.z) | __ldg(F + c.w);
-                bytes += 48;  // four columns and their four frontier words
+        } else {
+            bytes += 8;  // V[p]
+            const uint64_t vis = vis_c;
+            bool active = vis != kAll;
+            const int32_t ng = active ? (wd_c + 3) >> 2 : 0;
+            const int4 *cp = a.col4 + (so_c >> 2) + (p & (a.C - 1));
+            uint64_t acc = 0;
+            // group g+1 is requested before group g's frontier fetches, so each
+            // lane keeps a column load in flight while it waits on the gathers
+            const int32_t pp = (int32_t)p;
+            int4 c = make_int4(pp, pp, pp, pp);
+            if (active && ng > 0) c = ld_stream(cp, pol);
+            for (int32_t g = 0;; g++) {
+                active = active && g < ng;
+                if (!__any_sync(kFull, active)) break;
+                if (!active) continue;
+                int4 nx = make_int4(pp, pp, pp, pp);
+                if (g + 1 < ng) nx = ld_stream(cp + (int64_t)(g + 1) * a.C, pol);
+                // padding entries hold p itself: S[j][p] only has bits already in
+                // V[p], so OR-ing it changes nothing
+                if (kFilt) {
+                    const uint32_t z0 = __ldg(Az + (c.x >> 5)), z1 = __ldg(Az + (c.y >> 5)),
+                                   z2 = __ldg(Az + (c.z >> 5)), z3 = __ldg(Az + (c.w >> 5));
+                    const bool h0 = (z0 >> (c.x & 31)) & 1u, h1 = (z1 >> (c.y & 31)) & 1u,
+                               h2 = (z2 >> (c.z & 31)) & 1u, h3 = (z3 >> (c.w & 31)) & 1u;
+                    if (h0) acc |= __ldg(F + c.x);
+                    if (h1) acc |= __ldg(F + c.y);
+                    if (h2) acc |= __ldg(F + c.z);
+                    if (h3) acc |= __ldg(F + c.w);
+                    // four columns, four bitmap words, the frontier words fetched
+                    bytes += 32 + 8 * (h0 + h1 + h2 + h3);
+                } else {
+                    acc |= __ldg(F + c.x) | __ldg(F + c.y) | __ldg(F + c.z) | __ldg(F + c.w);
+                    bytes += 48;  // four columns and their four frontier words
+                }
+                if (kEarly && (c.w == pp || (acc | vis) == kAll)) active = false;
+                c = nx;
             }
-            if (kEarly && (c.w == pp || (acc | vis) == kAll)) active = false;
-            c = nx;
-        }
-        const uint64_t nb = acc & ~vis;
-        N[p] = nb;
-        const unsigned nzm = __ballot_sync(kFull, nb != 0);
-        if (lane == 0) An[w] = nzm;
-        bool done_now = false;
-        if (nb) {
-            const uint64_t nv = vis | nb;
-            a.V[p] = nv;
-            const int pc = __popcll(nb);
-            const int32_t od = __ldg(a.odeg + p);
-            bytes += 12;  // V[p] written, push degree
-            cn++;
-            cbits += pc;
-            cmo += od;
-            cedges += (unsigned long long)pc * od;
-            if (nv == kAll) {
-                done_now = true;
-                cdone++;
-                cmi += __ldg(a.ideg + p);
+            const uint64_t nb = acc & ~vis;
+            N[p] = nb;
+            const unsigned nzm = __ballot_sync(kFull, nb != 0);
+            if (lane == 0) An[w] = nzm;
+            bool done_now = false;
+            if (nb) {
+                const uint64_t nv = vis | nb;
+                a.V[p] = nv;
+                const int pc = __popcll(nb);
+                const int32_t od = __ldg(a.odeg + p);
+                bytes += 12;  // V[p] written, push degree
+                cn++;
+                cbits += pc;
+                cmo += od;
+                cedges += (unsigned long long)pc * od;
+                if (nv == kAll) {
+                    done_now = true;
+                    cdone++;
+                    cmi += __ldg(a.ideg + p);
+                }
+            }
+            const unsigned dm = __ballot_sync(kFull, done_now);
+            if (lane == 0 && dm) {
+                a.D[w] = d | dm;
+                cfull += (d != kFull && (d | dm) == kFull);
             }
         }
-        const unsigned dm = __ballot_sync(kFull, done_now);
-        if (lane == 0 && dm) {
-            a.D[w] = d | dm;
-            cfull += (d != kFull && (d | dm) == kFull);
-        }
+        w = w1;
+        d = d1;
+        vis_c = vis1;
+        wd_c = wd1;
+        so_c = so1;
+        w1 = w2;
+        d1 = d2;
     }
     cn = warp_sum(cn);
     cbits = warp_sum(cbits);
@@ -808,29 +834,55 @@ __global__ void k_ms_expand(MsArgs a, int nslots, int base, int nroots, int32_t 
 
 // The same output, one CTA per aligned tile of kExpandTile rows. The sort
 // permutes rows only inside sigma windows, so when sigma divides the tile the
-// positions of the tile's original ids are the tile's own positions: the CTA
-// stages the tile's slot words in shared memory (coalesced), then writes the
-// tile's 256-byte output rows in original-id order, a sequential stream.
+// positions of the tile's original ids are the tile's own positions. The CTA
+// first reads the tile's slot words (coalesced) and folds them, per
+// position, into five words: R = OR of all slots (roots that reached it) and
+// M_t = OR of the slots whose index has bit t set, so that root i's slot
+// index is the number whose bit t is bit i of M_t. It then writes the tile's
+// 256-byte output rows in original-id order, a sequential stream: lane q of a
+// half warp turns nibble q of the five words into the levels of roots
+// 4q .. 4q+3 with a few integer operations, independent of the slot count.
 // First flush, 16-byte aligned output, at most kExpandMaxSlots slots.
 constexpr int kExpandTile = 1024;
 constexpr int kExpandMaxSlots = 16;
-
 constexpr int kExpandThreads = 512;
+constexpr size_t kExpandSmem = (5 * sizeof(uint64_t) + sizeof(int32_t)) * kExpandTile;
+
+// Bit k of the nibble n moves to bit 8k (copies shifted by 0, 7, 14, 21 do
+// not overlap for n < 16, so the product has no carries).
+__device__ __forceinline__ uint32_t nibble_to_bytes(uint32_t n) {
+    return (n * 0x00204081u) & 0x01010101u;
+}
 
 __global__ void __launch_bounds__(kExpandThreads) k_ms_expand_tile(MsArgs a, int nslots, int base,
                                                                    int nroots, int32_t *out) {
-    extern __shared__ uint64_t s_slots[];  // nslots x kExpandTile, then kExpandTile positions
-    int32_t *s_pos = reinterpret_cast<int32_t *>(s_slots + (size_t)nslots * kExpandTile);
+    extern __shared__ uint64_t s_fold[];  // 5 x kExpandTile words, then kExpandTile positions
+    int32_t *s_pos = reinterpret_cast<int32_t *>(s_fold + 5 * kExpandTile);
     const int64_t t0 = (int64_t)blockIdx.x * kExpandTile;
     const int rows = (int)min((int64_t)kExpandTile, a.n - t0);
-    for (int i = threadIdx.x; i < nslots * kExpandTile; i += blockDim.x) {
-        const int jj = i / kExpandTile, r = i % kExpandTile;
-        s_slots[i] = r < rows ? __ldcs(a.S + (int64_t)jj * a.npad + t0 + r) : 0ull;
+    for (int r = threadIdx.x; r < kExpandTile; r += blockDim.x) {
+        uint64_t m0 = 0, m1 = 0, m2 = 0, m3 = 0, all = 0;
+        if (r < rows) {
+#pragma unroll 4
+            for (int jj = 0; jj < nslots; jj++) {
+                const uint64_t w = __ldcs(a.S + (int64_t)jj * a.npad + t0 + r);
+                all |= w;
+                if (jj & 1) m0 |= w;
+                if (jj & 2) m1 |= w;
+                if (jj & 4) m2 |= w;
+                if (jj & 8) m3 |= w;
+            }
+            s_pos[r] = (int32_t)((int64_t)__ldg(a.inv + t0 + r) - t0);  // position in the tile
+        }
+        s_fold[r] = all;
+        s_fold[kExpandTile + r] = m0;
+        s_fold[2 * kExpandTile + r] = m1;
+        s_fold[3 * kExpandTile + r] = m2;
+        s_fold[4 * kExpandTile + r] = m3;
     }
-    for (int r = threadIdx.x; r < rows; r += blockDim.x)
-        s_pos[r] = (int32_t)((int64_t)__ldg(a.inv + t0 + r) - t0);  // position in the tile
     __syncthreads();
     const int q = threadIdx.x & 15;
+    const int sh = 4 * q;
     for (int r = threadIdx.x >> 4; r < rows; r += blockDim.x >> 4) {
         const int64_t v = t0 + r;  // original id
         const int pl = s_pos[r];
@@ -838,18 +890,19 @@ __global__ void __launch_bounds__(kExpandThreads) k_ms_expand_tile(MsArgs a, int
             a.ctl->err = ALB_ERR_DEVICE;
             continue;
         }
-        int32_t l[4] = {-1, -1, -1, -1};
-        for (int jj = 0; jj < nslots; jj++) {
-            const uint32_t b = (uint32_t)(s_slots[jj * kExpandTile + pl] >> (4 * q)) & 0xFu;
-            if (b) {
+        const uint32_t reach =
+            nibble_to_bytes((uint32_t)(s_fold[pl] >> sh) & 0xFu);
+        const uint32_t idx =
+            nibble_to_bytes((uint32_t)(s_fold[kExpandTile + pl] >> sh) & 0xFu) |
+            (nibble_to_bytes((uint32_t)(s_fold[2 * kExpandTile + pl] >> sh) & 0xFu) << 1) |
+            (nibble_to_bytes((uint32_t)(s_fold[3 * kExpandTile + pl] >> sh) & 0xFu) << 2) |
+            (nibble_to_bytes((uint32_t)(s_fold[4 * kExpandTile + pl] >> sh) & 0xFu) << 3);
+        int32_t l[4];
 #pragma unroll
-                for (int k = 0; k < 4; k++)
-                    if ((b >> k) & 1u) l[k] = base + jj;
-            }
+        for (int k = 0; k < 4; k++) {
+            const bool hit = ((reach >> (8 * k)) & 1u) && (sh + k < nroots);
+            l[k] = hit ? base + (int32_t)((idx >> (8 * k)) & 0xFu) : -1;
         }
-#pragma unroll
-        for (int k = 0; k < 4; k++)
-            if (4 * q + k >= nroots) l[k] = -1;
         __stcs(reinterpret_cast<int4 *>(out + v * 64 + 4 * q), make_int4(l[0], l[1], l[2], l[3]));
     }
 }
@@ -904,13 +957,11 @@ void launch_expand(const MsArgs &a, int nslots, int base, bool first, int nroots
     const bool tiled = first && vec && nslots <= kExpandMaxSlots && a.sigma >= 1 &&
                        a.sigma <= kExpandTile && kExpandTile % a.sigma == 0;
     if (tiled) {
-        const size_t sm = (sizeof(uint64_t) * (size_t)std::max(nslots, 1) + sizeof(int32_t)) *
-                          kExpandTile;
         cudaFuncSetAttribute(k_ms_expand_tile, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)((sizeof(uint64_t) * kExpandMaxSlots + sizeof(int32_t)) *
-                                   kExpandTile));
+                             (int)kExpandSmem);
         const unsigned tiles = (unsigned)((a.n + kExpandTile - 1) / kExpandTile);
-        k_ms_expand_tile<<<tiles, kExpandThreads, sm, st>>>(a, nslots, base, nroots, out);
+        k_ms_expand_tile<<<tiles, kExpandThreads, kExpandSmem, st>>>(a, nslots, base, nroots,
+                                                                      out);
     } else if (first && vec)
         k_ms_expand<true, true><<<grid((const void *)k_ms_expand<true, true>), 256, 0, st>>>(
             a, nslots, base, nroots, out);
