@@ -136,20 +136,56 @@ def cmd_worklist(a):
 
 
 def cmd_selector(a):
+    """Held-out evaluation of the learned selector: RMAT at the given scales
+    (edge factor 16, seed 24, not in the training set) plus a held-out grid
+    and Erdos-Renyi graph. Per form: GTEPS with the learned policy and with
+    Beamer (device time, same roots), levels compared bit for bit between the
+    two, and per-level regret of both against the per-level oracle-best
+    variant."""
+    import torch
     from albba_gb300 import selector
-    for form in ("plain", "batched"):
-        w = selector.load(form)
-        if w is None:
-            emit({"config": "selector", "form": form, "error": "no weights"})
-            continue
-        for sc in a.scales:
-            g = ab.gen_rmat(sc, 16, seed=24)
-            pr = selector.profile_graph(g, form, a.roots, seed=7)
-            feat, us, state, group = pr.arrays()
-            mlp = selector.regret(us, selector.mlp_choices(w, feat))
-            beam = selector.regret(us, selector.beamer_choices(state, group, us.argmin(1)))
-            emit({"config": "selector", "form": form, "scale": sc, "levels": len(us),
-                  "mlp_regret": mlp, "beamer_regret": beam})
+    loaded = selector.install()
+    graphs = [(f"rmat s{sc} ef16", (lambda sc=sc: ab.gen_rmat(sc, 16, seed=24))) for sc in a.scales]
+    graphs += [("grid 2048x2048", lambda: ab.gen_grid(2048, 2048, 0.1, 1e-4, seed=77)),
+               ("er 2^22 d8", lambda: ab.gen_er(1 << 22, 8.0, seed=77))]
+    for name, mk in graphs:
+        g = mk()
+        roots = g.pick_roots(64, seed=7)
+        with ab.Graph(g, flags=ab.CSR_SYMMETRIC | ab.CSR_SORTED) as dg:
+            dg.sell_build(32, 1024)
+            for form in ("plain", "batched"):
+                if not loaded.get(form):
+                    emit({"config": "selector", "form": form, "error": "no weights"})
+                    continue
+                res = {}
+                if form == "plain":
+                    sub = roots[:a.roots]
+                    for pol in ("learned", "beamer"):
+                        plain_runs(dg, sub[:1], ab.bfs_opts(pol))
+                        res[pol] = plain_runs(dg, sub, ab.bfs_opts(pol))[0]
+                    same = all(np.array_equal(dg.bfs(int(r), ab.bfs_opts("learned"))[0],
+                                              dg.bfs(int(r), ab.bfs_opts("beamer"))[0])
+                               for r in sub[:4])
+                else:
+                    d = torch.empty((g.n, 64), dtype=torch.int32, device="cuda")
+                    out = {}
+                    for pol in ("learned", "beamer"):
+                        dg.msbfs64_device(roots, d, ab.bfs_opts(pol))
+                        st = dg.msbfs64_device(roots, d, ab.bfs_opts(pol))
+                        res[pol] = st.edges / 2 / st.ms / 1e6
+                        out[pol] = d.cpu().numpy()
+                    same = bool(np.array_equal(out["learned"], out["beamer"]))
+                    del d
+                pr = selector.profile_graph(g, form, min(a.roots, 4), seed=7)
+                feat, us, state, group = pr.arrays()
+                w = selector.load(form)
+                mlp = selector.regret(us, selector.mlp_choices(w, feat))
+                beam = selector.regret(us, selector.beamer_choices(state, group, us.argmin(1)))
+                emit({"config": "selector", "graph": name, "form": form,
+                      "gteps_learned": res["learned"], "gteps_beamer": res["beamer"],
+                      "levels_bit_exact": same, "profiled_levels": len(us),
+                      "mlp_regret": mlp, "beamer_regret": beam})
+        del g
 
 
 def main(argv=None):

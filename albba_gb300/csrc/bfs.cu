@@ -484,23 +484,41 @@ __device__ void bu_long_phase(const BfsArgs &a, int L, Range r) {
     const int64_t nwarps = (int64_t)r.nblk * wpb;
     unsigned long long *cont = &a.ctl->nbig[L % 3];
     unsigned long long bytes = 0;
-    for (int64_t i = (int64_t)r.bid * wpb + (threadIdx.x >> 5); i < a.nlong; i += nwarps) {
-        const int32_t p = __ldg(a.lrow + i);
-        if ((ld_bits<kPersist>(a.vis + (p >> 5)) >> (p & 31)) & 1u) continue;
-        const int64_t st = __ldg(a.lptr + i), en = __ldg(a.lptr + i + 1);
-        const int64_t hen = min(en, st + kLongChunk);
-        bytes += 24;
-        const int32_t found = long_scan<kPersist, kEarly>(a, F, st, hen, bytes);
-        if (lane == 0) {
-            if (found >= 0) {
-                atomicMin(a.parent_pos + p, (uint32_t)__ldg(a.perm + found));
-            } else if (hen < en) {
-                const unsigned long long nch =
-                    (unsigned long long)((en - hen + kLongChunk - 1) / kLongChunk);
-                const unsigned long long old = atomicAdd(cont, (1ull << kBigShift) | nch);
-                const int64_t idx = (int64_t)(old >> kBigShift);
-                a.big[idx] = (int32_t)i;
-                a.big_base[idx] = (int64_t)(old & kBigMask);
+    // rows stay strided over the warps (row gw + k * nwarps goes to warp gw),
+    // but a warp loads the position, visited bit and offsets of its next 32
+    // rows at once, one per lane, then scans the unvisited ones
+    const int64_t gw = (int64_t)r.bid * wpb + (threadIdx.x >> 5);
+    for (int64_t i0 = gw; i0 < a.nlong; i0 += 32 * nwarps) {
+        const int64_t i = i0 + lane * nwarps;
+        int32_t p_l = 0;
+        int64_t st_l = 0, en_l = 0;
+        bool todo_l = false;
+        if (i < a.nlong) {
+            p_l = __ldg(a.lrow + i);
+            st_l = __ldg(a.lptr + i);
+            en_l = __ldg(a.lptr + i + 1);
+            todo_l = !((ld_bits<kPersist>(a.vis + (p_l >> 5)) >> (p_l & 31)) & 1u);
+        }
+        unsigned todo = __ballot_sync(kFull, todo_l);
+        while (todo) {
+            const int b = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const int32_t p = __shfl_sync(kFull, p_l, b);
+            const int64_t st = __shfl_sync(kFull, st_l, b), en = __shfl_sync(kFull, en_l, b);
+            const int64_t hen = min(en, st + kLongChunk);
+            bytes += 24;
+            const int32_t found = long_scan<kPersist, kEarly>(a, F, st, hen, bytes);
+            if (lane == 0) {
+                if (found >= 0) {
+                    atomicMin(a.parent_pos + p, (uint32_t)__ldg(a.perm + found));
+                } else if (hen < en) {
+                    const unsigned long long nch =
+                        (unsigned long long)((en - hen + kLongChunk - 1) / kLongChunk);
+                    const unsigned long long old = atomicAdd(cont, (1ull << kBigShift) | nch);
+                    const int64_t idx = (int64_t)(old >> kBigShift);
+                    a.big[idx] = (int32_t)(i0 + b * nwarps);
+                    a.big_base[idx] = (int64_t)(old & kBigMask);
+                }
             }
         }
     }

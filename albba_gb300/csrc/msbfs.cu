@@ -368,6 +368,57 @@ __device__ __forceinline__ uint64_t ms_long_scan(const MsArgs &a, const uint64_t
     return acc | warp_or64(mine);
 }
 
+// Counters of the long rows folded in one level (per thread).
+struct MsLongCounts {
+    unsigned long long cn = 0, cbits = 0, cmo = 0, cmi = 0, cfull = 0, cedges = 0, cdone = 0;
+    __device__ void flush(const MsArgs &a, int k) {
+        cn = warp_sum(cn);
+        cbits = warp_sum(cbits);
+        cmo = warp_sum(cmo);
+        cmi = warp_sum(cmi);
+        cfull = warp_sum(cfull);
+        cedges = warp_sum(cedges);
+        cdone = warp_sum(cdone);
+        if ((threadIdx.x & 31) == 0 && cn) {
+            atomicAdd(&a.ctl->acc_n[k], cn);
+            atomicAdd(&a.ctl->acc_bits[k], cbits);
+            atomicAdd(&a.ctl->acc_mo[k], cmo);
+            atomicAdd(&a.ctl->acc_mi[k], cmi);
+            atomicAdd(&a.ctl->acc_edges[k], cedges);
+            if (cdone) atomicAdd(&a.ctl->acc_done[k], cdone);
+            if (cfull) atomicAdd(&a.ctl->acc_full[k], cfull);
+        }
+    }
+};
+
+// Long row p reached by the roots nb (not in vis) this level: visited word,
+// nonzero and done bitmaps, counters. One thread per row.
+__device__ __forceinline__ void ms_long_fold(const MsArgs &a, int32_t p, uint64_t nb, uint64_t vis,
+                                             uint32_t *An, MsLongCounts &c) {
+    const uint64_t nv = vis | nb;
+    a.V[p] = nv;
+    const uint32_t bit = 1u << (p & 31);
+    atomicOr(An + (p >> 5), bit);
+    const int pc = __popcll(nb);
+    const int32_t od = __ldg(a.odeg + p);
+    c.cn++;
+    c.cbits += pc;
+    c.cmo += od;
+    c.cedges += (unsigned long long)pc * od;
+    if (nv == kAll) {
+        c.cdone++;
+        c.cmi += __ldg(a.ideg + p);
+        const uint32_t od2 = atomicOr(a.D + (p >> 5), bit);
+        c.cfull += (od2 != kFull && (od2 | bit) == kFull);
+    }
+}
+
+// Head pass over the long rows: a warp loads the position, visited word and
+// offsets of 32 of its rows at once (one per lane), then scans the first
+// kLongChunk sources of every one some root has not visited. A row settled by its head (every root accounted for, or no
+// sources left) is folded in here; the rest go on the continuation list for
+// k_ms_bu_long_tail with their new bits ORed into N[p], and k_ms_bu_long_fin
+// folds them in.
 template <bool kEarly>
 __global__ void k_ms_bu_long(MsArgs a, int j, int filt) {
     if (a.nlong == 0) return;
@@ -378,29 +429,52 @@ __global__ void k_ms_bu_long(MsArgs a, int j, int filt) {
     const int64_t nwarps = (int64_t)gridDim.x * wpb;
     const int L = a.ctl->level;
     const uint32_t *Az = nz_bits(a, L);
+    uint32_t *An = nz_bits(a, L + 1);
     unsigned long long *cont = &a.ctl->nbig[L % 3];
     unsigned long long bytes = 0;
-    for (int64_t i = blockIdx.x * wpb + (threadIdx.x >> 5); i < a.nlong; i += nwarps) {
-        const int32_t p = __ldg(a.lrow + i);
-        const uint64_t vis = __ldg(a.V + p);
-        if (vis == kAll) continue;
-        const int64_t st = __ldg(a.lptr + i), en = __ldg(a.lptr + i + 1);
-        const int64_t hen = min(en, st + kLongChunk);
-        bytes += 24;
-        const uint64_t acc = ms_long_scan<kEarly>(a, F, Az, filt, st, hen, 0ull, vis, bytes);
-        const uint64_t nb = acc & ~vis;
-        if (lane == 0) {
-            if (nb) atomicOr((unsigned long long *)N + p, (unsigned long long)nb);
-            if ((acc | vis) != kAll && hen < en) {
-                const unsigned long long nch =
-                    (unsigned long long)((en - hen + kLongChunk - 1) / kLongChunk);
-                const unsigned long long old = atomicAdd(cont, (1ull << kMsBigShift) | nch);
-                const int64_t idx = (int64_t)(old >> kMsBigShift);
-                a.big[idx] = (int32_t)i;
-                a.big_base[idx] = (int64_t)(old & kMsBigMask);
+    MsLongCounts cnt;
+    // rows stay strided over the warps (row gw + k * nwarps goes to warp gw),
+    // but a warp loads the metadata of its next 32 rows at once, one per lane
+    const int64_t gw = blockIdx.x * wpb + (threadIdx.x >> 5);
+    for (int64_t i0 = gw; i0 < a.nlong; i0 += 32 * nwarps) {
+        const int64_t i = i0 + lane * nwarps;
+        int32_t p_l = 0;
+        uint64_t vis_l = kAll;
+        int64_t st_l = 0, en_l = 0;
+        if (i < a.nlong) {
+            p_l = __ldg(a.lrow + i);
+            st_l = __ldg(a.lptr + i);
+            en_l = __ldg(a.lptr + i + 1);
+            vis_l = __ldg(a.V + p_l);
+        }
+        unsigned todo = __ballot_sync(kFull, vis_l != kAll);
+        while (todo) {
+            const int b = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const int32_t p = __shfl_sync(kFull, p_l, b);
+            const uint64_t vis = __shfl_sync(kFull, vis_l, b);
+            const int64_t st = __shfl_sync(kFull, st_l, b), en = __shfl_sync(kFull, en_l, b);
+            const int64_t hen = min(en, st + kLongChunk);
+            bytes += 24;
+            const uint64_t acc = ms_long_scan<kEarly>(a, F, Az, filt, st, hen, 0ull, vis, bytes);
+            const uint64_t nb = acc & ~vis;
+            if (lane == 0) {
+                if ((acc | vis) != kAll && hen < en) {
+                    if (nb) atomicOr((unsigned long long *)N + p, (unsigned long long)nb);
+                    const unsigned long long nch =
+                        (unsigned long long)((en - hen + kLongChunk - 1) / kLongChunk);
+                    const unsigned long long old = atomicAdd(cont, (1ull << kMsBigShift) | nch);
+                    const int64_t idx = (int64_t)(old >> kMsBigShift);
+                    a.big[idx] = (int32_t)(i0 + b * nwarps);
+                    a.big_base[idx] = (int64_t)(old & kMsBigMask);
+                } else if (nb) {
+                    N[p] = nb;  // the slice pass wrote 0 here
+                    ms_long_fold(a, p, nb, vis, An, cnt);
+                }
             }
         }
     }
+    cnt.flush(a, (L + 1) % 3);
     if (lane == 0 && bytes) atomicAdd(&a.ctl->acc_bytes[(L + 1) % 3], bytes);
 }
 
@@ -443,54 +517,23 @@ __global__ void k_ms_bu_long_tail(MsArgs a, int j, int filt) {
     if (lane == 0 && bytes) atomicAdd(&a.ctl->acc_bytes[(L + 1) % 3], bytes);
 }
 
-// Long rows, second half: thread per long row folds N[p] into V, the
-// nonzero and done bitmaps and the level counters.
+// Long rows on the continuation list: thread per entry folds N[p] (head and
+// tail bits) into the state.
 __global__ void k_ms_bu_long_fin(MsArgs a, int j) {
-    if (a.nlong == 0) return;
-    const uint64_t *N = slot(a, j + 1);
     const int L = a.ctl->level;
-    const int k = (L + 1) % 3;
+    const unsigned long long ctr = a.ctl->nbig[L % 3];
+    if (ctr == 0) return;
+    const int64_t nrows = (int64_t)(ctr >> kMsBigShift);
+    const uint64_t *N = slot(a, j + 1);
     uint32_t *An = nz_bits(a, L + 1);
-    unsigned long long cn = 0, cbits = 0, cmo = 0, cmi = 0, cfull = 0, cedges = 0, cdone = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.nlong;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t p = __ldg(a.lrow + i);
+    MsLongCounts cnt;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nrows;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t p = __ldg(a.lrow + a.big[e]);
         const uint64_t nb = N[p];
-        if (!nb) continue;
-        const uint64_t vis = a.V[p];
-        const uint64_t nv = vis | nb;
-        a.V[p] = nv;
-        const uint32_t bit = 1u << (p & 31);
-        atomicOr(An + (p >> 5), bit);
-        const int pc = __popcll(nb);
-        const int32_t od = __ldg(a.odeg + p);
-        cn++;
-        cbits += pc;
-        cmo += od;
-        cedges += (unsigned long long)pc * od;
-        if (nv == kAll) {
-            cdone++;
-            cmi += __ldg(a.ideg + p);
-            const uint32_t od2 = atomicOr(a.D + (p >> 5), bit);
-            cfull += (od2 != kFull && (od2 | bit) == kFull);
-        }
+        if (nb) ms_long_fold(a, p, nb, a.V[p], An, cnt);
     }
-    cn = warp_sum(cn);
-    cbits = warp_sum(cbits);
-    cmo = warp_sum(cmo);
-    cmi = warp_sum(cmi);
-    cfull = warp_sum(cfull);
-    cedges = warp_sum(cedges);
-    cdone = warp_sum(cdone);
-    if ((threadIdx.x & 31) == 0 && cn) {
-        atomicAdd(&a.ctl->acc_n[k], cn);
-        atomicAdd(&a.ctl->acc_bits[k], cbits);
-        atomicAdd(&a.ctl->acc_mo[k], cmo);
-        atomicAdd(&a.ctl->acc_mi[k], cmi);
-        atomicAdd(&a.ctl->acc_edges[k], cedges);
-        if (cdone) atomicAdd(&a.ctl->acc_done[k], cdone);
-        if (cfull) atomicAdd(&a.ctl->acc_full[k], cfull);
-    }
+    cnt.flush(a, (L + 1) % 3);
 }
 
 // Frontier-nonzero bitmap A[M & 1] -> queue of level M (M = L + ahead):
@@ -527,17 +570,22 @@ __global__ void k_ms_compact(MsArgs a, int ahead) {
     }
 }
 
-// One pushed edge: the roots f reaching v this level. The push that makes
-// N[v] nonzero marks v in the next nonzero bitmap An (the next queue is
-// compacted from it afterwards). N[v] is read first so that the many pushes
-// into a hub stop issuing atomics once its word holds their bits.
+// One pushed edge: the roots f reaching v this level. Only two small words
+// are read per edge: v's done bit (D, 1 bit per row, stays in L2) and N[v]
+// (so that the many pushes into a hub stop issuing atomics once its word
+// holds their bits); f is ORed in without masking by V[v], and
+// k_ms_td_finish removes the roots that had already visited v. A push that
+// finds N[v] empty marks v in the next nonzero bitmap An (setting a bit is
+// idempotent, so racing pushers need no claim); the next queue is compacted
+// from An afterwards.
 __device__ __forceinline__ void ms_push(const MsArgs &a, uint64_t *N, uint32_t *An, int32_t v,
                                         uint64_t f) {
-    const uint64_t vis = __ldg(a.V + v);
+    const uint32_t dw = __ldg(a.D + (v >> 5));
     const uint64_t cur = __ldcg((const unsigned long long *)N + v);
-    const uint64_t nb = f & ~vis;
-    if (!nb || !(nb & ~cur)) return;  // nothing new (cur != 0: already marked)
-    if (atomicOr((unsigned long long *)N + v, nb) == 0) atomicOr(An + (v >> 5), 1u << (v & 31));
+    if ((dw >> (v & 31)) & 1u) return;  // every root has visited v
+    if (!(f & ~cur)) return;            // nothing new
+    atomicOr((unsigned long long *)N + v, (unsigned long long)f);
+    if (!cur) atomicOr(An + (v >> 5), 1u << (v & 31));
 }
 
 
@@ -644,7 +692,7 @@ __global__ void k_ms_td_big(MsArgs a, int j) {
 
 // After a top-down level: fold the new frontier words into V and count.
 __global__ void k_ms_td_finish(MsArgs a, int j) {
-    const uint64_t *N = slot(a, j + 1);
+    uint64_t *N = slot(a, j + 1);
     const int L = a.ctl->level;
     const int32_t *NQ = (L & 1) ? a.q0 : a.q1;
     const int64_t nqlen = (int64_t)a.ctl->qn[(L + 1) % 3];
@@ -653,8 +701,14 @@ __global__ void k_ms_td_finish(MsArgs a, int j) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nqlen;
          i += (int64_t)gridDim.x * blockDim.x) {
         const int32_t v = NQ[i];
-        const uint64_t nb = N[v];
+        const uint64_t raw = N[v];
         const uint64_t old = a.V[v];  // only this thread writes V[v] in this kernel
+        const uint64_t nb = raw & ~old;  // the pushes did not mask by V
+        if (nb != raw) N[v] = nb;
+        if (!nb) {  // reached only by roots that had visited it: not in the frontier
+            atomicAnd(nz_bits(a, L + 1) + (v >> 5), ~(1u << (v & 31)));
+            continue;
+        }
         const uint64_t nv = old | nb;
         a.V[v] = nv;
         const int pc = __popcll(nb);
