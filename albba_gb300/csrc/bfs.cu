@@ -924,11 +924,39 @@ alb_status bfs_scratch_alloc(alb_graph *g) {
     BfsScratch &b = g->bfs;
     if (b.ready) return ALB_OK;
     const int64_t n = g->n, nw = g->sell.nwords;
-    // frontier bitmaps padded to 16 bytes: k_bu_smem copies them whole
+    // the three bitmaps in one allocation (one L2 window covers them), each
+    // padded to 16 bytes: k_bu_smem copies a frontier bitmap whole
     const int64_t nw16 = (nw + 3) & ~3ll;
-    ALB_TRY(dmalloc((void **)&b.bm0, sizeof(uint32_t) * nw16, "frontier bitmap"));
-    ALB_TRY(dmalloc((void **)&b.bm1, sizeof(uint32_t) * nw16, "frontier bitmap"));
-    ALB_TRY(dmalloc((void **)&b.vis, sizeof(uint32_t) * nw, "visited bitmap"));
+    ALB_TRY(dmalloc((void **)&b.bits, sizeof(uint32_t) * 3 * nw16, "bitmaps"));
+    b.bm0 = b.bits;
+    b.bm1 = b.bits + nw16;
+    b.vis = b.bits + 2 * nw16;
+    b.win = cudaAccessPolicyWindow{};
+    if (nw * 4 > kSmemFrontierMax) {
+        // the frontier is gathered from global memory: keep the bitmaps in a
+        // persisting L2 window (the column stream is marked evict-first) so
+        // a level's gathers do not miss on lines the previous level wrote
+        int maxwin = 0, maxpers = 0;
+        cudaDeviceGetAttribute(&maxwin, cudaDevAttrMaxAccessPolicyWindowSize, g->device);
+        cudaDeviceGetAttribute(&maxpers, cudaDevAttrMaxPersistingL2CacheSize, g->device);
+        const size_t bytes = sizeof(uint32_t) * 3 * (size_t)nw16;
+        if (maxwin > 0 && maxpers > 0) {
+            const size_t win = std::min(bytes, (size_t)maxwin);
+            const size_t pers = std::min(win, (size_t)maxpers);
+            size_t cur = 0;
+            cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize);
+            if (cur < pers && cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, pers) != cudaSuccess)
+                cudaGetLastError();
+            cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize);
+            if (cur > 0) {
+                b.win.base_ptr = b.bits;
+                b.win.num_bytes = win;
+                b.win.hitRatio = std::min(1.0f, (float)cur / (float)win);
+                b.win.hitProp = cudaAccessPropertyPersisting;
+                b.win.missProp = cudaAccessPropertyStreaming;
+            }
+        }
+    }
     ALB_TRY(dmalloc((void **)&b.q0, sizeof(int32_t) * n, "frontier queue"));
     ALB_TRY(dmalloc((void **)&b.q1, sizeof(int32_t) * n, "frontier queue"));
     ALB_TRY(dmalloc((void **)&b.big, sizeof(int32_t) * n, "long-row list"));
@@ -945,9 +973,7 @@ alb_status bfs_scratch_alloc(alb_graph *g) {
 
 void bfs_scratch_free(alb_graph *g) {
     BfsScratch &b = g->bfs;
-    dfree(b.bm0);
-    dfree(b.bm1);
-    dfree(b.vis);
+    dfree(b.bits);
     dfree(b.q0);
     dfree(b.q1);
     dfree(b.big);
@@ -1043,7 +1069,8 @@ Launch fit(const void *func, const Launch &w) {
 }
 
 alb_status add_kernel_node(cudaGraph_t graph, cudaGraphNode_t *node, const cudaGraphNode_t *deps,
-                           size_t ndeps, void *func, Launch l, void **args, size_t smem = 0) {
+                           size_t ndeps, void *func, Launch l, void **args, size_t smem = 0,
+                           const cudaAccessPolicyWindow *win = nullptr) {
     cudaKernelNodeParams p;
     std::memset(&p, 0, sizeof(p));
     p.func = func;
@@ -1052,6 +1079,11 @@ alb_status add_kernel_node(cudaGraph_t graph, cudaGraphNode_t *node, const cudaG
     p.sharedMemBytes = (unsigned)smem;
     p.kernelParams = args;
     ALB_CK(cudaGraphAddKernelNode(node, graph, deps, ndeps, &p));
+    if (win) {
+        cudaKernelNodeAttrValue v = {};
+        v.accessPolicyWindow = *win;
+        ALB_CK(cudaGraphKernelNodeSetAttribute(*node, cudaKernelNodeAttributeAccessPolicyWindow, &v));
+    }
     return ALB_OK;
 }
 
@@ -1093,6 +1125,8 @@ alb_status build_loop_graph(alb_graph *g, int block) {
     const Launch wide = level_launch(g, block);
     const Launch one{1, 32, g->num_sms};
     const BuSlices bu2 = bu_slices<true, true>(a, wide), bu3 = bu_slices<false, false>(a, wide);
+    // every level kernel carries the bitmaps' L2 window (when there is one)
+    const cudaAccessPolicyWindow *W = g->bfs.win.num_bytes > 0 ? &g->bfs.win : nullptr;
     ALB_CK(cudaGraphCreate(&cl->graph, 0));
     cudaGraphConditionalHandle wh;
     ALB_CK(cudaGraphConditionalHandleCreate(&wh, cl->graph, 1, cudaGraphCondAssignDefault));
@@ -1109,7 +1143,7 @@ alb_status build_loop_graph(alb_graph *g, int block) {
     int forced = -1;
     void *dargs[] = {&a, &forced, &sh};
     cudaGraphNode_t ndecide;
-    ALB_TRY(add_kernel_node(body, &ndecide, nullptr, 0, (void *)k_decide, one, dargs));
+    ALB_TRY(add_kernel_node(body, &ndecide, nullptr, 0, (void *)k_decide, one, dargs, 0, W));
     cudaGraphNodeParams sp = {cudaGraphNodeTypeConditional};
     sp.conditional.handle = sh;
     sp.conditional.type = cudaGraphCondTypeSwitch;
@@ -1121,46 +1155,46 @@ alb_status build_loop_graph(alb_graph *g, int block) {
         cudaGraph_t b0 = sp.conditional.phGraph_out[0];
         cudaGraphNode_t t, bg, f;
         ALB_TRY(add_kernel_node(b0, &t, nullptr, 0, (void *)k_td, fit((const void *)k_td, wide),
-                                aargs));
+                                aargs, 0, W));
         ALB_TRY(add_kernel_node(b0, &bg, &t, 1, (void *)k_td_big,
-                                fit((const void *)k_td_big, wide), aargs));
-        ALB_TRY(add_kernel_node(b0, &f, &bg, 1, (void *)k_td_finish, wide, aargs));
+                                fit((const void *)k_td_big, wide), aargs, 0, W));
+        ALB_TRY(add_kernel_node(b0, &f, &bg, 1, (void *)k_td_finish, wide, aargs, 0, W));
     }
     {  // 1: compaction / clear, then top-down
         cudaGraph_t b1 = sp.conditional.phGraph_out[1];
         cudaGraphNode_t pr, t, bg, f;
-        ALB_TRY(add_kernel_node(b1, &pr, nullptr, 0, (void *)k_prep, wide, aargs));
+        ALB_TRY(add_kernel_node(b1, &pr, nullptr, 0, (void *)k_prep, wide, aargs, 0, W));
         ALB_TRY(add_kernel_node(b1, &t, &pr, 1, (void *)k_td, fit((const void *)k_td, wide),
-                                aargs));
+                                aargs, 0, W));
         ALB_TRY(add_kernel_node(b1, &bg, &t, 1, (void *)k_td_big,
-                                fit((const void *)k_td_big, wide), aargs));
-        ALB_TRY(add_kernel_node(b1, &f, &bg, 1, (void *)k_td_finish, wide, aargs));
+                                fit((const void *)k_td_big, wide), aargs, 0, W));
+        ALB_TRY(add_kernel_node(b1, &f, &bg, 1, (void *)k_td_finish, wide, aargs, 0, W));
     }
     {  // 2: the long rows (head, tail), then bottom-up with bypass
         cudaGraphNode_t b, l, t;
         ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[2], &l, nullptr, 0,
                                 (void *)k_bu_long<true>,
-                                fit((const void *)k_bu_long<true>, wide), aargs));
+                                fit((const void *)k_bu_long<true>, wide), aargs, 0, W));
         ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[2], &t, &l, 1,
                                 (void *)k_bu_long_tail<true>,
-                                fit((const void *)k_bu_long_tail<true>, wide), aargs));
+                                fit((const void *)k_bu_long_tail<true>, wide), aargs, 0, W));
         ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[2], &b, &t, 1,
-                                bu2.func, bu2.l, aargs, bu2.smem));
+                                bu2.func, bu2.l, aargs, bu2.smem, W));
     }
     {  // 3: the long rows (head, tail), then bottom-up without bypass
         cudaGraphNode_t b, l, t;
         ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[3], &l, nullptr, 0,
                                 (void *)k_bu_long<false>,
-                                fit((const void *)k_bu_long<false>, wide), aargs));
+                                fit((const void *)k_bu_long<false>, wide), aargs, 0, W));
         ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[3], &t, &l, 1,
                                 (void *)k_bu_long_tail<false>,
-                                fit((const void *)k_bu_long_tail<false>, wide), aargs));
+                                fit((const void *)k_bu_long_tail<false>, wide), aargs, 0, W));
         ALB_TRY(add_kernel_node(sp.conditional.phGraph_out[3], &b, &t, 1,
-                                bu3.func, bu3.l, aargs, bu3.smem));
+                                bu3.func, bu3.l, aargs, bu3.smem, W));
     }
     void *eargs[] = {&a, &wh};
     cudaGraphNode_t nend;
-    ALB_TRY(add_kernel_node(body, &nend, &nswitch, 1, (void *)k_end, one, eargs));
+    ALB_TRY(add_kernel_node(body, &nend, &nswitch, 1, (void *)k_end, one, eargs, 0, W));
     ALB_CK(cudaGraphInstantiate(&cl->exec, cl->graph, 0));
     return ALB_OK;
 }
@@ -1270,15 +1304,32 @@ alb_status bfs_impl(alb_graph *g, int32_t root, const alb_bfs_opts &o, int32_t *
     k_init_bulk<<<wide.grid, wide.block, 0, stream>>>(a);
     k_init_root<<<1, 32, 0, stream>>>(a, ip);
     ALB_CK(cudaGetLastError());
-    std::vector<float> step_us;
-    if (o.loop == ALB_LOOP_HOST) {
-        ALB_TRY(run_host_loop(g, a, o, step_us));
-    } else if (o.loop == ALB_LOOP_PERSISTENT) {
-        ALB_TRY(run_persistent(g, a));
-    } else {
-        if (!g->loop || g->loop->block != o.block) ALB_TRY(build_loop_graph(g, o.block));
-        ALB_CK(cudaGraphLaunch(g->loop->exec, stream));
+    // the bitmaps' L2 window applies to the level loop's launches on the
+    // stream (the CUDA-graph loop carries it on its kernel nodes); it is
+    // removed again before the stream is handed back
+    const bool win = g->bfs.win.num_bytes > 0 && o.loop != ALB_LOOP_GRAPH;
+    if (win) {
+        cudaStreamAttrValue v = {};
+        v.accessPolicyWindow = g->bfs.win;
+        ALB_CK(cudaStreamSetAttribute(stream, cudaStreamAttributeAccessPolicyWindow, &v));
     }
+    std::vector<float> step_us;
+    alb_status lrc = ALB_OK;
+    if (o.loop == ALB_LOOP_HOST) {
+        lrc = run_host_loop(g, a, o, step_us);
+    } else if (o.loop == ALB_LOOP_PERSISTENT) {
+        lrc = run_persistent(g, a);
+    } else {
+        if (!g->loop || g->loop->block != o.block) lrc = build_loop_graph(g, o.block);
+        if (lrc == ALB_OK && cudaGraphLaunch(g->loop->exec, stream) != cudaSuccess)
+            lrc = fail(ALB_ERR_CUDA, "cudaGraphLaunch: %s", cudaGetErrorString(cudaGetLastError()));
+    }
+    if (win) {
+        cudaStreamAttrValue v = {};
+        v.accessPolicyWindow.num_bytes = 0;
+        cudaStreamSetAttribute(stream, cudaStreamAttributeAccessPolicyWindow, &v);
+    }
+    ALB_TRY(lrc);
     if (d_level || d_parent) k_scatter<<<wide.grid, wide.block, 0, stream>>>(a, d_level, d_parent);
     ALB_CK(cudaGetLastError());
     ALB_CK(cudaEventRecord(g->ev1, stream));

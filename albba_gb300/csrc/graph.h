@@ -18,6 +18,16 @@ void dfree(void *p);
 // function and block size; 0 if the query fails).
 int resident_blocks(const void *func, int block);
 
+// Launches a grid-stride kernel with as many blocks as are resident at once
+// (2048 / block per SM if the occupancy query fails).
+template <class... P, class... A>
+void launch_resident(void (*f)(P...), int block, int num_sms, cudaStream_t st, A &&...args) {
+    const int per = resident_blocks((const void *)f, block);
+    const int fallback = 2048 / block > 0 ? 2048 / block : 1;
+    const unsigned grid = (unsigned)(num_sms * (per > 0 ? per : fallback));
+    f<<<grid, block, 0, st>>>(static_cast<A &&>(args)...);
+}
+
 // CUDA error check that records the failing call and returns ALB_ERR_CUDA.
 #define ALB_CK(call)                                                                 \
     do {                                                                             \
@@ -62,7 +72,11 @@ struct Sell {
 
 struct BfsScratch {
     bool ready = false;
+    uint32_t *bits = nullptr;  // one allocation: bm0 | bm1 | vis
     uint32_t *bm0 = nullptr, *bm1 = nullptr, *vis = nullptr;
+    // L2 persisting-access window over `bits`, used when the frontier bitmap
+    // is too large to stage in shared memory (num_bytes == 0: none)
+    cudaAccessPolicyWindow win = {};
     int32_t *q0 = nullptr, *q1 = nullptr;
     int32_t *big = nullptr;
     int64_t *big_base = nullptr;

@@ -415,10 +415,10 @@ __device__ __forceinline__ void ms_long_fold(const MsArgs &a, int32_t p, uint64_
 
 // Head pass over the long rows: a warp loads the position, visited word and
 // offsets of 32 of its rows at once (one per lane), then scans the first
-// kLongChunk sources of every one some root has not visited. A row settled by its head (every root accounted for, or no
-// sources left) is folded in here; the rest go on the continuation list for
-// k_ms_bu_long_tail with their new bits ORed into N[p], and k_ms_bu_long_fin
-// folds them in.
+// kLongChunk sources of every one some root has not visited. A row settled
+// by its head (every root accounted for, or no sources left) is folded in
+// here; the rest go on the continuation list for k_ms_bu_long_tail with their
+// new bits ORed into N[p], and k_ms_bu_long_fin folds them in.
 template <bool kEarly>
 __global__ void k_ms_bu_long(MsArgs a, int j, int filt) {
     if (a.nlong == 0) return;
@@ -1120,11 +1120,6 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
     cudaStream_t stream = g->stream;
     const int block = o.block;
     const unsigned wide = (unsigned)(g->num_sms * std::max(1, 2048 / block));
-    // grid-stride kernels get as many blocks as are resident at once (one wave)
-    auto rg = [&](const void *f, int b) -> unsigned {
-        const int per = resident_blocks(f, b);
-        return (unsigned)(g->num_sms * (per > 0 ? per : std::max(1, 2048 / b)));
-    };
     MsInit in;
     std::memset(&in, 0, sizeof(in));
     for (int i = 0; i < nroots; i++) in.roots[i] = roots[i];
@@ -1218,28 +1213,28 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
                                        sizeof(uint64_t) * a.npad, stream));
                 ALB_CK(cudaMemsetAsync(a.A + (int64_t)((L + 1) & 1) * a.nwords, 0,
                                        sizeof(uint32_t) * a.nwords, stream));
-                k_ms_td<<<rg((const void *)k_ms_td, block), block, 0, stream>>>(a, j);
-                k_ms_td_big<<<rg((const void *)k_ms_td_big, block), block, 0, stream>>>(a, j);
+                launch_resident(k_ms_td, block, g->num_sms, stream, a, j);
+                launch_resident(k_ms_td_big, block, g->num_sms, stream, a, j);
                 k_ms_compact<<<wide, block, 0, stream>>>(a, 1);
-                k_ms_td_finish<<<rg((const void *)k_ms_td_finish, block), block, 0, stream>>>(a, j);
+                launch_resident(k_ms_td_finish, block, g->num_sms, stream, a, j);
                 launches += 4;
             } else if (d == ALB_DIR_BOTTOMUP) {
                 if (filt)
-                    k_ms_bu<true, true, true><<<rg((const void *)k_ms_bu<true, true, true>, kMsBuBlock), kMsBuBlock, 0, stream>>>(a, j);
+                    launch_resident(k_ms_bu<true, true, true>, kMsBuBlock, g->num_sms, stream, a, j);
                 else
-                    k_ms_bu<true, true, false><<<rg((const void *)k_ms_bu<true, true, false>, kMsBuBlock), kMsBuBlock, 0, stream>>>(a, j);
-                k_ms_bu_long<true><<<rg((const void *)k_ms_bu_long<true>, block), block, 0, stream>>>(a, j, filt);
-                k_ms_bu_long_tail<true><<<rg((const void *)k_ms_bu_long_tail<true>, block), block, 0, stream>>>(a, j, filt);
-                k_ms_bu_long_fin<<<rg((const void *)k_ms_bu_long_fin, block), block, 0, stream>>>(a, j);
+                    launch_resident(k_ms_bu<true, true, false>, kMsBuBlock, g->num_sms, stream, a, j);
+                launch_resident(k_ms_bu_long<true>, block, g->num_sms, stream, a, j, filt);
+                launch_resident(k_ms_bu_long_tail<true>, block, g->num_sms, stream, a, j, filt);
+                launch_resident(k_ms_bu_long_fin, block, g->num_sms, stream, a, j);
                 launches += 4;
             } else {
                 if (filt)
-                    k_ms_bu<false, false, true><<<rg((const void *)k_ms_bu<false, false, true>, kMsBuBlock), kMsBuBlock, 0, stream>>>(a, j);
+                    launch_resident(k_ms_bu<false, false, true>, kMsBuBlock, g->num_sms, stream, a, j);
                 else
-                    k_ms_bu<false, false, false><<<rg((const void *)k_ms_bu<false, false, false>, kMsBuBlock), kMsBuBlock, 0, stream>>>(a, j);
-                k_ms_bu_long<false><<<rg((const void *)k_ms_bu_long<false>, block), block, 0, stream>>>(a, j, filt);
-                k_ms_bu_long_tail<false><<<rg((const void *)k_ms_bu_long_tail<false>, block), block, 0, stream>>>(a, j, filt);
-                k_ms_bu_long_fin<<<rg((const void *)k_ms_bu_long_fin, block), block, 0, stream>>>(a, j);
+                    launch_resident(k_ms_bu<false, false, false>, kMsBuBlock, g->num_sms, stream, a, j);
+                launch_resident(k_ms_bu_long<false>, block, g->num_sms, stream, a, j, filt);
+                launch_resident(k_ms_bu_long_tail<false>, block, g->num_sms, stream, a, j, filt);
+                launch_resident(k_ms_bu_long_fin, block, g->num_sms, stream, a, j);
                 launches += 4;
             }
             return ALB_OK;

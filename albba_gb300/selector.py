@@ -21,7 +21,9 @@ from __future__ import annotations
 
 import argparse
 import json
+import sys
 import time
+from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass, field
 from pathlib import Path
 
@@ -200,15 +202,25 @@ def run(full: bool, forms, roots: int, steps: int, heldout_scale: int, log=print
         out_dir: Path | None = None) -> dict:
     report = {}
     specs = training_specs(full)
-    for form in forms:
-        t0 = time.time()
-        data = Profiles()
+    # every graph is generated once and profiled for every form; the host
+    # generates the next graph while the GPU profiles the current one
+    t0 = time.time()
+    datas = {form: Profiles() for form in forms}
+    with ThreadPoolExecutor(max_workers=1) as pool:
+        nxt = pool.submit(make_graph, specs[0]) if specs else None
         for i, spec in enumerate(specs):
-            csr = make_graph(spec)
-            data.extend(profile_graph(csr, form, roots, seed=11 + i))
+            csr = nxt.result()
+            nxt = pool.submit(make_graph, specs[i + 1]) if i + 1 < len(specs) else None
+            for form in forms:
+                datas[form].extend(profile_graph(csr, form, roots, seed=11 + i))
             del csr
-        feat, us, state, group = data.arrays()
-        t1 = time.time()
+            if (i + 1) % 25 == 0:
+                print(f"profiled {i + 1}/{len(specs)} graphs in {time.time() - t0:.0f} s",
+                      file=sys.stderr, flush=True)
+    t1 = time.time()
+    for form in forms:
+        feat, us, state, group = datas[form].arrays()
+        tf = time.time()
         params, loss = train(feat, us, steps=steps)
         t2 = time.time()
         best = us.argmin(axis=1)
@@ -222,7 +234,7 @@ def run(full: bool, forms, roots: int, steps: int, heldout_scale: int, log=print
         held = {"mlp": regret(hus, mlp_choices(params, hf)),
                 "beamer": regret(hus, beamer_choices(hst, hgr, hb))}
         meta = {"graphs": len(specs), "full_spec": full, "levels": int(len(us)),
-                "train_loss": loss, "steps": steps, "profile_s": t1 - t0, "train_s": t2 - t1,
+                "train_loss": loss, "steps": steps, "profile_s": t1 - t0, "train_s": t2 - tf,
                 "train_regret": tr, "heldout": {"graph": f"rmat s{heldout_scale} ef16",
                                                 "regret": held}}
         save(params, form, meta, out_dir)
