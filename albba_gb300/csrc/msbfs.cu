@@ -45,7 +45,21 @@ struct MsCtl {
         qn[3], acc_bytes[3], acc_done[3], nbig[3], work[3];
     int64_t launches;
     float feat_mean_deg, feat_skew;
+    // set for the next level by k_ms_end (and for level 0 by k_ms_roots):
+    // frontier-nonzero filter on/off, the CUDA-graph switch branch, and
+    // whether the snapshot store must be flushed before the level runs
+    int32_t filt, branch, need_flush, level_cap;
+    int64_t m_in;
 };
+
+// Branches of the CUDA-graph level loop's switch node.
+enum MsBranch { kBrTD = 0, kBrBUFilt, kBrBU, kBrBUNBFilt, kBrBUNB, kBrCount };
+
+__host__ __device__ inline int ms_branch_of(int dir, int filt) {
+    if (dir == ALB_DIR_TOPDOWN) return kBrTD;
+    if (dir == ALB_DIR_BOTTOMUP) return filt ? kBrBUFilt : kBrBU;
+    return filt ? kBrBUNBFilt : kBrBUNB;
+}
 
 struct MsArgs {
     int64_t n, nwords, npad;
@@ -77,6 +91,16 @@ __device__ __forceinline__ uint32_t *nz_bits(const MsArgs &a, int L) {
 
 __device__ __forceinline__ uint64_t *slot(const MsArgs &a, int j) { return a.S + (int64_t)j * a.npad; }
 
+// Level kernels take the slot index j and the filter flag from the host loop,
+// or read them from the control block when launched by the CUDA-graph loop
+// (passed as -1).
+__device__ __forceinline__ int ms_j(const MsArgs &a, int j) {
+    return j >= 0 ? j : a.ctl->level - a.ctl->base;
+}
+__device__ __forceinline__ int ms_filt(const MsArgs &a, int filt) {
+    return filt >= 0 ? filt : a.ctl->filt;
+}
+
 __global__ void k_ms_init(MsArgs a, uint64_t unused) {
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t str = (int64_t)gridDim.x * blockDim.x;
@@ -100,7 +124,7 @@ __global__ void k_ms_init(MsArgs a, uint64_t unused) {
 
 struct MsInit {
     int32_t roots[64];
-    int32_t nroots, policy;
+    int32_t nroots, policy, level_cap;
     float alpha, beta, mean_deg, skew;
     int64_t n_live, m_in, active0;
 };
@@ -162,6 +186,26 @@ __global__ void k_ms_roots(MsArgs a, MsInit in) {
         c.qn[0] = s_nf;
         c.feat_mean_deg = in.mean_deg;
         c.feat_skew = in.skew;
+        c.m_in = in.m_in;
+        c.level_cap = in.level_cap;
+        c.done = c.nf == 0;
+        // level 0's direction: the rule of later levels (the learned policy
+        // falls back to Beamer here: no level has run yet)
+        BfsCtl fc;
+        memset(&fc, 0, sizeof(fc));
+        fc.n = c.n;
+        fc.nwords = c.nwords;
+        fc.nf = c.nf;
+        fc.mf = c.mf;
+        fc.nu = c.nu;
+        fc.mu = c.mu;
+        fc.prev_dir = -1;
+        fc.policy = in.policy == ALB_POLICY_LEARNED ? ALB_POLICY_BEAMER : in.policy;
+        fc.alpha = in.alpha;
+        fc.beta = in.beta;
+        c.dir = rule_dir(fc);
+        c.filt = c.mf < c.m_in / 8;
+        c.branch = ms_branch_of(c.dir, c.filt);
         *a.ctl = c;
     }
 }
@@ -178,6 +222,7 @@ constexpr int kMsBuBlock = 256;
 
 template <bool kBypass, bool kEarly, bool kFilt>
 __global__ void __launch_bounds__(kMsBuBlock, 5) k_ms_bu(MsArgs a, int j) {
+    j = ms_j(a, j);
     const uint64_t *F = slot(a, j);
     uint64_t *N = slot(a, j + 1);
     const int lane = threadIdx.x & 31;
@@ -421,6 +466,8 @@ __device__ __forceinline__ void ms_long_fold(const MsArgs &a, int32_t p, uint64_
 // new bits ORed into N[p], and k_ms_bu_long_fin folds them in.
 template <bool kEarly>
 __global__ void k_ms_bu_long(MsArgs a, int j, int filt) {
+    j = ms_j(a, j);
+    filt = ms_filt(a, filt);
     if (a.nlong == 0) return;
     const uint64_t *F = slot(a, j);
     uint64_t *N = slot(a, j + 1);
@@ -483,6 +530,8 @@ __global__ void k_ms_bu_long(MsArgs a, int j, int filt) {
 // the scan starts from the bits N[p] already holds so it can stop early.
 template <bool kEarly>
 __global__ void k_ms_bu_long_tail(MsArgs a, int j, int filt) {
+    j = ms_j(a, j);
+    filt = ms_filt(a, filt);
     const int L = a.ctl->level;
     const unsigned long long ctr = a.ctl->nbig[L % 3];
     if (ctr == 0) return;
@@ -520,6 +569,7 @@ __global__ void k_ms_bu_long_tail(MsArgs a, int j, int filt) {
 // Long rows on the continuation list: thread per entry folds N[p] (head and
 // tail bits) into the state.
 __global__ void k_ms_bu_long_fin(MsArgs a, int j) {
+    j = ms_j(a, j);
     const int L = a.ctl->level;
     const unsigned long long ctr = a.ctl->nbig[L % 3];
     if (ctr == 0) return;
@@ -543,6 +593,7 @@ __global__ void k_ms_bu_long_fin(MsArgs a, int j) {
 // (whose pushes only mark the bitmap, so no atomic counter is shared by
 // every claim).
 __global__ void k_ms_compact(MsArgs a, int ahead) {
+    if (ahead == 0 && a.ctl->q_valid) return;  // the queue already lists the frontier
     const int M = a.ctl->level + ahead;
     const uint32_t *Az = nz_bits(a, M);
     int32_t *Q = (M & 1) ? a.q1 : a.q0;
@@ -590,6 +641,7 @@ __device__ __forceinline__ void ms_push(const MsArgs &a, uint64_t *N, uint32_t *
 
 
 __global__ void k_ms_td(MsArgs a, int j) {
+    j = ms_j(a, j);
     const uint64_t *F = slot(a, j);
     uint64_t *N = slot(a, j + 1);
     const int L = a.ctl->level;
@@ -647,6 +699,7 @@ __global__ void k_ms_td(MsArgs a, int j) {
 // binary search over the chunk bases (monotone in the list index) and walks
 // forward from there.
 __global__ void k_ms_td_big(MsArgs a, int j) {
+    j = ms_j(a, j);
     const int L = a.ctl->level;
     const unsigned long long ctr = a.ctl->nbig[L % 3];
     if (ctr == 0) return;
@@ -692,6 +745,7 @@ __global__ void k_ms_td_big(MsArgs a, int j) {
 
 // After a top-down level: fold the new frontier words into V and count.
 __global__ void k_ms_td_finish(MsArgs a, int j) {
+    j = ms_j(a, j);
     uint64_t *N = slot(a, j + 1);
     const int L = a.ctl->level;
     const int32_t *NQ = (L & 1) ? a.q0 : a.q1;
@@ -763,35 +817,52 @@ __device__ inline void ms_feature_ctl(const MsCtl &m, BfsCtl &c) {
 }
 
 // Rollover of level L's counters and the device-side decision for L+1.
-__global__ void k_ms_end(MsArgs a, int dir) {
+// dir: the direction level L ran (-1: the one recorded in the control block,
+// as in the CUDA-graph loop). wh: the graph loop's while condition (0 when
+// the host drives the loop), cleared when the traversal is done or the
+// snapshot store must be flushed before the next level.
+__global__ void k_ms_end(MsArgs a, int dir, cudaGraphConditionalHandle wh) {
     if (threadIdx.x >= 32) return;
     __shared__ MsCtl s;
+    __shared__ int s_skip;
     if (threadIdx.x == 0) {
         MsCtl c = *a.ctl;
-        const int k = (c.level + 1) % 3;
-        const unsigned long long nn = c.acc_n[k];
-        c.prev_nf = c.nf;
-        c.nf = (int64_t)nn;
-        c.mf = (int64_t)c.acc_mo[k];
-        c.nu -= (int64_t)c.acc_done[k];  // vertices every root has visited
-        c.mu -= (int64_t)c.acc_mi[k];
-        c.active_words -= (int64_t)c.acc_full[k];
-        c.pairs += (int64_t)c.acc_bits[k];
-        c.edges += (int64_t)c.acc_edges[k];
-        c.q_valid = dir == ALB_DIR_TOPDOWN;
-        c.prev_dir = dir;
-        c.dir = dir;
-        if (dir == ALB_DIR_TOPDOWN) c.levels_td++; else c.levels_bu++;
-        c.level++;
-        c.launches += 1;
-        if (nn == 0) c.done = 1;
-        // zero the slots level L+1 accumulates into after the next rollover
-        const int z = (c.level + 1) % 3;
-        c.acc_n[z] = c.acc_mo[z] = c.acc_mi[z] = c.acc_full[z] = c.acc_bits[z] = 0;
-        c.acc_edges[z] = c.qn[z] = c.acc_bytes[z] = c.acc_done[z] = c.nbig[z] = c.work[z] = 0;
+        s_skip = c.done;  // the graph loop's first pass when nothing is left to do
+        if (!c.done) {
+            if (dir < 0) dir = c.dir;
+            const int k = (c.level + 1) % 3;
+            const unsigned long long nn = c.acc_n[k];
+            c.prev_nf = c.nf;
+            c.nf = (int64_t)nn;
+            c.mf = (int64_t)c.acc_mo[k];
+            c.nu -= (int64_t)c.acc_done[k];  // vertices every root has visited
+            c.mu -= (int64_t)c.acc_mi[k];
+            c.active_words -= (int64_t)c.acc_full[k];
+            c.pairs += (int64_t)c.acc_bits[k];
+            c.edges += (int64_t)c.acc_edges[k];
+            c.q_valid = dir == ALB_DIR_TOPDOWN;
+            c.prev_dir = dir;
+            c.dir = dir;
+            if (dir == ALB_DIR_TOPDOWN) c.levels_td++; else c.levels_bu++;
+            c.level++;
+            c.launches += 1;
+            if (nn == 0) c.done = 1;
+            if (!c.done && c.level >= c.level_cap) {  // cannot happen in a BFS: refuse
+                c.done = 1;
+                c.err = ALB_ERR_DEVICE;
+            }
+            // zero the slots level L+1 accumulates into after the next rollover
+            const int z = (c.level + 1) % 3;
+            c.acc_n[z] = c.acc_mo[z] = c.acc_mi[z] = c.acc_full[z] = c.acc_bits[z] = 0;
+            c.acc_edges[z] = c.qn[z] = c.acc_bytes[z] = c.acc_done[z] = c.nbig[z] = c.work[z] = 0;
+        }
         s = c;
     }
     __syncwarp();
+    if (s_skip) {
+        if (threadIdx.x == 0 && wh) cudaGraphSetConditional(wh, 0);
+        return;
+    }
     // decide the next level (one warp; the MLP runs here when loaded)
     BfsCtl fc;
     ms_feature_ctl(s, fc);
@@ -805,8 +876,38 @@ __global__ void k_ms_end(MsArgs a, int dir) {
     }
     if (threadIdx.x == 0) {
         s.dir = next;
+        // nonzero-bitmap filter when under 1/8 of all entries point into the frontier
+        s.filt = s.mf < s.m_in / 8;
+        s.branch = ms_branch_of(next, s.filt);
+        s.need_flush = !s.done && (s.level - s.base + 1 >= a.K);
         *a.ctl = s;
+        if (wh) cudaGraphSetConditional(wh, (s.done || s.need_flush) ? 0u : 1u);
     }
+}
+
+// Graph loop: the level's branch (none once done).
+__global__ void k_ms_branch(MsArgs a, cudaGraphConditionalHandle sh) {
+    const MsCtl *c = a.ctl;
+    cudaGraphSetConditional(sh, c->done ? (unsigned)kBrCount : (unsigned)c->branch);
+}
+
+// After a flush of the snapshot store: slot 0 now holds level `base`.
+__global__ void k_ms_set_base(MsArgs a, int base) {
+    a.ctl->base = base;
+    a.ctl->need_flush = 0;
+}
+
+// Before a top-down level: clear the next snapshot slot and nonzero bitmap.
+__global__ void k_ms_zero_next(MsArgs a, int j) {
+    j = ms_j(a, j);
+    const int L = a.ctl->level;
+    uint64_t *N = slot(a, j + 1);
+    uint32_t *An = nz_bits(a, L + 1);
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t str = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = tid; i < a.npad / 2; i += str)
+        reinterpret_cast<uint4 *>(N)[i] = make_uint4(0u, 0u, 0u, 0u);
+    for (int64_t w = tid; w < a.nwords; w += str) An[w] = 0u;
 }
 
 // Writes the levels held by snapshot slots [0, nslots) (levels base ..) into
@@ -970,6 +1071,10 @@ struct MsScratch {
     int64_t *big_base = nullptr;
     MsCtl *ctl = nullptr, *h_ctl = nullptr;
     int32_t *out = nullptr;
+    // CUDA-graph level loop (built for one block size)
+    cudaGraph_t lg = nullptr;
+    cudaGraphExec_t lexec = nullptr;
+    int lblock = 0;
 };
 
 }  // namespace alb
@@ -995,6 +1100,8 @@ void ms_scratch_free(alb_graph *g) {
     dfree(m.ctl);
     dfree(m.out);
     if (m.h_ctl) cudaFreeHost(m.h_ctl);
+    if (m.lexec) cudaGraphExecDestroy(m.lexec);
+    if (m.lg) cudaGraphDestroy(m.lg);
     delete (MsScratch *)g->ms;
     g->ms = nullptr;
 }
@@ -1109,6 +1216,109 @@ alb_status ms_snapshot(const MsArgs &a, MsSnapshot &s, cudaStream_t st, bool res
     return ALB_OK;
 }
 
+// The level loop as one CUDA graph, decided on the device like the
+// single-root loop:
+//   while (!done && !need_flush) {
+//     k_ms_branch;                    // sets the switch from the control block
+//     switch { TD | BU+filter | BU | BU-no-bypass+filter | BU-no-bypass };
+//     k_ms_end;                       // rollover, next decision, while condition
+//   }
+// Level kernels get j = -1 and filt = -1 and read both from the control
+// block. A flush of the snapshot store ends the loop; the host does it and
+// launches the graph again.
+struct MsNode {
+    void *func;
+    unsigned grid, block;
+};
+
+alb_status ms_add(cudaGraph_t gr, cudaGraphNode_t *node, const cudaGraphNode_t *dep, MsNode k,
+                  void **args) {
+    cudaKernelNodeParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.func = k.func;
+    p.gridDim = dim3(k.grid);
+    p.blockDim = dim3(k.block);
+    p.kernelParams = args;
+    ALB_CK(cudaGraphAddKernelNode(node, gr, dep, dep ? 1 : 0, &p));
+    return ALB_OK;
+}
+
+alb_status build_ms_graph(alb_graph *g, MsScratch &m, MsArgs &a, int block) {
+    if (m.lexec) cudaGraphExecDestroy(m.lexec);
+    if (m.lg) cudaGraphDestroy(m.lg);
+    m.lexec = nullptr;
+    m.lg = nullptr;
+    const int sms = g->num_sms;
+    auto res = [&](const void *f, int b) -> MsNode {
+        const int per = resident_blocks(f, b);
+        return MsNode{(void *)f, (unsigned)(sms * (per > 0 ? per : std::max(1, 2048 / b))),
+                      (unsigned)b};
+    };
+    const MsNode wide{nullptr, (unsigned)(sms * std::max(1, 2048 / block)), (unsigned)block};
+    ALB_CK(cudaGraphCreate(&m.lg, 0));
+    cudaGraphConditionalHandle wh;
+    ALB_CK(cudaGraphConditionalHandleCreate(&wh, m.lg, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams wp = {cudaGraphNodeTypeConditional};
+    wp.conditional.handle = wh;
+    wp.conditional.type = cudaGraphCondTypeWhile;
+    wp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    ALB_CK(cudaGraphAddNode(&wnode, m.lg, nullptr, nullptr, 0, &wp));
+    cudaGraph_t body = wp.conditional.phGraph_out[0];
+    cudaGraphConditionalHandle sh;
+    ALB_CK(cudaGraphConditionalHandleCreate(&sh, body, 0, cudaGraphCondAssignDefault));
+    void *bargs[] = {&a, &sh};
+    cudaGraphNode_t nbranch;
+    ALB_TRY(ms_add(body, &nbranch, nullptr, MsNode{(void *)k_ms_branch, 1, 1}, bargs));
+    cudaGraphNodeParams sp = {cudaGraphNodeTypeConditional};
+    sp.conditional.handle = sh;
+    sp.conditional.type = cudaGraphCondTypeSwitch;
+    sp.conditional.size = kBrCount;
+    cudaGraphNode_t nswitch;
+    ALB_CK(cudaGraphAddNode(&nswitch, body, &nbranch, nullptr, 1, &sp));
+    int jneg = -1, fneg = -1, ahead0 = 0, ahead1 = 1;
+    void *aj[] = {&a, &jneg};
+    void *ajf[] = {&a, &jneg, &fneg};
+    void *ac0[] = {&a, &ahead0};
+    void *ac1[] = {&a, &ahead1};
+    auto chain = [&](cudaGraph_t br, std::initializer_list<std::pair<MsNode, void **>> ks)
+        -> alb_status {
+        cudaGraphNode_t prev = nullptr, cur;
+        for (const auto &k : ks) {
+            ALB_TRY(ms_add(br, &cur, prev ? &prev : nullptr, k.first, k.second));
+            prev = cur;
+        }
+        return ALB_OK;
+    };
+    auto bu = [&](int br, const void *slices, bool early) -> alb_status {
+        const void *hd = early ? (const void *)k_ms_bu_long<true> : (const void *)k_ms_bu_long<false>;
+        const void *tl = early ? (const void *)k_ms_bu_long_tail<true>
+                               : (const void *)k_ms_bu_long_tail<false>;
+        return chain(sp.conditional.phGraph_out[br],
+                     {{res(slices, kMsBuBlock), aj}, {res(hd, block), ajf}, {res(tl, block), ajf},
+                      {res((const void *)k_ms_bu_long_fin, block), aj}});
+    };
+    MsNode cmp = wide;
+    cmp.func = (void *)k_ms_compact;
+    MsNode zero = wide;
+    zero.func = (void *)k_ms_zero_next;
+    ALB_TRY(chain(sp.conditional.phGraph_out[kBrTD],
+                  {{cmp, ac0}, {zero, aj}, {res((const void *)k_ms_td, block), aj},
+                   {res((const void *)k_ms_td_big, block), aj}, {cmp, ac1},
+                   {res((const void *)k_ms_td_finish, block), aj}}));
+    ALB_TRY(bu(kBrBUFilt, (const void *)k_ms_bu<true, true, true>, true));
+    ALB_TRY(bu(kBrBU, (const void *)k_ms_bu<true, true, false>, true));
+    ALB_TRY(bu(kBrBUNBFilt, (const void *)k_ms_bu<false, false, true>, false));
+    ALB_TRY(bu(kBrBUNB, (const void *)k_ms_bu<false, false, false>, false));
+    int dneg = -1;
+    void *eargs[] = {&a, &dneg, &wh};
+    cudaGraphNode_t nend;
+    ALB_TRY(ms_add(body, &nend, &nswitch, MsNode{(void *)k_ms_end, 1, 32}, eargs));
+    ALB_CK(cudaGraphInstantiate(&m.lexec, m.lg, 0));
+    m.lblock = block;
+    return ALB_OK;
+}
+
 alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const alb_bfs_opts &o,
                       int32_t *d_levels, alb_stats *st, std::vector<alb_level_rec> *trace,
                       std::vector<alb_level_profile> *prof = nullptr) {
@@ -1132,174 +1342,177 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
     in.n_live = g->n - s.zero_in;
     in.m_in = s.m_in;
     in.active0 = s.active0;
+    const int32_t level_cap = (int32_t)std::min<int64_t>(g->n + 1, INT32_MAX - 1);
+    in.level_cap = level_cap;
     const uint64_t unused = nroots >= 64 ? 0ull : ~((1ull << nroots) - 1);
     ALB_CK(cudaEventRecord(g->ev0, stream));
     k_ms_init<<<wide, 256, 0, stream>>>(a, unused);
-    k_ms_roots<<<1, 64, 0, stream>>>(a, in);
+    k_ms_roots<<<1, 64, 0, stream>>>(a, in);  // also decides level 0's direction
     ALB_CK(cudaGetLastError());
     int64_t launches = 2;
     MsCtl *h = m.h_ctl;
-    ALB_CK(cudaMemcpyAsync(h, a.ctl, sizeof(MsCtl), cudaMemcpyDeviceToHost, stream));
-    ALB_CK(cudaStreamSynchronize(stream));
-    // level 0's direction: same decision rule as later levels
-    {
-        BfsCtl fc;
-        std::memset(&fc, 0, sizeof(fc));
-        fc.n = h->n;
-        fc.nwords = h->nwords;
-        fc.nf = h->nf;
-        fc.mf = h->mf;
-        fc.nu = h->nu;
-        fc.mu = h->mu;
-        fc.prev_dir = -1;
-        fc.policy = o.policy == ALB_POLICY_LEARNED ? ALB_POLICY_BEAMER : o.policy;
-        fc.alpha = o.alpha;
-        fc.beta = o.beta;
-        h->dir = rule_dir(fc);
-    }
     int base = 0;      // level held by slot 0
     bool first_flush = true;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    if (trace) trace->clear();
-    if (trace || prof) {
-        ALB_CK(cudaEventCreate(&e0));
-        ALB_CK(cudaEventCreate(&e1));
-    }
-    MsSnapshot snap;
-    if (prof) {
-        prof->clear();
-        ALB_TRY(dmalloc((void **)&snap.V, 8 * a.npad, "msbfs snapshot"));
-        ALB_TRY(dmalloc((void **)&snap.D, 4 * a.nwords, "msbfs snapshot"));
-        ALB_TRY(dmalloc((void **)&snap.ctl, sizeof(MsCtl), "msbfs snapshot"));
-    }
-    const int32_t level_cap = (int32_t)std::min<int64_t>(g->n + 1, INT32_MAX - 1);
-    while (!h->done && h->level < level_cap) {
-        const int L = h->level;
-        int j = L - base;
-        if (j + 1 >= m.K) {
-            // snapshot store full: write out levels [base, base + K - 1) and
-            // restart the store from the current frontier
-            if (d_levels) {
-                launch_expand(a, m.K - 1, base, first_flush, nroots, d_levels, g->num_sms, stream);
-                launches++;
-            }
-            first_flush = false;
-            ALB_CK(cudaMemcpyAsync(a.S, a.S + (int64_t)(m.K - 1) * a.npad,
-                                   sizeof(uint64_t) * a.npad, cudaMemcpyDeviceToDevice, stream));
-            base += m.K - 1;
-            j = 0;
+    // flush of the snapshot store: write out levels [base, base + K - 1) and
+    // restart the store from the current frontier
+    auto flush = [&]() -> alb_status {
+        if (d_levels) {
+            launch_expand(a, m.K - 1, base, first_flush, nroots, d_levels, g->num_sms, stream);
+            launches++;
         }
-        int dir = h->dir;
-        alb_level_rec rec;
-        std::memset(&rec, 0, sizeof(rec));
-        rec.dir = dir;
-        rec.level = L;
-        rec.nf = h->nf;
-        rec.mf = h->mf;
-        rec.nu = h->nu;
-        rec.mu = h->mu;
-        rec.active_slices = h->active_words;
-        rec.step_us = -1.f;
-        const bool q_valid = h->q_valid != 0;
-        // nonzero-bitmap filter when under 1/8 of all entries point into the frontier
-        const int filt = (h->mf < s.m_in / 8) ? 1 : 0;
-        auto launch_step = [&](int d) -> alb_status {
-            if (d == ALB_DIR_TOPDOWN) {
-                if (!q_valid) {
-                    k_ms_compact<<<wide, block, 0, stream>>>(a, 0);
-                    launches++;
-                }
-                ALB_CK(cudaMemsetAsync(a.S + (int64_t)(j + 1) * a.npad, 0,
-                                       sizeof(uint64_t) * a.npad, stream));
-                ALB_CK(cudaMemsetAsync(a.A + (int64_t)((L + 1) & 1) * a.nwords, 0,
-                                       sizeof(uint32_t) * a.nwords, stream));
-                launch_resident(k_ms_td, block, g->num_sms, stream, a, j);
-                launch_resident(k_ms_td_big, block, g->num_sms, stream, a, j);
-                k_ms_compact<<<wide, block, 0, stream>>>(a, 1);
-                launch_resident(k_ms_td_finish, block, g->num_sms, stream, a, j);
-                launches += 4;
-            } else if (d == ALB_DIR_BOTTOMUP) {
-                if (filt)
-                    launch_resident(k_ms_bu<true, true, true>, kMsBuBlock, g->num_sms, stream, a, j);
-                else
-                    launch_resident(k_ms_bu<true, true, false>, kMsBuBlock, g->num_sms, stream, a, j);
-                launch_resident(k_ms_bu_long<true>, block, g->num_sms, stream, a, j, filt);
-                launch_resident(k_ms_bu_long_tail<true>, block, g->num_sms, stream, a, j, filt);
-                launch_resident(k_ms_bu_long_fin, block, g->num_sms, stream, a, j);
-                launches += 4;
-            } else {
-                if (filt)
-                    launch_resident(k_ms_bu<false, false, true>, kMsBuBlock, g->num_sms, stream, a, j);
-                else
-                    launch_resident(k_ms_bu<false, false, false>, kMsBuBlock, g->num_sms, stream, a, j);
-                launch_resident(k_ms_bu_long<false>, block, g->num_sms, stream, a, j, filt);
-                launch_resident(k_ms_bu_long_tail<false>, block, g->num_sms, stream, a, j, filt);
-                launch_resident(k_ms_bu_long_fin, block, g->num_sms, stream, a, j);
-                launches += 4;
-            }
-            return ALB_OK;
-        };
-        if (prof) {
-            // time every variant from the same state, then take the fastest
-            alb_level_profile pr;
-            std::memset(&pr, 0, sizeof(pr));
-            ALB_TRY(ms_snapshot(a, snap, stream, false));
-            for (int v = 0; v < 3; v++) {
-                if (v) ALB_TRY(ms_snapshot(a, snap, stream, true));
-                ALB_CK(cudaEventRecord(e0, stream));
-                ALB_TRY(launch_step(v));
-                ALB_CK(cudaEventRecord(e1, stream));
-                ALB_CK(cudaStreamSynchronize(stream));
-                float ms = 0;
-                ALB_CK(cudaEventElapsedTime(&ms, e0, e1));
-                pr.us[v] = ms * 1000.f;
-            }
-            int best = 0;
-            for (int v = 1; v < 3; v++)
-                if (pr.us[v] < pr.us[best]) best = v;
-            ALB_TRY(ms_snapshot(a, snap, stream, true));
-            dir = best;
-            pr.best = best;
-            pr.rec = rec;
-            pr.rec.dir = best;
-            pr.rec.step_us = pr.us[best];
-            BfsCtl fc;
-            std::memset(&fc, 0, sizeof(fc));
-            fc.level = L;
-            fc.n = h->n;
-            fc.nwords = h->nwords;
-            fc.nf = h->nf;
-            fc.mf = h->mf;
-            fc.nu = h->nu;
-            fc.mu = h->mu;
-            fc.active_words = h->active_words;
-            fc.feat_mean_deg = h->feat_mean_deg;
-            fc.feat_skew = h->feat_skew;
-            level_features(fc, pr.feat);
-            prof->push_back(pr);
-        }
-        if (e0) cudaEventRecord(e0, stream);
-        ALB_TRY(launch_step(dir));
-        if (e1) cudaEventRecord(e1, stream);
-        k_ms_end<<<1, 32, 0, stream>>>(a, dir);
+        first_flush = false;
+        ALB_CK(cudaMemcpyAsync(a.S, a.S + (int64_t)(m.K - 1) * a.npad, sizeof(uint64_t) * a.npad,
+                               cudaMemcpyDeviceToDevice, stream));
+        base += m.K - 1;
+        k_ms_set_base<<<1, 1, 0, stream>>>(a, base);
         launches++;
-        ALB_CK(cudaGetLastError());
+        return ALB_OK;
+    };
+    if (o.loop == ALB_LOOP_GRAPH && !trace && !prof) {
+        // device-driven level loop: the host only steps in for flushes
+        if (!m.lexec || m.lblock != block) ALB_TRY(build_ms_graph(g, m, a, block));
+        while (true) {
+            ALB_CK(cudaGraphLaunch(m.lexec, stream));
+            ALB_CK(cudaMemcpyAsync(h, a.ctl, sizeof(MsCtl), cudaMemcpyDeviceToHost, stream));
+            ALB_CK(cudaStreamSynchronize(stream));
+            if (h->err) return fail(h->err, "msbfs: the device refused the traversal");
+            if (h->done || !h->need_flush) break;
+            ALB_TRY(flush());
+        }
+        // per level: branch and end kernels plus the branch's step kernels
+        launches += (int64_t)h->levels_td * 8 + (int64_t)h->levels_bu * 6;
+    } else {
         ALB_CK(cudaMemcpyAsync(h, a.ctl, sizeof(MsCtl), cudaMemcpyDeviceToHost, stream));
         ALB_CK(cudaStreamSynchronize(stream));
-        if (trace) {
-            float ms = 0;
-            cudaEventElapsedTime(&ms, e0, e1);
-            rec.dir = dir;
-            rec.step_us = ms * 1000.f;
-            const int k = (L + 1) % 3;
-            rec.bytes = dir == ALB_DIR_TOPDOWN
-                            ? (int64_t)(20 * rec.nf + 16 * rec.mf + 16 * (int64_t)h->acc_n[k])
-                            : (int64_t)h->acc_bytes[k] + 8 * a.npad + 8 * a.nwords;
-            trace->push_back(rec);
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (trace) trace->clear();
+        if (trace || prof) {
+            ALB_CK(cudaEventCreate(&e0));
+            ALB_CK(cudaEventCreate(&e1));
         }
+        MsSnapshot snap;
+        if (prof) {
+            prof->clear();
+            ALB_TRY(dmalloc((void **)&snap.V, 8 * a.npad, "msbfs snapshot"));
+            ALB_TRY(dmalloc((void **)&snap.D, 4 * a.nwords, "msbfs snapshot"));
+            ALB_TRY(dmalloc((void **)&snap.ctl, sizeof(MsCtl), "msbfs snapshot"));
+        }
+        while (!h->done && h->level < level_cap) {
+            const int L = h->level;
+            int j = L - base;
+            if (j + 1 >= m.K) {
+                ALB_TRY(flush());
+                j = 0;
+            }
+            int dir = h->dir;
+            alb_level_rec rec;
+            std::memset(&rec, 0, sizeof(rec));
+            rec.dir = dir;
+            rec.level = L;
+            rec.nf = h->nf;
+            rec.mf = h->mf;
+            rec.nu = h->nu;
+            rec.mu = h->mu;
+            rec.active_slices = h->active_words;
+            rec.step_us = -1.f;
+            const bool q_valid = h->q_valid != 0;
+            // nonzero-bitmap filter when under 1/8 of all entries point into the frontier
+            const int filt = (h->mf < s.m_in / 8) ? 1 : 0;
+            auto launch_step = [&](int d) -> alb_status {
+                if (d == ALB_DIR_TOPDOWN) {
+                    if (!q_valid) {
+                        k_ms_compact<<<wide, block, 0, stream>>>(a, 0);
+                        launches++;
+                    }
+                    k_ms_zero_next<<<wide, block, 0, stream>>>(a, j);
+                    launch_resident(k_ms_td, block, g->num_sms, stream, a, j);
+                    launch_resident(k_ms_td_big, block, g->num_sms, stream, a, j);
+                    k_ms_compact<<<wide, block, 0, stream>>>(a, 1);
+                    launch_resident(k_ms_td_finish, block, g->num_sms, stream, a, j);
+                    launches += 5;
+                } else if (d == ALB_DIR_BOTTOMUP) {
+                    if (filt)
+                        launch_resident(k_ms_bu<true, true, true>, kMsBuBlock, g->num_sms, stream, a, j);
+                    else
+                        launch_resident(k_ms_bu<true, true, false>, kMsBuBlock, g->num_sms, stream, a, j);
+                    launch_resident(k_ms_bu_long<true>, block, g->num_sms, stream, a, j, filt);
+                    launch_resident(k_ms_bu_long_tail<true>, block, g->num_sms, stream, a, j, filt);
+                    launch_resident(k_ms_bu_long_fin, block, g->num_sms, stream, a, j);
+                    launches += 4;
+                } else {
+                    if (filt)
+                        launch_resident(k_ms_bu<false, false, true>, kMsBuBlock, g->num_sms, stream, a, j);
+                    else
+                        launch_resident(k_ms_bu<false, false, false>, kMsBuBlock, g->num_sms, stream, a, j);
+                    launch_resident(k_ms_bu_long<false>, block, g->num_sms, stream, a, j, filt);
+                    launch_resident(k_ms_bu_long_tail<false>, block, g->num_sms, stream, a, j, filt);
+                    launch_resident(k_ms_bu_long_fin, block, g->num_sms, stream, a, j);
+                    launches += 4;
+                }
+                return ALB_OK;
+            };
+            if (prof) {
+                // time every variant from the same state, then take the fastest
+                alb_level_profile pr;
+                std::memset(&pr, 0, sizeof(pr));
+                ALB_TRY(ms_snapshot(a, snap, stream, false));
+                for (int v = 0; v < 3; v++) {
+                    if (v) ALB_TRY(ms_snapshot(a, snap, stream, true));
+                    ALB_CK(cudaEventRecord(e0, stream));
+                    ALB_TRY(launch_step(v));
+                    ALB_CK(cudaEventRecord(e1, stream));
+                    ALB_CK(cudaStreamSynchronize(stream));
+                    float ms = 0;
+                    ALB_CK(cudaEventElapsedTime(&ms, e0, e1));
+                    pr.us[v] = ms * 1000.f;
+                }
+                int best = 0;
+                for (int v = 1; v < 3; v++)
+                    if (pr.us[v] < pr.us[best]) best = v;
+                ALB_TRY(ms_snapshot(a, snap, stream, true));
+                dir = best;
+                pr.best = best;
+                pr.rec = rec;
+                pr.rec.dir = best;
+                pr.rec.step_us = pr.us[best];
+                BfsCtl fc;
+                std::memset(&fc, 0, sizeof(fc));
+                fc.level = L;
+                fc.n = h->n;
+                fc.nwords = h->nwords;
+                fc.nf = h->nf;
+                fc.mf = h->mf;
+                fc.nu = h->nu;
+                fc.mu = h->mu;
+                fc.active_words = h->active_words;
+                fc.feat_mean_deg = h->feat_mean_deg;
+                fc.feat_skew = h->feat_skew;
+                level_features(fc, pr.feat);
+                prof->push_back(pr);
+            }
+            if (e0) cudaEventRecord(e0, stream);
+            ALB_TRY(launch_step(dir));
+            if (e1) cudaEventRecord(e1, stream);
+            k_ms_end<<<1, 32, 0, stream>>>(a, dir, 0);
+            launches++;
+            ALB_CK(cudaGetLastError());
+            ALB_CK(cudaMemcpyAsync(h, a.ctl, sizeof(MsCtl), cudaMemcpyDeviceToHost, stream));
+            ALB_CK(cudaStreamSynchronize(stream));
+            if (trace) {
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                rec.dir = dir;
+                rec.step_us = ms * 1000.f;
+                const int k = (L + 1) % 3;
+                rec.bytes = dir == ALB_DIR_TOPDOWN
+                                ? (int64_t)(20 * rec.nf + 16 * rec.mf + 16 * (int64_t)h->acc_n[k])
+                                : (int64_t)h->acc_bytes[k] + 8 * a.npad + 8 * a.nwords;
+                trace->push_back(rec);
+            }
+        }
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
     }
-    if (e0) cudaEventDestroy(e0);
-    if (e1) cudaEventDestroy(e1);
     if (!h->done) return fail(ALB_ERR_DEVICE, "msbfs: level cap reached");
     if (d_levels) {
         const int nslots = h->level - base;  // slots 0 .. level-base-1 hold levels
