@@ -11,7 +11,8 @@ namespace alb {
 // Two parameter blocks (0: single-root BFS, 1: 64-root batched BFS); the
 // element after the parameters is 1.0f once weights are loaded. Fixed
 // addresses, so cached CUDA graphs may hold the pointer.
-__device__ float g_selector[2][kMlpParams + 1];
+// 16-byte aligned rows (1444 floats each): mlp_select_warp reads them as float4
+__device__ __align__(16) float g_selector[2][kMlpParams + 1];
 
 static std::mutex g_sel_mu;
 static float g_sel_host[2][kMlpParams];

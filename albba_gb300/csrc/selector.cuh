@@ -60,20 +60,42 @@ __host__ __device__ inline int argmin3(const float *o) {
 
 #ifdef __CUDACC__
 // Warp-parallel forward pass (lane j owns hidden unit j); every lane returns
-// the argmin variant. Must be called by a full warp.
+// the argmin variant. Must be called by a full warp. Each lane first issues
+// all of its parameter loads (its rows of W1 and W2 as 16-byte loads, its
+// biases, its column of W3), so the pass costs one memory round trip rather
+// than one per layer; P must be 16-byte aligned (the parameter blocks are).
 __device__ inline int mlp_select_warp(const float *P, const float *x) {
     const int j = threadIdx.x & 31;
-    float a = P[kMlpB1 + j];
+    const float4 *w1 = reinterpret_cast<const float4 *>(P + kMlpW1 + j * kMlpIn);
+    const float4 *w2 = reinterpret_cast<const float4 *>(P + kMlpW2 + j * kMlpH);
+    float4 r1[kMlpIn / 4], r2[kMlpH / 4];
 #pragma unroll
-    for (int i = 0; i < kMlpIn; i++) a += P[kMlpW1 + j * kMlpIn + i] * x[i];
+    for (int i = 0; i < kMlpIn / 4; i++) r1[i] = __ldg(w1 + i);
+#pragma unroll
+    for (int i = 0; i < kMlpH / 4; i++) r2[i] = __ldg(w2 + i);
+    const float b1 = __ldg(P + kMlpB1 + j), b2 = __ldg(P + kMlpB2 + j);
+    float w3[kMlpOut], b3[kMlpOut];
+#pragma unroll
+    for (int k = 0; k < kMlpOut; k++) {
+        w3[k] = __ldg(P + kMlpW3 + k * kMlpH + j);
+        b3[k] = __ldg(P + kMlpB3 + k);
+    }
+    float a = b1;
+#pragma unroll
+    for (int i = 0; i < kMlpIn / 4; i++)
+        a += r1[i].x * x[4 * i] + r1[i].y * x[4 * i + 1] + r1[i].z * x[4 * i + 2] +
+             r1[i].w * x[4 * i + 3];
     const float h1 = a > 0.f ? a : 0.f;
-    float b = P[kMlpB2 + j];
-#pragma unroll 8
-    for (int i = 0; i < kMlpH; i++) b += P[kMlpW2 + j * kMlpH + i] * __shfl_sync(kFull, h1, i);
+    float b = b2;
+#pragma unroll
+    for (int i = 0; i < kMlpH / 4; i++) {
+        b += r2[i].x * __shfl_sync(kFull, h1, 4 * i) + r2[i].y * __shfl_sync(kFull, h1, 4 * i + 1) +
+             r2[i].z * __shfl_sync(kFull, h1, 4 * i + 2) + r2[i].w * __shfl_sync(kFull, h1, 4 * i + 3);
+    }
     const float h2 = b > 0.f ? b : 0.f;
     float o[kMlpOut];
 #pragma unroll
-    for (int k = 0; k < kMlpOut; k++) o[k] = warp_sum(P[kMlpW3 + k * kMlpH + j] * h2) + P[kMlpB3 + k];
+    for (int k = 0; k < kMlpOut; k++) o[k] = warp_sum(w3[k] * h2) + b3[k];
     return argmin3(o);
 }
 #endif
