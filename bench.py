@@ -61,7 +61,9 @@ def parse():
     p.add_argument("--cpu-roots", type=int, default=1, help="roots timed for the CPU baseline")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-roofline", action="store_true")
-    p.add_argument("--loop", choices=["graph", "host", "persistent"], default="graph")
+    p.add_argument("--loop", choices=["graph", "host", "persistent"], default="graph",
+                   help="level loop of both forms (the batched form has graph and host loops; "
+                        "host lets a profiler see its kernels)")
     p.add_argument("--out", default=None, help="also write the JSON line to this file")
     return p.parse_args()
 
@@ -237,7 +239,7 @@ def run_ours(args, rank: int, world: int, dist) -> None:
     d_pa = torch.empty(n, dtype=torch.int32, device="cuda")
     d_ms = torch.empty((n, 64), dtype=torch.int32, device="cuda")
     policy = "learned" if loaded.get("batched") else "beamer"
-    bopts = ab.bfs_opts(policy)
+    bopts = ab.bfs_opts(policy, args.loop)
     popts = ab.bfs_opts("learned" if loaded.get("plain") else "beamer", args.loop)
     sync = (lambda: dist.barrier()) if dist else (lambda: None)
 
