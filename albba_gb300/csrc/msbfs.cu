@@ -20,6 +20,7 @@
 //   receive atomicOr(S[l+1][v], S[l][u] & ~V[v]) (64-bit atomics); the first
 //   writer of a target appends it to the next queue.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -50,7 +51,26 @@ struct MsCtl {
     // whether the snapshot store must be flushed before the level runs
     int32_t filt, branch, need_flush, level_cap;
     int64_t m_in;
+    // Roots whose frontier is small (or empty) at a bottom-up level: the pull
+    // does not wait for their bits (a row stops once every other root is
+    // accounted for) and a push over their frontier finds their new rows.
+    // Chosen by k_ms_end from per-root frontier counts sampled on every
+    // kSampleStride-th bitmap word (MsSample, filled by k_ms_sample).
+    unsigned long long tmask;
+    int64_t push_edges;  // a root joins tmask below this many estimated push edges
 };
+
+// Rows and push degrees of each root's sampled frontier. Kept beside the
+// control block (same allocation) so that k_ms_end's copy of it stays small.
+struct MsSample {
+    unsigned int rows[64];
+    unsigned long long deg[64];
+};
+
+// Per-root frontier sampling: one bitmap word (32 rows) in kSampleStride.
+constexpr int kSampleStride = 32;
+// Default push budget per root: m_in / kPushRootDiv estimated edges.
+constexpr int kPushRootDiv = 1024;
 
 // Branches of the CUDA-graph level loop's switch node.
 enum MsBranch { kBrTD = 0, kBrBUFilt, kBrBU, kBrBUNBFilt, kBrBUNB, kBrCount };
@@ -82,6 +102,7 @@ struct MsArgs {
     int32_t *big;  // frontier rows longer than kBigRow (top-down)
     int64_t *big_base;
     MsCtl *ctl;
+    MsSample *smp;  // directly after *ctl
     const float *mlp;
 };
 
@@ -126,7 +147,7 @@ struct MsInit {
     int32_t roots[64];
     int32_t nroots, policy, level_cap;
     float alpha, beta, mean_deg, skew;
-    int64_t n_live, m_in, active0;
+    int64_t n_live, m_in, active0, push_edges;
 };
 
 // One block of 64 threads: thread i seeds root i; thread 0 fills the control block.
@@ -134,6 +155,8 @@ __global__ void k_ms_roots(MsArgs a, MsInit in) {
     __shared__ unsigned long long s_nf, s_mf, s_pairs, s_edges, s_done_mi, s_full, s_done_v;
     const int i = threadIdx.x;
     if (i == 0) s_nf = s_mf = s_pairs = s_edges = s_done_mi = s_full = s_done_v = 0;
+    a.smp->rows[i] = 0;
+    a.smp->deg[i] = 0;
     __syncthreads();
     if (i < in.nroots) {
         const int32_t p = a.inv[in.roots[i]];
@@ -188,6 +211,7 @@ __global__ void k_ms_roots(MsArgs a, MsInit in) {
         c.feat_skew = in.skew;
         c.m_in = in.m_in;
         c.level_cap = in.level_cap;
+        c.push_edges = in.push_edges;
         c.done = c.nf == 0;
         // level 0's direction: the rule of later levels (the learned policy
         // falls back to Beamer here: no level has run yet)
@@ -228,6 +252,7 @@ __global__ void __launch_bounds__(kMsBuBlock, 5) k_ms_bu(MsArgs a, int j) {
     const int lane = threadIdx.x & 31;
     const int L = a.ctl->level;
     const int k = (L + 1) % 3;
+    const uint64_t tm = a.ctl->tmask;
     const uint32_t *Az = nz_bits(a, L);
     uint32_t *An = nz_bits(a, L + 1);
     // per-thread counts fit 32 bits; degree sums and bytes need 64
@@ -276,7 +301,9 @@ __global__ void __launch_bounds__(kMsBuBlock, 5) k_ms_bu(MsArgs a, int j) {
         } else {
             bytes += 8;  // V[p]
             const uint64_t vis = vis_c;
-            bool active = vis != kAll;
+            // roots in tmask are found by the push over their frontier
+            const uint64_t visx = vis | tm;
+            bool active = visx != kAll;
             const int32_t ng = active ? (wd_c + 3) >> 2 : 0;
             const int4 *cp = a.col4 + (so_c >> 2) + (p & (a.C - 1));
             uint64_t acc = 0;
@@ -308,7 +335,7 @@ __global__ void __launch_bounds__(kMsBuBlock, 5) k_ms_bu(MsArgs a, int j) {
                     acc |= __ldg(F + c.x) | __ldg(F + c.y) | __ldg(F + c.z) | __ldg(F + c.w);
                     bytes += 48;  // four columns and their four frontier words
                 }
-                if (kEarly && (c.w == pp || (acc | vis) == kAll)) active = false;
+                if (kEarly && (c.w == pp || (acc | visx) == kAll)) active = false;
                 c = nx;
             }
             const uint64_t nb = acc & ~vis;
@@ -424,7 +451,7 @@ struct MsLongCounts {
         cfull = warp_sum(cfull);
         cedges = warp_sum(cedges);
         cdone = warp_sum(cdone);
-        if ((threadIdx.x & 31) == 0 && cn) {
+        if ((threadIdx.x & 31) == 0 && (cn | cbits | cdone)) {
             atomicAdd(&a.ctl->acc_n[k], cn);
             atomicAdd(&a.ctl->acc_bits[k], cbits);
             atomicAdd(&a.ctl->acc_mo[k], cmo);
@@ -475,6 +502,7 @@ __global__ void k_ms_bu_long(MsArgs a, int j, int filt) {
     const int64_t wpb = blockDim.x >> 5;
     const int64_t nwarps = (int64_t)gridDim.x * wpb;
     const int L = a.ctl->level;
+    const uint64_t tm = a.ctl->tmask;  // roots the push handles: not waited for
     const uint32_t *Az = nz_bits(a, L);
     uint32_t *An = nz_bits(a, L + 1);
     unsigned long long *cont = &a.ctl->nbig[L % 3];
@@ -494,7 +522,7 @@ __global__ void k_ms_bu_long(MsArgs a, int j, int filt) {
             en_l = __ldg(a.lptr + i + 1);
             vis_l = __ldg(a.V + p_l);
         }
-        unsigned todo = __ballot_sync(kFull, vis_l != kAll);
+        unsigned todo = __ballot_sync(kFull, (vis_l | tm) != kAll);
         while (todo) {
             const int b = __ffs(todo) - 1;
             todo &= todo - 1;
@@ -503,10 +531,11 @@ __global__ void k_ms_bu_long(MsArgs a, int j, int filt) {
             const int64_t st = __shfl_sync(kFull, st_l, b), en = __shfl_sync(kFull, en_l, b);
             const int64_t hen = min(en, st + kLongChunk);
             bytes += 24;
-            const uint64_t acc = ms_long_scan<kEarly>(a, F, Az, filt, st, hen, 0ull, vis, bytes);
+            const uint64_t acc =
+                ms_long_scan<kEarly>(a, F, Az, filt, st, hen, 0ull, vis | tm, bytes);
             const uint64_t nb = acc & ~vis;
             if (lane == 0) {
-                if ((acc | vis) != kAll && hen < en) {
+                if ((acc | vis | tm) != kAll && hen < en) {
                     if (nb) atomicOr((unsigned long long *)N + p, (unsigned long long)nb);
                     const unsigned long long nch =
                         (unsigned long long)((en - hen + kLongChunk - 1) / kLongChunk);
@@ -543,6 +572,7 @@ __global__ void k_ms_bu_long_tail(MsArgs a, int j, int filt) {
     const int64_t wpb = blockDim.x >> 5;
     const int64_t nwarps = (int64_t)gridDim.x * wpb;
     const uint32_t *Az = nz_bits(a, L);
+    const uint64_t tm = a.ctl->tmask;  // roots the push handles: not waited for
     unsigned long long bytes = 0;
     for (int64_t k = blockIdx.x * wpb + (threadIdx.x >> 5); k < total; k += nwarps) {
         int64_t lo = 0, hi = nrows - 1;
@@ -555,11 +585,11 @@ __global__ void k_ms_bu_long_tail(MsArgs a, int j, int filt) {
         const int32_t p = __ldg(a.lrow + i);
         const uint64_t vis = __ldg(a.V + p);
         const uint64_t have = __ldcg((const unsigned long long *)N + p);
-        if ((have | vis) == kAll) continue;
+        if ((have | vis | tm) == kAll) continue;
         const int64_t st = __ldg(a.lptr + i) + (1 + k - a.big_base[lo]) * kLongChunk;
         const int64_t en = min(__ldg(a.lptr + i + 1), st + kLongChunk);
         bytes += 24;
-        const uint64_t acc = ms_long_scan<kEarly>(a, F, Az, filt, st, en, have, vis, bytes);
+        const uint64_t acc = ms_long_scan<kEarly>(a, F, Az, filt, st, en, have, vis | tm, bytes);
         const uint64_t nb = acc & ~vis & ~have;
         if (lane == 0 && nb) atomicOr((unsigned long long *)N + p, (unsigned long long)nb);
     }
@@ -640,15 +670,54 @@ __device__ __forceinline__ void ms_push(const MsArgs &a, uint64_t *N, uint32_t *
 }
 
 
+// Push of the roots in tmask during a bottom-up level (after the pull): one
+// edge u -> v carrying the roots f. The new roots are claimed on V[v] itself
+// (atomicOr), so concurrent pushers and the pull's own discoveries are never
+// counted twice, and the level's state and counters are updated in place.
+__device__ __forceinline__ void ms_tpush(const MsArgs &a, uint64_t *N, uint32_t *An, int32_t v,
+                                         uint64_t f, MsLongCounts &c) {
+    const uint32_t bit = 1u << (v & 31);
+    if (__ldg(a.D + (v >> 5)) & bit) return;  // visited by every root before this level
+    uint64_t nb = f & ~__ldcg((const unsigned long long *)a.V + v);
+    if (!nb) return;
+    const uint64_t oldv = atomicOr((unsigned long long *)a.V + v, (unsigned long long)nb);
+    nb &= ~oldv;
+    if (!nb) return;
+    const uint64_t oldn = atomicOr((unsigned long long *)N + v, (unsigned long long)nb);
+    const int pc = __popcll(nb);
+    const int32_t od = __ldg(a.odeg + v);
+    c.cbits += pc;
+    c.cedges += (unsigned long long)pc * od;
+    if (oldn == 0) {  // v enters the next frontier
+        c.cn++;
+        c.cmo += od;
+        atomicOr(An + (v >> 5), bit);
+    }
+    if ((oldv | nb) == kAll) {
+        c.cdone++;
+        c.cmi += __ldg(a.ideg + v);
+        const uint32_t od2 = atomicOr(a.D + (v >> 5), bit);
+        c.cfull += (od2 != kFull && (od2 | bit) == kFull);
+    }
+}
+
+// Top-down push over the frontier queue. kPush: the push of a bottom-up
+// level's tmask roots, over the queue k_ms_tq built (next-parity queue and
+// counters, which that level leaves unused), with the state updated in place.
+template <bool kPush>
 __global__ void k_ms_td(MsArgs a, int j) {
     j = ms_j(a, j);
     const uint64_t *F = slot(a, j);
     uint64_t *N = slot(a, j + 1);
     const int L = a.ctl->level;
-    const int32_t *Q = (L & 1) ? a.q1 : a.q0;
-    const int64_t qlen = (int64_t)a.ctl->qn[L % 3];
+    const uint64_t tm = kPush ? a.ctl->tmask : kAll;
+    if (kPush && !tm) return;
+    const int qp = kPush ? L + 1 : L;
+    const int32_t *Q = (qp & 1) ? a.q1 : a.q0;
+    const int64_t qlen = (int64_t)a.ctl->qn[qp % 3];
     uint32_t *An = nz_bits(a, L + 1);
-    unsigned long long *big_slot = &a.ctl->nbig[L % 3];
+    unsigned long long *big_slot = &a.ctl->nbig[qp % 3];
+    MsLongCounts cnt;
     __shared__ int64_t s_ex[32][32];
     __shared__ int64_t s_st[32][32];
     __shared__ uint64_t s_f[32][32];
@@ -666,7 +735,7 @@ __global__ void k_ms_td(MsArgs a, int j) {
         if (u >= 0) {
             st = __ldg(a.prow + u);
             d = __ldg(a.prow + u + 1) - st;
-            f = __ldg(F + u);
+            f = __ldg(F + u) & tm;
             if (d > kBigRow) {  // pushed in chunks by all warps in k_ms_td_big
                 const unsigned long long nch = (unsigned long long)((d + kBigChunk - 1) / kBigChunk);
                 const unsigned long long old = atomicAdd(big_slot, (1ull << kMsBigShift) | nch);
@@ -688,21 +757,27 @@ __global__ void k_ms_td(MsArgs a, int j) {
             for (int step = 16; step > 0; step >>= 1)
                 if (s_ex[wib][jj + step] <= e) jj += step;
             const int32_t v = __ldg(a.pcol + s_st[wib][jj] + (e - s_ex[wib][jj]));
-            ms_push(a, N, An, v, s_f[wib][jj]);
+            if (kPush)
+                ms_tpush(a, N, An, v, s_f[wib][jj], cnt);
+            else
+                ms_push(a, N, An, v, s_f[wib][jj]);
         }
         __syncwarp();
     }
+    if (kPush) cnt.flush(a, (L + 1) % 3);
 }
 
 // Long frontier rows in kBigChunk-edge chunks over all warps. Each warp
 // takes a contiguous run of chunks: it finds the row of its first chunk by
 // binary search over the chunk bases (monotone in the list index) and walks
 // forward from there.
+template <bool kPush>
 __global__ void k_ms_td_big(MsArgs a, int j) {
     j = ms_j(a, j);
     const int L = a.ctl->level;
-    const unsigned long long ctr = a.ctl->nbig[L % 3];
+    const unsigned long long ctr = a.ctl->nbig[(kPush ? L + 1 : L) % 3];
     if (ctr == 0) return;
+    const uint64_t tm = kPush ? a.ctl->tmask : kAll;
     const int64_t nbig = (int64_t)(ctr >> kMsBigShift);
     const int64_t total = (int64_t)(ctr & kMsBigMask);
     const uint64_t *F = slot(a, j);
@@ -714,7 +789,8 @@ __global__ void k_ms_td_big(MsArgs a, int j) {
     const int64_t nwarps = (int64_t)gridDim.x * wpb;
     const int64_t per = (total + nwarps - 1) / nwarps;
     const int64_t k0 = gw * per, k1 = min(total, k0 + per);
-    if (k0 >= k1) return;
+    if (k0 >= k1) return;  // warp-uniform: whole warps leave
+    MsLongCounts cnt;
     int64_t lo = 0, hi = nbig - 1;
     while (lo < hi) {
         const int64_t mid = (lo + hi + 1) >> 1;
@@ -725,7 +801,7 @@ __global__ void k_ms_td_big(MsArgs a, int j) {
     int64_t next = lo + 1 < nbig ? a.big_base[lo + 1] : total;
     int32_t u = a.big[lo];
     int64_t st = __ldg(a.prow + u), d = __ldg(a.prow + u + 1) - st;
-    uint64_t f = __ldg(F + u);
+    uint64_t f = __ldg(F + u) & tm;
     for (int64_t k = k0; k < k1; k++) {
         while (k >= next) {  // the run crosses into the next long row
             lo++;
@@ -734,13 +810,18 @@ __global__ void k_ms_td_big(MsArgs a, int j) {
             u = a.big[lo];
             st = __ldg(a.prow + u);
             d = __ldg(a.prow + u + 1) - st;
-            f = __ldg(F + u);
+            f = __ldg(F + u) & tm;
         }
         const int64_t c = k - base;
         const int64_t e1 = min(d, (c + 1) * kBigChunk);
-        for (int64_t e = c * kBigChunk + lane; e < e1; e += 32)
-            ms_push(a, N, An, __ldg(a.pcol + st + e), f);
+        for (int64_t e = c * kBigChunk + lane; e < e1; e += 32) {
+            if (kPush)
+                ms_tpush(a, N, An, __ldg(a.pcol + st + e), f, cnt);
+            else
+                ms_push(a, N, An, __ldg(a.pcol + st + e), f);
+        }
     }
+    if (kPush) cnt.flush(a, (L + 1) % 3);
 }
 
 // After a top-down level: fold the new frontier words into V and count.
@@ -794,6 +875,108 @@ __global__ void k_ms_td_finish(MsArgs a, int j) {
         atomicAdd(&a.ctl->acc_mi[k], cmi);
         atomicAdd(&a.ctl->acc_edges[k], cedges);
         if (cfull) atomicAdd(&a.ctl->acc_full[k], cfull);
+    }
+}
+
+// Per-root size of the frontier level L produced (S[j+1]), sampled on every
+// kSampleStride-th bitmap word: warp per sampled word, lane i keeps roots i
+// and i + 32; rows and push degrees go to MsSample for k_ms_end.
+constexpr int kSampleBlock = 256;
+
+__global__ void __launch_bounds__(kSampleBlock) k_ms_sample(MsArgs a, int j) {
+    __shared__ unsigned s_cnt[64];
+    __shared__ unsigned long long s_deg[64];
+    // the graph loop's pass after the last level: no next slot to read
+    if (a.ctl->done) return;
+    j = ms_j(a, j);
+    const int L = a.ctl->level;
+    const uint64_t *N = slot(a, j + 1);
+    const uint32_t *An = nz_bits(a, L + 1);
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x < 64) {
+        s_cnt[threadIdx.x] = 0;
+        s_deg[threadIdx.x] = 0;
+    }
+    __syncthreads();
+    unsigned c0 = 0, c1 = 0;
+    unsigned long long d0 = 0, d1 = 0;
+    const int64_t nsamp = (a.nwords + kSampleStride - 1) / kSampleStride;
+    const int64_t wpb = blockDim.x >> 5;
+    for (int64_t sidx = blockIdx.x * wpb + (threadIdx.x >> 5); sidx < nsamp;
+         sidx += (int64_t)gridDim.x * wpb) {
+        const int64_t w = sidx * kSampleStride;
+        uint32_t m = __ldg(An + w);
+        if (!m) continue;
+        const int64_t p = w * 32 + lane;
+        uint64_t x = 0;
+        int32_t od = 0;
+        if ((m >> lane) & 1u) {
+            x = __ldcg((const unsigned long long *)N + p);
+            od = __ldg(a.odeg + p);
+        }
+        while (m) {
+            const int q = __ffs(m) - 1;
+            m &= m - 1;
+            const uint64_t xq = __shfl_sync(kFull, x, q);
+            const int32_t oq = __shfl_sync(kFull, od, q);
+            if ((xq >> lane) & 1ull) {
+                c0++;
+                d0 += (unsigned)oq;
+            }
+            if ((xq >> (lane + 32)) & 1ull) {
+                c1++;
+                d1 += (unsigned)oq;
+            }
+        }
+    }
+    if (c0) {
+        atomicAdd(&s_cnt[lane], c0);
+        atomicAdd(&s_deg[lane], d0);
+    }
+    if (c1) {
+        atomicAdd(&s_cnt[lane + 32], c1);
+        atomicAdd(&s_deg[lane + 32], d1);
+    }
+    __syncthreads();
+    if (threadIdx.x < 64 && s_cnt[threadIdx.x]) {
+        atomicAdd(&a.smp->rows[threadIdx.x], s_cnt[threadIdx.x]);
+        atomicAdd(&a.smp->deg[threadIdx.x], s_deg[threadIdx.x]);
+    }
+}
+
+// Queue of the rows in level L's frontier that hold a tmask root, for the
+// push after a bottom-up level's pull: next-parity queue q[(L + 1) & 1],
+// count qn[(L + 1) % 3] (both idle during a bottom-up level). A warp takes 32
+// bitmap words at a time and reads the frontier words of the set bits only.
+__global__ void k_ms_tq(MsArgs a, int j) {
+    const uint64_t tm = a.ctl->tmask;
+    if (!tm) return;
+    j = ms_j(a, j);
+    const int L = a.ctl->level;
+    const uint64_t *F = slot(a, j);
+    const uint32_t *Az = nz_bits(a, L);
+    int32_t *Q = ((L + 1) & 1) ? a.q1 : a.q0;
+    unsigned long long *qslot = &a.ctl->qn[(L + 1) % 3];
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    // warp-uniform bound: every lane reaches the ballots
+    for (int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) & ~31ll; w0 < a.nwords;
+         w0 += stride) {
+        const uint32_t mine = w0 + lane < a.nwords ? __ldg(Az + w0 + lane) : 0u;
+        unsigned words = __ballot_sync(kFull, mine != 0);
+        while (words) {
+            const int q = __ffs(words) - 1;
+            words &= words - 1;
+            const uint32_t m = __shfl_sync(kFull, mine, q);
+            const int64_t p = (w0 + q) * 32 + lane;
+            const bool hit = ((m >> lane) & 1u) && (__ldg(F + p) & tm);
+            const unsigned hm = __ballot_sync(kFull, hit);
+            if (!hm) continue;
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(qslot, (unsigned long long)__popc(hm));
+            base = __shfl_sync(kFull, base, 0);
+            if (hit) Q[base + __popc(hm & ((1u << lane) - 1u))] = (int32_t)p;
+        }
     }
 }
 
@@ -855,6 +1038,10 @@ __global__ void k_ms_end(MsArgs a, int dir, cudaGraphConditionalHandle wh) {
             const int z = (c.level + 1) % 3;
             c.acc_n[z] = c.acc_mo[z] = c.acc_mi[z] = c.acc_full[z] = c.acc_bits[z] = 0;
             c.acc_edges[z] = c.qn[z] = c.acc_bytes[z] = c.acc_done[z] = c.nbig[z] = c.work[z] = 0;
+            // a bottom-up level's push of its tmask roots used the new level's
+            // long-row counter and, after a bottom-up level, its queue count
+            c.nbig[c.level % 3] = 0;
+            if (!c.q_valid) c.qn[c.level % 3] = 0;
         }
         s = c;
     }
@@ -873,6 +1060,21 @@ __global__ void k_ms_end(MsArgs a, int dir, cudaGraphConditionalHandle wh) {
         next = mlp_select_warp(a.mlp, f);
     } else {
         next = rule_dir(fc);
+    }
+    // roots pushed instead of pulled at a bottom-up level: those whose sampled
+    // frontier's push degree, scaled by the sampling stride, is within budget.
+    // The samples are cleared for the next level.
+    {
+        const int i = threadIdx.x;
+        const bool bu = next != ALB_DIR_TOPDOWN && !s.done && s.push_edges > 0;
+        const unsigned long long d0 = a.smp->deg[i], d1 = a.smp->deg[i + 32];
+        const unsigned long long lim = (unsigned long long)s.push_edges;
+        const unsigned lo = __ballot_sync(kFull, bu && d0 * kSampleStride < lim);
+        const unsigned hi = __ballot_sync(kFull, bu && d1 * kSampleStride < lim);
+        a.smp->rows[i] = a.smp->rows[i + 32] = 0;
+        a.smp->deg[i] = a.smp->deg[i + 32] = 0;
+        if (i == 0) s.tmask = (unsigned long long)lo | ((unsigned long long)hi << 32);
+        __syncwarp();
     }
     if (threadIdx.x == 0) {
         s.dir = next;
@@ -1147,7 +1349,7 @@ alb_status ms_alloc(alb_graph *g, MsScratch &m) {
     ALB_TRY(dmalloc((void **)&m.q1, sizeof(int32_t) * npad, "msbfs queue"));
     ALB_TRY(dmalloc((void **)&m.big, sizeof(int32_t) * npad, "msbfs long-row list"));
     ALB_TRY(dmalloc((void **)&m.big_base, sizeof(int64_t) * npad, "msbfs long-row chunk bases"));
-    ALB_TRY(dmalloc((void **)&m.ctl, sizeof(MsCtl), "msbfs control"));
+    ALB_TRY(dmalloc((void **)&m.ctl, sizeof(MsCtl) + sizeof(MsSample), "msbfs control"));
     ALB_CK(cudaMallocHost((void **)&m.h_ctl, sizeof(MsCtl)));
     m.ready = true;
     return ALB_OK;
@@ -1186,6 +1388,7 @@ MsArgs ms_args(alb_graph *g, MsScratch &m) {
     a.big = m.big;
     a.big_base = m.big_base;
     a.ctl = m.ctl;
+    a.smp = reinterpret_cast<MsSample *>(m.ctl + 1);
     return a;
 }
 
@@ -1211,7 +1414,8 @@ alb_status ms_snapshot(const MsArgs &a, MsSnapshot &s, cudaStream_t st, bool res
     };
     cudaError_t e = restore ? cp(a.V, s.V, 8 * a.npad) : cp(s.V, a.V, 8 * a.npad);
     if (e == cudaSuccess) e = restore ? cp(a.D, s.D, 4 * a.nwords) : cp(s.D, a.D, 4 * a.nwords);
-    if (e == cudaSuccess) e = restore ? cp(a.ctl, s.ctl, sizeof(MsCtl)) : cp(s.ctl, a.ctl, sizeof(MsCtl));
+    const size_t cb = sizeof(MsCtl) + sizeof(MsSample);
+    if (e == cudaSuccess) e = restore ? cp(a.ctl, s.ctl, cb) : cp(s.ctl, a.ctl, cb);
     if (e != cudaSuccess) return fail(ALB_ERR_CUDA, "msbfs snapshot: %s", cudaGetErrorString(e));
     return ALB_OK;
 }
@@ -1221,6 +1425,7 @@ alb_status ms_snapshot(const MsArgs &a, MsSnapshot &s, cudaStream_t st, bool res
 //   while (!done && !need_flush) {
 //     k_ms_branch;                    // sets the switch from the control block
 //     switch { TD | BU+filter | BU | BU-no-bypass+filter | BU-no-bypass };
+//     k_ms_sample;                    // per-root frontier sizes
 //     k_ms_end;                       // rollover, next decision, while condition
 //   }
 // Level kernels get j = -1 and filt = -1 and read both from the control
@@ -1255,6 +1460,8 @@ alb_status build_ms_graph(alb_graph *g, MsScratch &m, MsArgs &a, int block) {
                       (unsigned)b};
     };
     const MsNode wide{nullptr, (unsigned)(sms * std::max(1, 2048 / block)), (unsigned)block};
+    MsNode tq = wide;
+    tq.func = (void *)k_ms_tq;
     ALB_CK(cudaGraphCreate(&m.lg, 0));
     cudaGraphConditionalHandle wh;
     ALB_CK(cudaGraphConditionalHandleCreate(&wh, m.lg, 1, cudaGraphCondAssignDefault));
@@ -1296,15 +1503,17 @@ alb_status build_ms_graph(alb_graph *g, MsScratch &m, MsArgs &a, int block) {
                                : (const void *)k_ms_bu_long_tail<false>;
         return chain(sp.conditional.phGraph_out[br],
                      {{res(slices, kMsBuBlock), aj}, {res(hd, block), ajf}, {res(tl, block), ajf},
-                      {res((const void *)k_ms_bu_long_fin, block), aj}});
+                      {res((const void *)k_ms_bu_long_fin, block), aj}, {tq, aj},
+                      {res((const void *)k_ms_td<true>, block), aj},
+                      {res((const void *)k_ms_td_big<true>, block), aj}});
     };
     MsNode cmp = wide;
     cmp.func = (void *)k_ms_compact;
     MsNode zero = wide;
     zero.func = (void *)k_ms_zero_next;
     ALB_TRY(chain(sp.conditional.phGraph_out[kBrTD],
-                  {{cmp, ac0}, {zero, aj}, {res((const void *)k_ms_td, block), aj},
-                   {res((const void *)k_ms_td_big, block), aj}, {cmp, ac1},
+                  {{cmp, ac0}, {zero, aj}, {res((const void *)k_ms_td<false>, block), aj},
+                   {res((const void *)k_ms_td_big<false>, block), aj}, {cmp, ac1},
                    {res((const void *)k_ms_td_finish, block), aj}}));
     ALB_TRY(bu(kBrBUFilt, (const void *)k_ms_bu<true, true, true>, true));
     ALB_TRY(bu(kBrBU, (const void *)k_ms_bu<true, true, false>, true));
@@ -1312,8 +1521,9 @@ alb_status build_ms_graph(alb_graph *g, MsScratch &m, MsArgs &a, int block) {
     ALB_TRY(bu(kBrBUNB, (const void *)k_ms_bu<false, false, false>, false));
     int dneg = -1;
     void *eargs[] = {&a, &dneg, &wh};
-    cudaGraphNode_t nend;
-    ALB_TRY(ms_add(body, &nend, &nswitch, MsNode{(void *)k_ms_end, 1, 32}, eargs));
+    cudaGraphNode_t nsample, nend;
+    ALB_TRY(ms_add(body, &nsample, &nswitch, res((const void *)k_ms_sample, kSampleBlock), aj));
+    ALB_TRY(ms_add(body, &nend, &nsample, MsNode{(void *)k_ms_end, 1, 32}, eargs));
     ALB_CK(cudaGraphInstantiate(&m.lexec, m.lg, 0));
     m.lblock = block;
     return ALB_OK;
@@ -1342,6 +1552,11 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
     in.n_live = g->n - s.zero_in;
     in.m_in = s.m_in;
     in.active0 = s.active0;
+    in.push_edges = s.m_in / kPushRootDiv;
+    if (const char *e = std::getenv("ALB_MS_PUSH_DIV")) {  // tuning: 0 turns the push off
+        const long long dv = std::atoll(e);
+        in.push_edges = dv > 0 ? s.m_in / dv : 0;
+    }
     const int32_t level_cap = (int32_t)std::min<int64_t>(g->n + 1, INT32_MAX - 1);
     in.level_cap = level_cap;
     const uint64_t unused = nroots >= 64 ? 0ull : ~((1ull << nroots) - 1);
@@ -1379,8 +1594,8 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
             if (h->done || !h->need_flush) break;
             ALB_TRY(flush());
         }
-        // per level: branch and end kernels plus the branch's step kernels
-        launches += (int64_t)h->levels_td * 8 + (int64_t)h->levels_bu * 6;
+        // per level: branch, sample and end kernels plus the branch's step kernels
+        launches += (int64_t)h->levels_td * 9 + (int64_t)h->levels_bu * 10;
     } else {
         ALB_CK(cudaMemcpyAsync(h, a.ctl, sizeof(MsCtl), cudaMemcpyDeviceToHost, stream));
         ALB_CK(cudaStreamSynchronize(stream));
@@ -1395,7 +1610,7 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
             prof->clear();
             ALB_TRY(dmalloc((void **)&snap.V, 8 * a.npad, "msbfs snapshot"));
             ALB_TRY(dmalloc((void **)&snap.D, 4 * a.nwords, "msbfs snapshot"));
-            ALB_TRY(dmalloc((void **)&snap.ctl, sizeof(MsCtl), "msbfs snapshot"));
+            ALB_TRY(dmalloc((void **)&snap.ctl, sizeof(MsCtl) + sizeof(MsSample), "msbfs snapshot"));
         }
         while (!h->done && h->level < level_cap) {
             const int L = h->level;
@@ -1425,8 +1640,8 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
                         launches++;
                     }
                     k_ms_zero_next<<<wide, block, 0, stream>>>(a, j);
-                    launch_resident(k_ms_td, block, g->num_sms, stream, a, j);
-                    launch_resident(k_ms_td_big, block, g->num_sms, stream, a, j);
+                    launch_resident(k_ms_td<false>, block, g->num_sms, stream, a, j);
+                    launch_resident(k_ms_td_big<false>, block, g->num_sms, stream, a, j);
                     k_ms_compact<<<wide, block, 0, stream>>>(a, 1);
                     launch_resident(k_ms_td_finish, block, g->num_sms, stream, a, j);
                     launches += 5;
@@ -1449,6 +1664,14 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
                     launch_resident(k_ms_bu_long_fin, block, g->num_sms, stream, a, j);
                     launches += 4;
                 }
+                if (d != ALB_DIR_TOPDOWN) {  // push of the roots in tmask
+                    k_ms_tq<<<wide, block, 0, stream>>>(a, j);
+                    launch_resident(k_ms_td<true>, block, g->num_sms, stream, a, j);
+                    launch_resident(k_ms_td_big<true>, block, g->num_sms, stream, a, j);
+                    launches += 3;
+                }
+                launch_resident(k_ms_sample, kSampleBlock, g->num_sms, stream, a, j);
+                launches++;
                 return ALB_OK;
             };
             if (prof) {
