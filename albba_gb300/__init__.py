@@ -77,11 +77,12 @@ class BfsOpts(C.Structure):
 
 class Stats(C.Structure):
     _fields_ = [("num_levels", C.c_int32), ("levels_topdown", C.c_int32),
-                ("levels_bottomup", C.c_int32), ("pad_", C.c_int32), ("reached", C.c_int64),
-                ("edges", C.c_int64), ("ms", C.c_double), ("kernels", C.c_int64)]
+                ("levels_bottomup", C.c_int32), ("pushed_roots", C.c_int32),
+                ("reached", C.c_int64), ("edges", C.c_int64), ("ms", C.c_double),
+                ("kernels", C.c_int64)]
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad_"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class LevelRec(C.Structure):

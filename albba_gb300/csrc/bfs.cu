@@ -1355,7 +1355,7 @@ alb_status bfs_impl(alb_graph *g, int32_t root, const alb_bfs_opts &o, int32_t *
         st->num_levels = c.level;
         st->levels_topdown = c.levels_td;
         st->levels_bottomup = c.levels_bu;
-        st->pad_ = 0;
+        st->pushed_roots = 0;
         st->reached = c.reached;
         st->edges = c.edges;
         st->ms = ms;

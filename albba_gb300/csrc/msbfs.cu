@@ -57,7 +57,10 @@ struct MsCtl {
     // Chosen by k_ms_end from per-root frontier counts sampled on every
     // kSampleStride-th bitmap word (MsSample, filled by k_ms_sample).
     unsigned long long tmask;
-    int64_t push_edges;  // a root joins tmask below this many estimated push edges
+    // budget of estimated push edges for all tmask roots together (0: off)
+    int64_t push_budget;
+    unsigned long long used;  // root bits in use
+    int32_t pushed_roots;     // sum of popc(tmask) over the levels
 };
 
 // Rows and push degrees of each root's sampled frontier. Kept beside the
@@ -69,8 +72,9 @@ struct MsSample {
 
 // Per-root frontier sampling: one bitmap word (32 rows) in kSampleStride.
 constexpr int kSampleStride = 32;
-// Default push budget per root: m_in / kPushRootDiv estimated edges.
-constexpr int kPushRootDiv = 1024;
+// Default push budget (all tmask roots together): m_in / kPushDiv estimated
+// push edges.
+constexpr int kPushDiv = 64;
 
 // Branches of the CUDA-graph level loop's switch node.
 enum MsBranch { kBrTD = 0, kBrBUFilt, kBrBU, kBrBUNBFilt, kBrBUNB, kBrCount };
@@ -103,6 +107,7 @@ struct MsArgs {
     int64_t *big_base;
     MsCtl *ctl;
     MsSample *smp;  // directly after *ctl
+    int32_t long_row;  // rows with more sources than this are the long rows
     const float *mlp;
 };
 
@@ -147,7 +152,7 @@ struct MsInit {
     int32_t roots[64];
     int32_t nroots, policy, level_cap;
     float alpha, beta, mean_deg, skew;
-    int64_t n_live, m_in, active0, push_edges;
+    int64_t n_live, m_in, active0, push_budget;
 };
 
 // One block of 64 threads: thread i seeds root i; thread 0 fills the control block.
@@ -211,7 +216,8 @@ __global__ void k_ms_roots(MsArgs a, MsInit in) {
         c.feat_skew = in.skew;
         c.m_in = in.m_in;
         c.level_cap = in.level_cap;
-        c.push_edges = in.push_edges;
+        c.push_budget = in.push_budget;
+        c.used = in.nroots >= 64 ? kAll : (1ull << in.nroots) - 1;
         c.done = c.nf == 0;
         // level 0's direction: the rule of later levels (the learned policy
         // falls back to Beamer here: no level has run yet)
@@ -443,6 +449,7 @@ __device__ __forceinline__ uint64_t ms_long_scan(const MsArgs &a, const uint64_t
 // Counters of the long rows folded in one level (per thread).
 struct MsLongCounts {
     unsigned long long cn = 0, cbits = 0, cmo = 0, cmi = 0, cfull = 0, cedges = 0, cdone = 0;
+    unsigned long long bytes = 0;  // algorithmic bytes, where the kernel counts them here
     __device__ void flush(const MsArgs &a, int k) {
         cn = warp_sum(cn);
         cbits = warp_sum(cbits);
@@ -451,6 +458,8 @@ struct MsLongCounts {
         cfull = warp_sum(cfull);
         cedges = warp_sum(cedges);
         cdone = warp_sum(cdone);
+        bytes = warp_sum(bytes);
+        if ((threadIdx.x & 31) == 0 && bytes) atomicAdd(&a.ctl->acc_bytes[k], bytes);
         if ((threadIdx.x & 31) == 0 && (cn | cbits | cdone)) {
             atomicAdd(&a.ctl->acc_n[k], cn);
             atomicAdd(&a.ctl->acc_bits[k], cbits);
@@ -684,6 +693,7 @@ __device__ __forceinline__ void ms_tpush(const MsArgs &a, uint64_t *N, uint32_t 
     nb &= ~oldv;
     if (!nb) return;
     const uint64_t oldn = atomicOr((unsigned long long *)N + v, (unsigned long long)nb);
+    c.bytes += 16;  // V and N words written
     const int pc = __popcll(nb);
     const int32_t od = __ldg(a.odeg + v);
     c.cbits += pc;
@@ -736,6 +746,7 @@ __global__ void k_ms_td(MsArgs a, int j) {
             st = __ldg(a.prow + u);
             d = __ldg(a.prow + u + 1) - st;
             f = __ldg(F + u) & tm;
+            if (kPush) cnt.bytes += 20;  // queue entry, row offsets, frontier word
             if (d > kBigRow) {  // pushed in chunks by all warps in k_ms_td_big
                 const unsigned long long nch = (unsigned long long)((d + kBigChunk - 1) / kBigChunk);
                 const unsigned long long old = atomicAdd(big_slot, (1ull << kMsBigShift) | nch);
@@ -757,9 +768,10 @@ __global__ void k_ms_td(MsArgs a, int j) {
             for (int step = 16; step > 0; step >>= 1)
                 if (s_ex[wib][jj + step] <= e) jj += step;
             const int32_t v = __ldg(a.pcol + s_st[wib][jj] + (e - s_ex[wib][jj]));
-            if (kPush)
+            if (kPush) {
+                cnt.bytes += 16;  // column, done bit, visited probe
                 ms_tpush(a, N, An, v, s_f[wib][jj], cnt);
-            else
+            } else
                 ms_push(a, N, An, v, s_f[wib][jj]);
         }
         __syncwarp();
@@ -815,9 +827,10 @@ __global__ void k_ms_td_big(MsArgs a, int j) {
         const int64_t c = k - base;
         const int64_t e1 = min(d, (c + 1) * kBigChunk);
         for (int64_t e = c * kBigChunk + lane; e < e1; e += 32) {
-            if (kPush)
+            if (kPush) {
+                cnt.bytes += 16;  // column, done bit, visited probe
                 ms_tpush(a, N, An, __ldg(a.pcol + st + e), f, cnt);
-            else
+            } else
                 ms_push(a, N, An, __ldg(a.pcol + st + e), f);
         }
     }
@@ -878,16 +891,25 @@ __global__ void k_ms_td_finish(MsArgs a, int j) {
     }
 }
 
-// Per-root size of the frontier level L produced (S[j+1]), sampled on every
-// kSampleStride-th bitmap word: warp per sampled word, lane i keeps roots i
-// and i + 32; rows and push degrees go to MsSample for k_ms_end.
+// Per-root size of the frontier level L produced (S[j+1]) for k_ms_end's
+// choice of pushed roots, in rows and push degrees (MsSample). The long rows
+// are counted exactly (they carry most of the degree in a skewed graph); the
+// others on one bitmap word in every kSampleStride, scaled by the stride. The
+// sampled word's offset inside its stride cycles with the stride index: rows
+// are sorted by length inside sigma windows, and a fixed offset would sample
+// one rank of length only. Warp per sampled word or per 32 long rows; lane i
+// keeps roots i and i + 32.
 constexpr int kSampleBlock = 256;
 
-__global__ void __launch_bounds__(kSampleBlock) k_ms_sample(MsArgs a, int j) {
+// dir: the direction level L ran (-1: the one in the control block).
+__global__ void __launch_bounds__(kSampleBlock) k_ms_sample(MsArgs a, int j, int dir) {
     __shared__ unsigned s_cnt[64];
     __shared__ unsigned long long s_deg[64];
     // the graph loop's pass after the last level: no next slot to read
     if (a.ctl->done) return;
+    // only a top-down level can be followed by a level with pushed roots
+    if (dir < 0) dir = a.ctl->dir;
+    if (a.ctl->push_budget <= 0 || dir != ALB_DIR_TOPDOWN) return;
     j = ms_j(a, j);
     const int L = a.ctl->level;
     const uint64_t *N = slot(a, j + 1);
@@ -899,33 +921,50 @@ __global__ void __launch_bounds__(kSampleBlock) k_ms_sample(MsArgs a, int j) {
     }
     __syncthreads();
     unsigned c0 = 0, c1 = 0;
-    unsigned long long d0 = 0, d1 = 0;
+    unsigned long long d0 = 0, d1 = 0, bytes = 0;
     const int64_t nsamp = (a.nwords + kSampleStride - 1) / kSampleStride;
+    const int64_t ntask = nsamp + (a.nlong + 31) / 32;
     const int64_t wpb = blockDim.x >> 5;
-    for (int64_t sidx = blockIdx.x * wpb + (threadIdx.x >> 5); sidx < nsamp;
-         sidx += (int64_t)gridDim.x * wpb) {
-        const int64_t w = sidx * kSampleStride;
-        uint32_t m = __ldg(An + w);
-        if (!m) continue;
-        const int64_t p = w * 32 + lane;
+    for (int64_t t = blockIdx.x * wpb + (threadIdx.x >> 5); t < ntask; t += (int64_t)gridDim.x * wpb) {
         uint64_t x = 0;
         int32_t od = 0;
-        if ((m >> lane) & 1u) {
-            x = __ldcg((const unsigned long long *)N + p);
-            od = __ldg(a.odeg + p);
+        unsigned wt;
+        if (t < nsamp) {
+            const int64_t w = min(t * kSampleStride + ((t * 13) & (kSampleStride - 1)), a.nwords - 1);
+            const uint32_t m = __ldg(An + w);
+            if (lane == 0) bytes += 4;
+            if (!m) continue;  // warp-uniform
+            const int64_t p = w * 32 + lane;
+            // long rows (long_row > 0) are counted below
+            if (((m >> lane) & 1u) && (a.long_row <= 0 || __ldg(a.ideg + p) <= a.long_row)) {
+                x = __ldcg((const unsigned long long *)N + p);
+                od = __ldg(a.odeg + p);
+                bytes += 16;  // length, frontier word, push degree
+            }
+            wt = kSampleStride;
+        } else {
+            const int64_t e = (t - nsamp) * 32 + lane;
+            if (e < a.nlong) {
+                const int32_t p = __ldg(a.lrow + e);
+                x = __ldcg((const unsigned long long *)N + p);
+                if (x) od = __ldg(a.odeg + p);
+                bytes += x ? 16 : 12;
+            }
+            wt = 1;
         }
+        unsigned m = __ballot_sync(kFull, x != 0);
         while (m) {
             const int q = __ffs(m) - 1;
             m &= m - 1;
             const uint64_t xq = __shfl_sync(kFull, x, q);
-            const int32_t oq = __shfl_sync(kFull, od, q);
+            const unsigned long long oq = (unsigned long long)(unsigned)__shfl_sync(kFull, od, q) * wt;
             if ((xq >> lane) & 1ull) {
-                c0++;
-                d0 += (unsigned)oq;
+                c0 += wt;
+                d0 += oq;
             }
             if ((xq >> (lane + 32)) & 1ull) {
-                c1++;
-                d1 += (unsigned)oq;
+                c1 += wt;
+                d1 += oq;
             }
         }
     }
@@ -937,6 +976,8 @@ __global__ void __launch_bounds__(kSampleBlock) k_ms_sample(MsArgs a, int j) {
         atomicAdd(&s_cnt[lane + 32], c1);
         atomicAdd(&s_deg[lane + 32], d1);
     }
+    bytes = warp_sum(bytes);
+    if (lane == 0 && bytes) atomicAdd(&a.ctl->acc_bytes[(L + 1) % 3], bytes);
     __syncthreads();
     if (threadIdx.x < 64 && s_cnt[threadIdx.x]) {
         atomicAdd(&a.smp->rows[threadIdx.x], s_cnt[threadIdx.x]);
@@ -959,10 +1000,12 @@ __global__ void k_ms_tq(MsArgs a, int j) {
     unsigned long long *qslot = &a.ctl->qn[(L + 1) % 3];
     const int lane = threadIdx.x & 31;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    unsigned long long bytes = 0;
     // warp-uniform bound: every lane reaches the ballots
     for (int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) & ~31ll; w0 < a.nwords;
          w0 += stride) {
         const uint32_t mine = w0 + lane < a.nwords ? __ldg(Az + w0 + lane) : 0u;
+        bytes += 4 + 8 * __popc(mine);  // bitmap word, the frontier words it selects
         unsigned words = __ballot_sync(kFull, mine != 0);
         while (words) {
             const int q = __ffs(words) - 1;
@@ -976,8 +1019,11 @@ __global__ void k_ms_tq(MsArgs a, int j) {
             if (lane == 0) base = atomicAdd(qslot, (unsigned long long)__popc(hm));
             base = __shfl_sync(kFull, base, 0);
             if (hit) Q[base + __popc(hm & ((1u << lane) - 1u))] = (int32_t)p;
+            if (lane == 0) bytes += 4 * __popc(hm);  // queue entries
         }
     }
+    bytes = warp_sum(bytes);
+    if (lane == 0 && bytes) atomicAdd(&a.ctl->acc_bytes[(L + 1) % 3], bytes);
 }
 
 __device__ inline void ms_feature_ctl(const MsCtl &m, BfsCtl &c) {
@@ -1061,19 +1107,51 @@ __global__ void k_ms_end(MsArgs a, int dir, cudaGraphConditionalHandle wh) {
     } else {
         next = rule_dir(fc);
     }
-    // roots pushed instead of pulled at a bottom-up level: those whose sampled
-    // frontier's push degree, scaled by the sampling stride, is within budget.
-    // The samples are cleared for the next level.
+    // Roots pushed instead of pulled, at the first bottom-up level after a
+    // top-down one (where the roots' frontiers differ most in size: some are
+    // still a few rows wide when most cover a good part of the graph): the
+    // roots with the smallest estimated push edges, in ascending order while
+    // their running sum stays within the budget. Later bottom-up levels pull
+    // every root. The samples are cleared for the next level.
     {
+        __shared__ unsigned long long s_val[64], s_cum[64];
         const int i = threadIdx.x;
-        const bool bu = next != ALB_DIR_TOPDOWN && !s.done && s.push_edges > 0;
-        const unsigned long long d0 = a.smp->deg[i], d1 = a.smp->deg[i + 32];
-        const unsigned long long lim = (unsigned long long)s.push_edges;
-        const unsigned lo = __ballot_sync(kFull, bu && d0 * kSampleStride < lim);
-        const unsigned hi = __ballot_sync(kFull, bu && d1 * kSampleStride < lim);
+        const int64_t budget = s.push_budget;
+        const bool bu = next != ALB_DIR_TOPDOWN && s.dir == ALB_DIR_TOPDOWN && !s.done && budget > 0;
+        const unsigned long long e0 = a.smp->deg[i], e1 = a.smp->deg[i + 32];
+        unsigned lo = 0, hi = 0;
+        if (bu) {
+            // rank of roots i and i + 32 by (estimate, root index)
+            int r0 = 0, r1 = 0;
+            for (int q = 0; q < 32; q++) {
+                const unsigned long long a0 = __shfl_sync(kFull, e0, q), a1 = __shfl_sync(kFull, e1, q);
+                r0 += (a0 < e0 || (a0 == e0 && q < i)) + (a1 < e0);
+                r1 += (a0 <= e1) + (a1 < e1 || (a1 == e1 && q < i));
+            }
+            s_val[r0] = e0;
+            s_val[r1] = e1;
+            __syncwarp();
+            // running sums in rank order: lane i holds ranks 2i and 2i + 1
+            const unsigned long long v0 = s_val[2 * i], v1 = s_val[2 * i + 1];
+            unsigned long long inc = v0 + v1;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned long long t = __shfl_up_sync(kFull, inc, o);
+                if (i >= o) inc += t;
+            }
+            s_cum[2 * i] = inc - v1;
+            s_cum[2 * i + 1] = inc;
+            __syncwarp();
+            const unsigned long long lim = (unsigned long long)budget;
+            lo = __ballot_sync(kFull, s_cum[r0] <= lim && ((s.used >> i) & 1ull));
+            hi = __ballot_sync(kFull, s_cum[r1] <= lim && ((s.used >> (i + 32)) & 1ull));
+        }
         a.smp->rows[i] = a.smp->rows[i + 32] = 0;
         a.smp->deg[i] = a.smp->deg[i + 32] = 0;
-        if (i == 0) s.tmask = (unsigned long long)lo | ((unsigned long long)hi << 32);
+        if (i == 0) {
+            s.tmask = (unsigned long long)lo | ((unsigned long long)hi << 32);
+            s.pushed_roots += __popcll(s.tmask);
+        }
         __syncwarp();
     }
     if (threadIdx.x == 0) {
@@ -1376,6 +1454,7 @@ MsArgs ms_args(alb_graph *g, MsScratch &m) {
     a.prow = s.prow;
     a.pcol = s.pcol;
     a.nlong = s.nlong;
+    a.long_row = s.long_row;
     a.lrow = s.lrow;
     a.lptr = s.lptr;
     a.lcol = s.lcol;
@@ -1522,7 +1601,8 @@ alb_status build_ms_graph(alb_graph *g, MsScratch &m, MsArgs &a, int block) {
     int dneg = -1;
     void *eargs[] = {&a, &dneg, &wh};
     cudaGraphNode_t nsample, nend;
-    ALB_TRY(ms_add(body, &nsample, &nswitch, res((const void *)k_ms_sample, kSampleBlock), aj));
+    void *sargs[] = {&a, &jneg, &dneg};
+    ALB_TRY(ms_add(body, &nsample, &nswitch, res((const void *)k_ms_sample, kSampleBlock), sargs));
     ALB_TRY(ms_add(body, &nend, &nsample, MsNode{(void *)k_ms_end, 1, 32}, eargs));
     ALB_CK(cudaGraphInstantiate(&m.lexec, m.lg, 0));
     m.lblock = block;
@@ -1552,10 +1632,10 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
     in.n_live = g->n - s.zero_in;
     in.m_in = s.m_in;
     in.active0 = s.active0;
-    in.push_edges = s.m_in / kPushRootDiv;
+    in.push_budget = s.m_in / kPushDiv;
     if (const char *e = std::getenv("ALB_MS_PUSH_DIV")) {  // tuning: 0 turns the push off
         const long long dv = std::atoll(e);
-        in.push_edges = dv > 0 ? s.m_in / dv : 0;
+        in.push_budget = dv > 0 ? s.m_in / dv : 0;
     }
     const int32_t level_cap = (int32_t)std::min<int64_t>(g->n + 1, INT32_MAX - 1);
     in.level_cap = level_cap;
@@ -1670,7 +1750,7 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
                     launch_resident(k_ms_td_big<true>, block, g->num_sms, stream, a, j);
                     launches += 3;
                 }
-                launch_resident(k_ms_sample, kSampleBlock, g->num_sms, stream, a, j);
+                launch_resident(k_ms_sample, kSampleBlock, g->num_sms, stream, a, j, d);
                 launches++;
                 return ALB_OK;
             };
@@ -1757,7 +1837,7 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
         st->num_levels = h->level;
         st->levels_topdown = h->levels_td;
         st->levels_bottomup = h->levels_bu;
-        st->pad_ = 0;
+        st->pushed_roots = h->pushed_roots;
         st->reached = h->pairs;
         st->edges = h->edges;
         st->ms = ms;

@@ -304,9 +304,10 @@ def run_ours(args, rank: int, world: int, dist) -> None:
 def roofline(dg, roots, d_ms, policy, levels=None) -> dict:
     """Dominant kernel of the batched step: the bottom-up level of the 64-root
     BFS (k_ms_bu over the slices, then the long-row head/tail passes and their
-    fold-in). Bytes are counted by the kernels themselves (the model in
-    include/albba.h); time is CUDA events around the level's launches on the
-    graph's stream, from the host-driven trace run with the bench's policy."""
+    fold-in, the push of the pushed roots and the frontier sampling). Bytes
+    are counted by the kernels themselves (the model in include/albba.h); time
+    is CUDA events around the level's launches on the graph's stream, from the
+    host-driven trace run with the bench's policy."""
     import albba_gb300 as ab
     peak, kind = peaks()
     byts, us, nlev = 0, 0.0, 0
@@ -323,6 +324,7 @@ def roofline(dg, roots, d_ms, policy, levels=None) -> dict:
     gbs = byts / us / 1e3 if us > 0 else 0.0
     return {"bound": "hbm",
             "kernel": "k_ms_bu + k_ms_bu_long + k_ms_bu_long_tail + k_ms_bu_long_fin "
+                      "+ k_ms_tq + k_ms_td<push> + k_ms_td_big<push> + k_ms_sample "
                       "(64-root bottom-up level)",
             "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
             "peak_kind": f"{kind} HBM copy bandwidth (burst)",

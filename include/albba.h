@@ -149,7 +149,8 @@ typedef struct {
     int32_t num_levels;   /* non-empty levels (the reference's num_iter) */
     int32_t levels_topdown;
     int32_t levels_bottomup;
-    int32_t pad_;
+    int32_t pushed_roots; /* 64-root batched BFS: roots pushed instead of pulled
+                             at a bottom-up level (0 for the other forms) */
     int64_t reached;      /* vertices reached (the reference's num_vex) */
     int64_t edges;        /* stored push-side entries of reached vertices */
     double ms;            /* device time of the traversal, SELL build excluded */
@@ -189,7 +190,11 @@ typedef struct {
  * counts the same way with 8-byte frontier and visited words: 8 per row
  * pulled, 48 per 4-column group (32 + 8 per frontier word fetched when the
  * nonzero bitmap is consulted), 12 per row reached, 8*npad + 8*nwords for the
- * next-frontier, done and nonzero-bitmap words. */
+ * next-frontier, done and nonzero-bitmap words; a bottom-up level's push of
+ * its pushed roots adds 4 per bitmap word + 8 per frontier row + 4 per queued
+ * row (queue build), 20 per queued row, 16 per edge, 16 per new claim, and
+ * the per-root frontier sampling that precedes it 4 per sampled word + 16 per
+ * sampled row + 12 to 16 per long row. */
 
 /* Per-level records of the last traversal on g (requires opts.trace). */
 alb_status alb_level_trace(const alb_graph *g, int32_t cap, alb_level_rec *out,

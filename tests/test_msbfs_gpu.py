@@ -100,3 +100,23 @@ def test_bad_roots_rejected(rmat16_dev):
     assert ei.value.code == ab.ERR_INVALID
     with pytest.raises(ab.AlbError):
         dg.msbfs64(np.zeros(65, np.int32))
+
+
+@pytest.mark.parametrize("loop", ["graph", "host"])
+def test_pushed_roots_exact(rmat16_dev, monkeypatch, loop):
+    # roots with small frontiers are pushed at the first bottom-up level; a
+    # budget of every stored entry (ALB_MS_PUSH_DIV=1) pushes many of them,
+    # 0 turns the push off: the levels are the oracle's either way
+    g, roots, dg = rmat16_dev
+    monkeypatch.setenv("ALB_MS_PUSH_DIV", "1")
+    _, st = check(g, dg, roots, ab.bfs_opts("beamer", loop))
+    assert st.levels_bottomup > 0
+    # popc(tmask) summed over the levels that follow a top-down level
+    assert 0 < st.pushed_roots <= len(roots) * st.levels_bottomup
+    monkeypatch.setenv("ALB_MS_PUSH_DIV", "0")
+    _, st = check(g, dg, roots, ab.bfs_opts("beamer", loop))
+    assert st.pushed_roots == 0
+    # a smaller root set: only the roots in use are pushed
+    monkeypatch.setenv("ALB_MS_PUSH_DIV", "1")
+    _, st = check(g, dg, roots[:7], ab.bfs_opts("beamer", loop))
+    assert st.pushed_roots <= 7 * st.levels_bottomup
