@@ -125,22 +125,45 @@ __device__ void prep_phase(const BfsArgs &a, int L, bool compact, bool zero_next
     }
 }
 
-// One pushed edge u -> v (u's original id ou): the smallest source wins the
+// Pushed edges u -> v (u's original id ou): the smallest source wins the
 // parent, and v's bit goes into the next-frontier bitmap N (the next queue,
 // levels and counters are made from N by td_finish_phase, so no counter is
 // shared by every claim).
-__device__ __forceinline__ void push_edge(const BfsArgs &a, uint32_t *N, int32_t v, uint32_t ou,
-                                          bool persist) {
-    const uint32_t bit = 1u << (v & 31);
-    const uint32_t w = persist ? __ldcg(a.vis + (v >> 5)) : __ldg(a.vis + (v >> 5));
-    if (w & bit) return;
+// Four edges per lane (v[k] < 0: none): the visited words of all four are
+// requested together, then the parent and bitmap words of the unvisited
+// targets together, then the atomics, so one lane keeps four loads in
+// flight where one edge at a time kept one.
+__device__ __forceinline__ void push_edges4(const BfsArgs &a, uint32_t *N, const int32_t (&v)[4],
+                                            const uint32_t (&ou)[4], bool persist) {
+    bool live[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        live[k] = false;
+        if (v[k] >= 0) {
+            const uint32_t w = persist ? __ldcg(a.vis + (v[k] >> 5)) : __ldg(a.vis + (v[k] >> 5));
+            live[k] = !((w >> (v[k] & 31)) & 1u);
+        }
+    }
     // read before writing: a hub target receives thousands of pushes in one
     // level, and atomics on one address serialise in L2, so the atomics are
     // issued only when they can still change something
-    const uint32_t cur_parent = __ldcg(a.parent_pos + v);
-    const uint32_t cur_n = __ldcg(N + (v >> 5));
-    if (ou < cur_parent) atomicMin(a.parent_pos + v, ou);
-    if (!(cur_n & bit)) atomicOr(N + (v >> 5), bit);
+    uint32_t cur_parent[4], cur_n[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        cur_parent[k] = 0;
+        cur_n[k] = ~0u;
+        if (live[k]) {
+            cur_parent[k] = __ldcg(a.parent_pos + v[k]);
+            cur_n[k] = __ldcg(N + (v[k] >> 5));
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        if (!live[k]) continue;
+        const uint32_t bit = 1u << (v[k] & 31);
+        if (ou[k] < cur_parent[k]) atomicMin(a.parent_pos + v[k], ou[k]);
+        if (!(cur_n[k] & bit)) atomicOr(N + (v[k] >> 5), bit);
+    }
 }
 
 // Rows per warp for the short-row pass: as many frontier rows as keep every
@@ -196,13 +219,24 @@ __device__ void td_phase(const BfsArgs &a, int L, Range r) {
         s_st[wib][lane] = st;
         s_ou[wib][lane] = ou;
         __syncwarp();
-        for (int64_t e = lane; e < T; e += 32) {
-            int j = 0;
+        for (int64_t e0 = lane; e0 < T; e0 += 128) {
+            int32_t v[4];
+            uint32_t ou4[4];
 #pragma unroll
-            for (int step = 16; step > 0; step >>= 1)
-                if (s_ex[wib][j + step] <= e) j += step;
-            push_edge(a, N, __ldg(a.pcol + s_st[wib][j] + (e - s_ex[wib][j])),
-                      (uint32_t)s_ou[wib][j], kPersist);
+            for (int k = 0; k < 4; k++) {
+                const int64_t e = e0 + 32 * k;
+                v[k] = -1;
+                ou4[k] = 0;
+                if (e < T) {
+                    int j = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1)
+                        if (s_ex[wib][j + step] <= e) j += step;
+                    v[k] = __ldg(a.pcol + s_st[wib][j] + (e - s_ex[wib][j]));
+                    ou4[k] = (uint32_t)s_ou[wib][j];
+                }
+            }
+            push_edges4(a, N, v, ou4, kPersist);
         }
         __syncwarp();
     }
@@ -249,8 +283,16 @@ __device__ void td_big_phase(const BfsArgs &a, int L, Range r) {
         }
         const int64_t c = k - base;
         const int64_t e1 = min(d, (c + 1) * kBigChunk);
-        for (int64_t e = c * kBigChunk + lane; e < e1; e += 32)
-            push_edge(a, N, __ldg(a.pcol + st + e), ou, kPersist);
+        static_assert(kBigChunk == 128, "four edges per lane per chunk");
+        int32_t v[4];
+        uint32_t ou4[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int64_t e = c * kBigChunk + 32 * q + lane;
+            v[q] = e < e1 ? __ldg(a.pcol + st + e) : -1;
+            ou4[q] = ou;
+        }
+        push_edges4(a, N, v, ou4, kPersist);
     }
 }
 

@@ -72,16 +72,21 @@ struct MsSample {
 
 // Per-root frontier sampling: one bitmap word (32 rows) in kSampleStride.
 constexpr int kSampleStride = 32;
+constexpr int kSampleMinDiv = 1024;
 // Default push budget (all tmask roots together): m_in / kPushDiv estimated
 // push edges.
 constexpr int kPushDiv = 64;
 
 // Branches of the CUDA-graph level loop's switch node.
-enum MsBranch { kBrTD = 0, kBrBUFilt, kBrBU, kBrBUNBFilt, kBrBUNB, kBrCount };
+// kBrBUWide: the unfiltered pull two column groups at a time, at the first
+// bottom-up level after a top-down one (prev_td), where rows scan longest
+// before every root is accounted for; at later levels rows stop sooner and
+// the second group is mostly fetched for nothing.
+enum MsBranch { kBrTD = 0, kBrBUFilt, kBrBU, kBrBUWide, kBrBUNBFilt, kBrBUNB, kBrCount };
 
-__host__ __device__ inline int ms_branch_of(int dir, int filt) {
+__host__ __device__ inline int ms_branch_of(int dir, int filt, bool prev_td) {
     if (dir == ALB_DIR_TOPDOWN) return kBrTD;
-    if (dir == ALB_DIR_BOTTOMUP) return filt ? kBrBUFilt : kBrBU;
+    if (dir == ALB_DIR_BOTTOMUP) return filt ? kBrBUFilt : (prev_td ? kBrBUWide : kBrBU);
     return filt ? kBrBUNBFilt : kBrBUNB;
 }
 
@@ -127,24 +132,23 @@ __device__ __forceinline__ int ms_filt(const MsArgs &a, int filt) {
     return filt >= 0 ? filt : a.ctl->filt;
 }
 
+// Initial state, thread per position: a warp covers one bitmap word (npad and
+// the grid stride are multiples of 32), so the done word comes from a ballot.
 __global__ void k_ms_init(MsArgs a, uint64_t unused) {
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t str = (int64_t)gridDim.x * blockDim.x;
     uint64_t *S0 = a.S;
     for (int64_t p = tid; p < a.npad; p += str) {
-        const bool live = p < a.n && a.ideg[p] > 0;
+        const bool live = p < a.n && __ldg(a.ideg + p) > 0;
         a.V[p] = live ? unused : kAll;
         S0[p] = 0;
-    }
-    for (int64_t w = tid; w < a.nwords; w += str) {
-        uint32_t d = 0;
-        for (int b = 0; b < 32; b++) {
-            const int64_t p = w * 32 + b;
-            if (!(p < a.n && a.ideg[p] > 0)) d |= 1u << b;
+        const unsigned dead = __ballot_sync(kFull, !live);
+        if ((threadIdx.x & 31) == 0) {
+            const int64_t w = p >> 5;
+            a.D[w] = dead;
+            a.A[w] = 0;
+            a.A[a.nwords + w] = 0;
         }
-        a.D[w] = d;
-        a.A[w] = 0;
-        a.A[a.nwords + w] = 0;
     }
 }
 
@@ -235,7 +239,7 @@ __global__ void k_ms_roots(MsArgs a, MsInit in) {
         fc.beta = in.beta;
         c.dir = rule_dir(fc);
         c.filt = c.mf < c.m_in / 8;
-        c.branch = ms_branch_of(c.dir, c.filt);
+        c.branch = ms_branch_of(c.dir, c.filt, false);
         *a.ctl = c;
     }
 }
@@ -250,8 +254,10 @@ __global__ void k_ms_roots(MsArgs a, MsInit in) {
 // (5 blocks, 40 warps per SM) without spills.
 constexpr int kMsBuBlock = 256;
 
-template <bool kBypass, bool kEarly, bool kFilt>
-__global__ void __launch_bounds__(kMsBuBlock, 5) k_ms_bu(MsArgs a, int j) {
+// kWide (with !kFilt): two column groups per step, eight frontier fetches in
+// flight per lane, at four blocks per SM.
+template <bool kBypass, bool kEarly, bool kFilt, bool kWide = false>
+__global__ void __launch_bounds__(kMsBuBlock, kWide ? 4 : 5) k_ms_bu(MsArgs a, int j) {
     j = ms_j(a, j);
     const uint64_t *F = slot(a, j);
     uint64_t *N = slot(a, j + 1);
@@ -310,12 +316,34 @@ __global__ void __launch_bounds__(kMsBuBlock, 5) k_ms_bu(MsArgs a, int j) {
             // roots in tmask are found by the push over their frontier
             const uint64_t visx = vis | tm;
             bool active = visx != kAll;
-            const int32_t ng = active ? (wd_c + 3) >> 2 : 0;
+            int32_t ng = active ? (wd_c + 3) >> 2 : 0;
             const int4 *cp = a.col4 + (so_c >> 2) + (p & (a.C - 1));
             uint64_t acc = 0;
             // group g+1 is requested before group g's frontier fetches, so each
             // lane keeps a column load in flight while it waits on the gathers
             const int32_t pp = (int32_t)p;
+            if (kWide && !kFilt) {
+                const int4 pad = make_int4(pp, pp, pp, pp);
+                int4 c0 = pad, c1 = pad;
+                if (active && ng > 0) c0 = ld_stream(cp, pol);
+                if (active && ng > 1) c1 = ld_stream(cp + a.C, pol);
+                for (int32_t g = 0;; g += 2) {
+                    active = active && g < ng;
+                    if (!__any_sync(kFull, active)) break;
+                    if (!active) continue;
+                    int4 n0 = pad, n1 = pad;
+                    if (g + 2 < ng) n0 = ld_stream(cp + (int64_t)(g + 2) * a.C, pol);
+                    if (g + 3 < ng) n1 = ld_stream(cp + (int64_t)(g + 3) * a.C, pol);
+                    // past the row's last group c1 is padding (p itself)
+                    acc |= __ldg(F + c0.x) | __ldg(F + c0.y) | __ldg(F + c0.z) | __ldg(F + c0.w) |
+                           __ldg(F + c1.x) | __ldg(F + c1.y) | __ldg(F + c1.z) | __ldg(F + c1.w);
+                    bytes += g + 1 < ng ? 96 : 48;
+                    if (kEarly && (c1.w == pp || (acc | visx) == kAll)) active = false;
+                    c0 = n0;
+                    c1 = n1;
+                }
+                ng = 0;  // the single-group loop below has nothing left
+            }
             int4 c = make_int4(pp, pp, pp, pp);
             if (active && ng > 0) c = ld_stream(cp, pol);
             for (int32_t g = 0;; g++) {
@@ -660,35 +688,15 @@ __global__ void k_ms_compact(MsArgs a, int ahead) {
     }
 }
 
-// One pushed edge: the roots f reaching v this level. Only two small words
-// are read per edge: v's done bit (D, 1 bit per row, stays in L2) and N[v]
-// (so that the many pushes into a hub stop issuing atomics once its word
-// holds their bits); f is ORed in without masking by V[v], and
-// k_ms_td_finish removes the roots that had already visited v. A push that
-// finds N[v] empty marks v in the next nonzero bitmap An (setting a bit is
-// idempotent, so racing pushers need no claim); the next queue is compacted
-// from An afterwards.
-__device__ __forceinline__ void ms_push(const MsArgs &a, uint64_t *N, uint32_t *An, int32_t v,
-                                        uint64_t f) {
-    const uint32_t dw = __ldg(a.D + (v >> 5));
-    const uint64_t cur = __ldcg((const unsigned long long *)N + v);
-    if ((dw >> (v & 31)) & 1u) return;  // every root has visited v
-    if (!(f & ~cur)) return;            // nothing new
-    atomicOr((unsigned long long *)N + v, (unsigned long long)f);
-    if (!cur) atomicOr(An + (v >> 5), 1u << (v & 31));
-}
-
-
-// Push of the roots in tmask during a bottom-up level (after the pull): one
-// edge u -> v carrying the roots f. The new roots are claimed on V[v] itself
-// (atomicOr), so concurrent pushers and the pull's own discoveries are never
-// counted twice, and the level's state and counters are updated in place.
-__device__ __forceinline__ void ms_tpush(const MsArgs &a, uint64_t *N, uint32_t *An, int32_t v,
-                                         uint64_t f, MsLongCounts &c) {
-    const uint32_t bit = 1u << (v & 31);
-    if (__ldg(a.D + (v >> 5)) & bit) return;  // visited by every root before this level
-    uint64_t nb = f & ~__ldcg((const unsigned long long *)a.V + v);
+// Push of the roots in tmask during a bottom-up level (after the pull): the
+// roots nb reach v (nb: the edge's roots not in v's visited word as read).
+// The new roots are claimed on V[v] itself (atomicOr), so concurrent pushers
+// and the pull's own discoveries are never counted twice, and the level's
+// state and counters are updated in place.
+__device__ __forceinline__ void ms_tclaim(const MsArgs &a, uint64_t *N, uint32_t *An, int32_t v,
+                                          uint64_t nb, MsLongCounts &c) {
     if (!nb) return;
+    const uint32_t bit = 1u << (v & 31);
     const uint64_t oldv = atomicOr((unsigned long long *)a.V + v, (unsigned long long)nb);
     nb &= ~oldv;
     if (!nb) return;
@@ -708,6 +716,46 @@ __device__ __forceinline__ void ms_tpush(const MsArgs &a, uint64_t *N, uint32_t 
         c.cmi += __ldg(a.ideg + v);
         const uint32_t od2 = atomicOr(a.D + (v >> 5), bit);
         c.cfull += (od2 != kFull && (od2 | bit) == kFull);
+    }
+}
+
+// Four pushed edges per lane (v[k] < 0: none), roots f[k] reaching v[k]
+// this level: the done words and the target words of all four are requested
+// before the first atomic, so one lane keeps eight loads in flight instead
+// of two. Top-down (kPush false): only two small words are read per edge,
+// v's done bit (D, 1 bit per row, stays in L2) and N[v] (so that the many
+// pushes into a hub stop issuing atomics once its word holds their bits); f
+// is ORed in without masking by V[v], and k_ms_td_finish removes the roots
+// that had already visited v. A push that finds N[v] empty marks v in the
+// next nonzero bitmap An (setting a bit is idempotent, so racing pushers need
+// no claim); the next queue is compacted from An afterwards. kPush: the push
+// of the tmask roots, ms_tclaim against V (D can change during that kernel
+// and is read through L2).
+template <bool kPush>
+__device__ __forceinline__ void ms_push4(const MsArgs &a, uint64_t *N, uint32_t *An,
+                                         const int32_t (&v)[4], const uint64_t (&f)[4],
+                                         MsLongCounts &c) {
+    uint32_t dw[4];
+    uint64_t cur[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        dw[k] = kFull;
+        cur[k] = 0;
+        if (v[k] >= 0) {
+            dw[k] = kPush ? __ldcg(a.D + (v[k] >> 5)) : __ldg(a.D + (v[k] >> 5));
+            cur[k] = __ldcg((const unsigned long long *)(kPush ? a.V : N) + v[k]);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        if (v[k] < 0 || ((dw[k] >> (v[k] & 31)) & 1u)) continue;  // every root has visited v
+        if (kPush) {
+            c.bytes += 16;  // column, done bit, visited probe
+            ms_tclaim(a, N, An, v[k], f[k] & ~cur[k], c);
+        } else if (f[k] & ~cur[k]) {
+            atomicOr((unsigned long long *)N + v[k], (unsigned long long)f[k]);
+            if (!cur[k]) atomicOr(An + (v[k] >> 5), 1u << (v[k] & 31));
+        }
     }
 }
 
@@ -762,17 +810,24 @@ __global__ void k_ms_td(MsArgs a, int j) {
         s_st[wib][lane] = st;
         s_f[wib][lane] = f;
         __syncwarp();
-        for (int64_t e = lane; e < T; e += 32) {
-            int jj = 0;
+        for (int64_t e0 = lane; e0 < T; e0 += 128) {
+            int32_t v[4];
+            uint64_t ff[4];
 #pragma unroll
-            for (int step = 16; step > 0; step >>= 1)
-                if (s_ex[wib][jj + step] <= e) jj += step;
-            const int32_t v = __ldg(a.pcol + s_st[wib][jj] + (e - s_ex[wib][jj]));
-            if (kPush) {
-                cnt.bytes += 16;  // column, done bit, visited probe
-                ms_tpush(a, N, An, v, s_f[wib][jj], cnt);
-            } else
-                ms_push(a, N, An, v, s_f[wib][jj]);
+            for (int k = 0; k < 4; k++) {
+                const int64_t e = e0 + 32 * k;
+                v[k] = -1;
+                ff[k] = 0;
+                if (e < T) {
+                    int jj = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1)
+                        if (s_ex[wib][jj + step] <= e) jj += step;
+                    v[k] = __ldg(a.pcol + s_st[wib][jj] + (e - s_ex[wib][jj]));
+                    ff[k] = s_f[wib][jj];
+                }
+            }
+            ms_push4<kPush>(a, N, An, v, ff, cnt);
         }
         __syncwarp();
     }
@@ -826,13 +881,16 @@ __global__ void k_ms_td_big(MsArgs a, int j) {
         }
         const int64_t c = k - base;
         const int64_t e1 = min(d, (c + 1) * kBigChunk);
-        for (int64_t e = c * kBigChunk + lane; e < e1; e += 32) {
-            if (kPush) {
-                cnt.bytes += 16;  // column, done bit, visited probe
-                ms_tpush(a, N, An, __ldg(a.pcol + st + e), f, cnt);
-            } else
-                ms_push(a, N, An, __ldg(a.pcol + st + e), f);
+        static_assert(kBigChunk == 128, "four edges per lane per chunk");
+        int32_t v[4];
+        uint64_t ff[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int64_t e = c * kBigChunk + 32 * q + lane;
+            v[q] = e < e1 ? __ldg(a.pcol + st + e) : -1;
+            ff[q] = f;
         }
+        ms_push4<kPush>(a, N, An, v, ff, cnt);
     }
     if (kPush) cnt.flush(a, (L + 1) % 3);
 }
@@ -910,6 +968,11 @@ __global__ void __launch_bounds__(kSampleBlock) k_ms_sample(MsArgs a, int j, int
     // only a top-down level can be followed by a level with pushed roots
     if (dir < 0) dir = a.ctl->dir;
     if (a.ctl->push_budget <= 0 || dir != ALB_DIR_TOPDOWN) return;
+    // a frontier under n / kSampleMinDiv rows is not sampled: every root's
+    // estimate stays 0, and a bottom-up level after it pushes all of them
+    // (a push over so few rows is cheaper than any pull)
+    const int L0 = a.ctl->level;
+    if ((int64_t)a.ctl->acc_n[(L0 + 1) % 3] * kSampleMinDiv < a.n) return;
     j = ms_j(a, j);
     const int L = a.ctl->level;
     const uint64_t *N = slot(a, j + 1);
@@ -1158,7 +1221,7 @@ __global__ void k_ms_end(MsArgs a, int dir, cudaGraphConditionalHandle wh) {
         s.dir = next;
         // nonzero-bitmap filter when under 1/8 of all entries point into the frontier
         s.filt = s.mf < s.m_in / 8;
-        s.branch = ms_branch_of(next, s.filt);
+        s.branch = ms_branch_of(next, s.filt, s.prev_dir == ALB_DIR_TOPDOWN);
         s.need_flush = !s.done && (s.level - s.base + 1 >= a.K);
         *a.ctl = s;
         if (wh) cudaGraphSetConditional(wh, (s.done || s.need_flush) ? 0u : 1u);
@@ -1596,6 +1659,7 @@ alb_status build_ms_graph(alb_graph *g, MsScratch &m, MsArgs &a, int block) {
                    {res((const void *)k_ms_td_finish, block), aj}}));
     ALB_TRY(bu(kBrBUFilt, (const void *)k_ms_bu<true, true, true>, true));
     ALB_TRY(bu(kBrBU, (const void *)k_ms_bu<true, true, false>, true));
+    ALB_TRY(bu(kBrBUWide, (const void *)k_ms_bu<true, true, false, true>, true));
     ALB_TRY(bu(kBrBUNBFilt, (const void *)k_ms_bu<false, false, true>, false));
     ALB_TRY(bu(kBrBUNB, (const void *)k_ms_bu<false, false, false>, false));
     int dneg = -1;
@@ -1713,6 +1777,8 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
             const bool q_valid = h->q_valid != 0;
             // nonzero-bitmap filter when under 1/8 of all entries point into the frontier
             const int filt = (h->mf < s.m_in / 8) ? 1 : 0;
+            // the first bottom-up level after a top-down one pulls two groups at a time
+            const bool wide = h->prev_dir == ALB_DIR_TOPDOWN;
             auto launch_step = [&](int d) -> alb_status {
                 if (d == ALB_DIR_TOPDOWN) {
                     if (!q_valid) {
@@ -1728,6 +1794,8 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
                 } else if (d == ALB_DIR_BOTTOMUP) {
                     if (filt)
                         launch_resident(k_ms_bu<true, true, true>, kMsBuBlock, g->num_sms, stream, a, j);
+                    else if (wide)
+                        launch_resident(k_ms_bu<true, true, false, true>, kMsBuBlock, g->num_sms, stream, a, j);
                     else
                         launch_resident(k_ms_bu<true, true, false>, kMsBuBlock, g->num_sms, stream, a, j);
                     launch_resident(k_ms_bu_long<true>, block, g->num_sms, stream, a, j, filt);
