@@ -244,6 +244,68 @@ __global__ void k_ms_roots(MsArgs a, MsInit in) {
     }
 }
 
+// Words of a bottom-up level in runs of kGrabWords from the level's counter
+// (dynamic distribution, as WordRuns). The done words of a run are loaded
+// together, one per lane, a run ahead of use. kSkip: words whose rows are all
+// done are not yielded; their next-frontier words and nonzero bits are
+// cleared when the run comes up, one coalesced store per word, so a warp
+// does not walk them one dependent round trip at a time (at late levels most
+// words are such). Call from all lanes of a warp.
+template <bool kSkip>
+struct MsWords {
+    int64_t cur, nxt;     // first word of the current run and of the next one
+    uint32_t dcur, dnxt;  // lane l < kGrabWords: done word of word cur + l / nxt + l
+    unsigned left;        // words of the current run not yet yielded
+    __device__ __forceinline__ uint32_t load(const MsArgs &a, int64_t r) const {
+        const int l = threadIdx.x & 31;
+        return (l < kGrabWords && r + l < a.nwords) ? __ldg(a.D + r + l) : kFull;
+    }
+    __device__ __forceinline__ unsigned prep(const MsArgs &a, uint64_t *N, uint32_t *An) const {
+        const int l = threadIdx.x & 31;
+        const bool valid = l < kGrabWords && cur + l < a.nwords;
+        const unsigned all = __ballot_sync(kFull, valid);
+        if (!kSkip) return all;
+        unsigned full = __ballot_sync(kFull, valid && dcur == kFull);
+        while (full) {
+            const int q = __ffs(full) - 1;
+            full &= full - 1;
+            N[(cur + q) * 32 + l] = 0;
+            if (l == 0) An[cur + q] = 0;
+        }
+        return __ballot_sync(kFull, valid && dcur != kFull);
+    }
+    __device__ __forceinline__ void start(const MsArgs &a, uint64_t *N, uint32_t *An,
+                                          unsigned long long *ctr) {
+        cur = grab_words(ctr);
+        nxt = grab_words(ctr);
+        dcur = load(a, cur);
+        dnxt = load(a, nxt);
+        left = prep(a, N, An);
+    }
+    // the next word (a.nwords when the level's words are exhausted) and its
+    // done word
+    __device__ __forceinline__ int64_t next(const MsArgs &a, uint64_t *N, uint32_t *An,
+                                            unsigned long long *ctr, uint32_t &d) {
+        while (!left) {
+            if (cur >= a.nwords) {
+                d = kFull;
+                return a.nwords;
+            }
+            cur = nxt;
+            dcur = dnxt;
+            if (cur < a.nwords) {
+                nxt = grab_words(ctr);
+                dnxt = load(a, nxt);
+            }
+            left = prep(a, N, An);
+        }
+        const int q = __ffs(left) - 1;
+        left &= left - 1;
+        d = __shfl_sync(kFull, dcur, q);
+        return cur + q;
+    }
+};
+
 // Bottom-up over S[j] -> S[j+1]. kBypass: skip words whose 32 positions are
 // done; kEarly: stop a row once every root is accounted for, or at padding.
 // kFilt: test the nonzero bitmap before each 8-byte frontier fetch. It pays
@@ -271,12 +333,13 @@ __global__ void __launch_bounds__(kMsBuBlock, kWide ? 4 : 5) k_ms_bu(MsArgs a, i
     unsigned cn = 0, cbits = 0, cfull = 0, cdone = 0;
     unsigned long long cmo = 0, cmi = 0, cedges = 0, bytes = 0;
     const uint64_t pol = l2_evict_first();
-    // words come in runs from the level's counter. Software pipeline over
-    // words: the done mask is requested two words ahead and the visited words
-    // and slice geometry one word ahead, so their latency overlaps the
-    // current word's column loads and gathers.
+    // words come in runs from the level's counter (MsWords, done words
+    // skipped when kBypass). Software pipeline over words: the visited words
+    // and slice geometry are requested one word ahead, so their latency
+    // overlaps the current word's column loads and gathers.
     unsigned long long *ctr = &a.ctl->work[L % 3];
-    WordRuns runs;
+    MsWords<kBypass> it;
+    it.start(a, N, An, ctr);
     auto geometry = [&](int64_t ww, uint32_t dd, uint64_t &vv, int32_t &wdv, int64_t &sov) {
         vv = kAll;
         wdv = 0;
@@ -291,23 +354,20 @@ __global__ void __launch_bounds__(kMsBuBlock, kWide ? 4 : 5) k_ms_bu(MsArgs a, i
             sov = __ldg(a.slice_off + sw);
         }
     };
-    int64_t w = runs.first(ctr, a.nwords);
-    int64_t w1 = w < a.nwords ? runs.after(w, ctr, a.nwords) : a.nwords;
-    uint32_t d = w < a.nwords ? __ldg(a.D + w) : kFull;
-    uint32_t d1 = w1 < a.nwords ? __ldg(a.D + w1) : kFull;
+    uint32_t d, d1 = kFull;
+    int64_t w = it.next(a, N, An, ctr, d);
+    int64_t w1 = w < a.nwords ? it.next(a, N, An, ctr, d1) : a.nwords;
     uint64_t vis_c;
     int32_t wd_c;
     int64_t so_c;
     geometry(w, d, vis_c, wd_c, so_c);
     while (w < a.nwords) {
-        const int64_t w2 = w1 < a.nwords ? runs.after(w1, ctr, a.nwords) : a.nwords;
-        const uint32_t d2 = w2 < a.nwords ? __ldg(a.D + w2) : kFull;
         uint64_t vis1;
         int32_t wd1;
         int64_t so1;
         geometry(w1, d1, vis1, wd1, so1);
         const int64_t p = w * 32 + lane;
-        if (kBypass && d == kFull) {
+        if (kBypass && d == kFull) {  // not reached: MsWords clears these words
             N[p] = 0;
             if (lane == 0) An[w] = 0;
         } else {
@@ -404,8 +464,7 @@ __global__ void __launch_bounds__(kMsBuBlock, kWide ? 4 : 5) k_ms_bu(MsArgs a, i
         vis_c = vis1;
         wd_c = wd1;
         so_c = so1;
-        w1 = w2;
-        d1 = d2;
+        w1 = w1 < a.nwords ? it.next(a, N, An, ctr, d1) : a.nwords;
     }
     cn = warp_sum(cn);
     cbits = warp_sum(cbits);
@@ -1778,7 +1837,7 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
             // nonzero-bitmap filter when under 1/8 of all entries point into the frontier
             const int filt = (h->mf < s.m_in / 8) ? 1 : 0;
             // the first bottom-up level after a top-down one pulls two groups at a time
-            const bool wide = h->prev_dir == ALB_DIR_TOPDOWN;
+            const bool two_groups = h->prev_dir == ALB_DIR_TOPDOWN;
             auto launch_step = [&](int d) -> alb_status {
                 if (d == ALB_DIR_TOPDOWN) {
                     if (!q_valid) {
@@ -1794,7 +1853,7 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
                 } else if (d == ALB_DIR_BOTTOMUP) {
                     if (filt)
                         launch_resident(k_ms_bu<true, true, true>, kMsBuBlock, g->num_sms, stream, a, j);
-                    else if (wide)
+                    else if (two_groups)
                         launch_resident(k_ms_bu<true, true, false, true>, kMsBuBlock, g->num_sms, stream, a, j);
                     else
                         launch_resident(k_ms_bu<true, true, false>, kMsBuBlock, g->num_sms, stream, a, j);
