@@ -338,7 +338,7 @@ class Graph:
         """Run on a caller stream (e.g. torch.cuda.current_stream().cuda_stream)."""
         check(_lib.alb_graph_set_stream(self._h, cuda_stream))
 
-    def sell_build(self, C_: int = 32, sigma: int = 1024, long_row: int = 256) -> float:
+    def sell_build(self, C_: int = 32, sigma: int = 1024, long_row: int = 1024) -> float:
         """Build SELL-C-sigma on the device; returns the build time in ms."""
         o = SellOpts(C_, sigma, long_row)
         ms = C.c_double()

@@ -23,7 +23,7 @@ import albba_gb300 as ab
 CACHE = Path(__file__).resolve().parent / "tuning" / "cache.json"
 GRID = {"C": [8, 16, 32, 64], "sigma": [1, 64, 1024, 16384], "block": [128, 256, 512],
         "alpha": [8.0, 14.0, 24.0], "beta": [12.0, 24.0, 48.0], "long_row": [128, 256, 1024]}
-DEFAULT = {"C": 32, "sigma": 1024, "long_row": 256, "block": 256, "alpha": 14.0, "beta": 24.0}
+DEFAULT = {"C": 32, "sigma": 1024, "long_row": 1024, "block": 256, "alpha": 14.0, "beta": 24.0}
 
 
 def shape_class(csr: ab.Csr) -> str:

@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--edgefactor", type=int, default=16)
     p.add_argument("--roots", type=int, default=64)
     p.add_argument("--sigma", type=int, default=1024)
+    p.add_argument("--long-row", type=int, default=1024,
+                   help="rows with more sources are pulled warp-cooperatively, outside the slices")
     p.add_argument("--cpu-roots", type=int, default=1, help="roots timed for the CPU baseline")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-roofline", action="store_true")
@@ -142,6 +144,7 @@ def config(args, g, extra=None):
     c = {"workload": f"RMAT scale {args.scale} edgefactor {args.edgefactor}, {args.roots} roots "
                      "(BFS from every root per step)",
          "n": g.n, "stored_entries": g.nnz, "roots": args.roots, "C": 32, "sigma": args.sigma,
+         "long_row": args.long_row,
          "graph_seed": SEED_GRAPH, "root_seed": SEED_ROOTS,
          "l2": "inputs larger than L2 (graph > 1 GB vs 129 MB L2); no flush"}
     if extra:
@@ -233,7 +236,7 @@ def run_ours(args, rank: int, world: int, dist) -> None:
     stream = torch.cuda.current_stream()
     dg = ab.Graph(g, flags=ab.CSR_SYMMETRIC | ab.CSR_SORTED)
     dg.set_stream(stream.cuda_stream)
-    build_ms = dg.sell_build(32, args.sigma)
+    build_ms = dg.sell_build(32, args.sigma, args.long_row)
     n = g.n
     d_lv = torch.empty(n, dtype=torch.int32, device="cuda")
     d_pa = torch.empty(n, dtype=torch.int32, device="cuda")
@@ -372,7 +375,7 @@ def e2e_batched(args, g, roots, ab, torch, opts) -> dict:
 
     def step():
         with ab.Graph(hg, flags=ab.CSR_SYMMETRIC | ab.CSR_SORTED) as dg:
-            dg.sell_build(32, args.sigma)
+            dg.sell_build(32, args.sigma, args.long_row)
             st = ab.check(ab.lib().alb_msbfs64(dg.handle, roots.ctypes.data, len(roots),
                                                 ab.C.byref(opts), levels.ctypes.data,
                                                 ab.C.byref(ab.Stats())))

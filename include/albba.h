@@ -88,7 +88,7 @@ typedef struct {
     int32_t C;        /* slice height: 8, 16, 32 (default) or 64 */
     int32_t sigma;    /* sort window in rows: 1 .. 16384 (default 1024) */
     int32_t long_row; /* rows longer than this are kept out of the slices and
-                         pulled by a whole warp each (default 256; <= 0: none) */
+                         pulled by a whole warp each (default 1024; <= 0: none) */
 } alb_sell_opts;
 
 void alb_sell_opts_default(alb_sell_opts *o);
