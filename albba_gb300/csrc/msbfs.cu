@@ -57,6 +57,7 @@ struct MsCtl {
     // Chosen by k_ms_end from per-root frontier counts sampled on every
     // kSampleStride-th bitmap word (MsSample, filled by k_ms_sample).
     unsigned long long tmask;
+    int32_t grab;  // words per run of the bottom-up pull (8 .. 32)
     // budget of estimated push edges for all tmask roots together (0: off)
     int64_t push_budget;
     unsigned long long used;  // root bits in use
@@ -157,6 +158,7 @@ struct MsInit {
     int32_t nroots, policy, level_cap;
     float alpha, beta, mean_deg, skew;
     int64_t n_live, m_in, active0, push_budget;
+    int32_t grab;
 };
 
 // One block of 64 threads: thread i seeds root i; thread 0 fills the control block.
@@ -221,6 +223,7 @@ __global__ void k_ms_roots(MsArgs a, MsInit in) {
         c.m_in = in.m_in;
         c.level_cap = in.level_cap;
         c.push_budget = in.push_budget;
+        c.grab = in.grab;
         c.used = in.nroots >= 64 ? kAll : (1ull << in.nroots) - 1;
         c.done = c.nf == 0;
         // level 0's direction: the rule of later levels (the learned policy
@@ -251,18 +254,25 @@ __global__ void k_ms_roots(MsArgs a, MsInit in) {
 // cleared when the run comes up, one coalesced store per word, so a warp
 // does not walk them one dependent round trip at a time (at late levels most
 // words are such). Call from all lanes of a warp.
+__device__ __forceinline__ int64_t grab_n(unsigned long long *ctr, int step) {
+    unsigned long long v = 0;
+    if ((threadIdx.x & 31) == 0) v = atomicAdd(ctr, (unsigned long long)step);
+    return (int64_t)__shfl_sync(kFull, v, 0);
+}
+
 template <bool kSkip>
 struct MsWords {
     int64_t cur, nxt;     // first word of the current run and of the next one
     uint32_t dcur, dnxt;  // lane l < kGrabWords: done word of word cur + l / nxt + l
     unsigned left;        // words of the current run not yet yielded
+    int step;             // words per run (<= 32)
     __device__ __forceinline__ uint32_t load(const MsArgs &a, int64_t r) const {
         const int l = threadIdx.x & 31;
-        return (l < kGrabWords && r + l < a.nwords) ? __ldg(a.D + r + l) : kFull;
+        return (l < step && r + l < a.nwords) ? __ldg(a.D + r + l) : kFull;
     }
     __device__ __forceinline__ unsigned prep(const MsArgs &a, uint64_t *N, uint32_t *An) const {
         const int l = threadIdx.x & 31;
-        const bool valid = l < kGrabWords && cur + l < a.nwords;
+        const bool valid = l < step && cur + l < a.nwords;
         const unsigned all = __ballot_sync(kFull, valid);
         if (!kSkip) return all;
         unsigned full = __ballot_sync(kFull, valid && dcur == kFull);
@@ -276,8 +286,9 @@ struct MsWords {
     }
     __device__ __forceinline__ void start(const MsArgs &a, uint64_t *N, uint32_t *An,
                                           unsigned long long *ctr) {
-        cur = grab_words(ctr);
-        nxt = grab_words(ctr);
+        step = a.ctl->grab;
+        cur = grab_n(ctr, step);
+        nxt = grab_n(ctr, step);
         dcur = load(a, cur);
         dnxt = load(a, nxt);
         left = prep(a, N, An);
@@ -294,7 +305,7 @@ struct MsWords {
             cur = nxt;
             dcur = dnxt;
             if (cur < a.nwords) {
-                nxt = grab_words(ctr);
+                nxt = grab_n(ctr, step);
                 dnxt = load(a, nxt);
             }
             left = prep(a, N, An);
@@ -1756,6 +1767,14 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
     in.m_in = s.m_in;
     in.active0 = s.active0;
     in.push_budget = s.m_in / kPushDiv;
+    {
+        // words per run of the pull: about three runs per resident warp, 8 .. 32
+        // (RMAT s22: 8 beats 32 by 7 %; s24: 32 beats 8 by 2 %, where longer runs
+        // save counter round trips and still leave every warp busy)
+        const int per = resident_blocks((const void *)k_ms_bu<true, true, false>, kMsBuBlock);
+        const int64_t warps = (int64_t)std::max(per, 1) * (kMsBuBlock / 32) * g->num_sms;
+        in.grab = (int32_t)std::max<int64_t>(kGrabWords, std::min<int64_t>(32, s.nwords / (3 * warps)));
+    }
     if (const char *e = std::getenv("ALB_MS_PUSH_DIV")) {  // tuning: 0 turns the push off
         const long long dv = std::atoll(e);
         in.push_budget = dv > 0 ? s.m_in / dv : 0;
