@@ -276,7 +276,7 @@ def run_ours(args, rank: int, world: int, dist) -> None:
     plain = world * pedges / pms / 1e6
     hm = len(per_root) / sum(m / (e / 1e6) for e, m in per_root if e > 0) if per_root else None
 
-    roof = None if args.no_roofline else roofline(dg, roots, d_ms, policy)
+    roof = None if args.no_roofline else roofline(dg, roots, d_ms, policy, profiled_traffic(args))
     roof_plain = None if args.no_roofline else roofline_plain(dg, roots[:8])
     e2e = None if args.no_e2e else e2e_batched(args, g, roots, ab, torch, bopts)
     cpu = cpu_baseline(g, roots, args.cpu_roots) if rank == 0 and args.cpu_roots > 0 else None
@@ -304,7 +304,25 @@ def run_ours(args, rank: int, world: int, dist) -> None:
     emit(line, args)
 
 
-def roofline(dg, roots, d_ms, policy, levels=None) -> dict:
+# DRAM traffic per bottom-up level from the committed ncu summary, which was
+# captured on this workload (RMAT s24 ef16, 64 roots, C 32, sigma 1024,
+# long_row 1024); other workloads report null.
+TRAFFIC_PROFILE = Path(__file__).resolve().parent / "profiles" / "k_ms_bu_rmat22_rmat24.md"
+
+
+def profiled_traffic(args):
+    if (args.scale, args.edgefactor, args.roots, args.sigma, args.long_row) != (24, 16, 64, 1024, 1024):
+        return None
+    try:
+        for line in TRAFFIC_PROFILE.read_text().splitlines():
+            if line.startswith("roofline.traffic:"):
+                return int(line.split(":", 1)[1])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
+def roofline(dg, roots, d_ms, policy, traffic=None) -> dict:
     """Dominant kernel of the batched step: the bottom-up level of the 64-root
     BFS (k_ms_bu over the slices, then the long-row head/tail passes and their
     fold-in, the push of the pushed roots and the frontier sampling). Bytes
@@ -332,7 +350,10 @@ def roofline(dg, roots, d_ms, policy, levels=None) -> dict:
             "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
             "peak_kind": f"{kind} HBM copy bandwidth (burst)",
             "bytes_per_launch": byts / max(nlev, 1), "us_per_launch": us / max(nlev, 1),
-            "launches": nlev, "levels": per_level, "traffic": None}
+            "launches": nlev, "levels": per_level, "traffic": traffic,
+            "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum over all launches "
+                               "of the step's bottom-up levels, per level "
+                               "(profiles/k_ms_bu_rmat22_rmat24.md)") if traffic else None}
 
 
 def roofline_plain(dg, roots) -> dict:
