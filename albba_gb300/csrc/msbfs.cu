@@ -1183,12 +1183,21 @@ __device__ inline void ms_feature_ctl(const MsCtl &m, BfsCtl &c) {
 // as in the CUDA-graph loop). wh: the graph loop's while condition (0 when
 // the host drives the loop), cleared when the traversal is done or the
 // snapshot store must be flushed before the next level.
+static_assert(sizeof(MsCtl) % 8 == 0, "the control block is copied in 8-byte words");
+
 __global__ void k_ms_end(MsArgs a, int dir, cudaGraphConditionalHandle wh) {
     if (threadIdx.x >= 32) return;
     __shared__ MsCtl s;
     __shared__ int s_skip;
+    // the control block moves between global and shared memory with all 32
+    // lanes (8-byte words), not one thread's serial copy
+    constexpr int kCtlWords = (int)(sizeof(MsCtl) / 8);
+    for (int w = threadIdx.x; w < kCtlWords; w += 32)
+        reinterpret_cast<unsigned long long *>(&s)[w] =
+            reinterpret_cast<const unsigned long long *>(a.ctl)[w];
+    __syncwarp();
     if (threadIdx.x == 0) {
-        MsCtl c = *a.ctl;
+        MsCtl &c = s;
         s_skip = c.done;  // the graph loop's first pass when nothing is left to do
         if (!c.done) {
             if (dir < 0) dir = c.dir;
@@ -1222,10 +1231,9 @@ __global__ void k_ms_end(MsArgs a, int dir, cudaGraphConditionalHandle wh) {
             c.nbig[c.level % 3] = 0;
             if (!c.q_valid) c.qn[c.level % 3] = 0;
         }
-        s = c;
     }
     __syncwarp();
-    if (s_skip) {
+    if (s_skip) {  // nothing changed: no write-back
         if (threadIdx.x == 0 && wh) cudaGraphSetConditional(wh, 0);
         return;
     }
@@ -1293,9 +1301,12 @@ __global__ void k_ms_end(MsArgs a, int dir, cudaGraphConditionalHandle wh) {
         s.filt = s.mf < s.m_in / 8;
         s.branch = ms_branch_of(next, s.filt, s.prev_dir == ALB_DIR_TOPDOWN);
         s.need_flush = !s.done && (s.level - s.base + 1 >= a.K);
-        *a.ctl = s;
-        if (wh) cudaGraphSetConditional(wh, (s.done || s.need_flush) ? 0u : 1u);
     }
+    __syncwarp();
+    for (int w = threadIdx.x; w < kCtlWords; w += 32)
+        reinterpret_cast<unsigned long long *>(a.ctl)[w] =
+            reinterpret_cast<const unsigned long long *>(&s)[w];
+    if (threadIdx.x == 0 && wh) cudaGraphSetConditional(wh, (s.done || s.need_flush) ? 0u : 1u);
 }
 
 // Graph loop: the level's branch (none once done).
