@@ -120,3 +120,28 @@ def test_pushed_roots_exact(rmat16_dev, monkeypatch, loop):
     monkeypatch.setenv("ALB_MS_PUSH_DIV", "1")
     _, st = check(g, dg, roots[:7], ab.bfs_opts("beamer", loop))
     assert st.pushed_roots <= 7 * st.levels_bottomup
+
+
+def test_full_scale_against_single_root():
+    # RMAT s23: large enough that the pull hands out runs of more than 8
+    # words, the pushed roots are chosen from sampled frontiers and the long
+    # rows are many; every root's levels equal the single-root BFS (itself
+    # oracle-exact at every size tested), and two roots are checked against
+    # the oracle directly
+    import torch
+    g = ab.gen_rmat(23, 16, seed=31)
+    roots = g.pick_roots(64, seed=5)
+    with ab.Graph(g, flags=ab.CSR_SYMMETRIC | ab.CSR_SORTED) as dg:
+        dg.sell_build()
+        d = torch.empty((g.n, 64), dtype=torch.int32, device="cuda")
+        st = dg.msbfs64_device(roots, d, ab.bfs_opts("beamer"))
+        torch.cuda.synchronize()
+        assert st.pushed_roots > 0
+        d_lv = torch.empty(g.n, dtype=torch.int32, device="cuda")
+        for i, r in enumerate(roots):
+            dg.bfs_device(int(r), d_lv, None, ab.bfs_opts("beamer"))
+            torch.cuda.synchronize()
+            assert torch.equal(d[:, i], d_lv), f"root {r}"
+        out = d.cpu().numpy()
+    for i in (0, 37):
+        assert np.array_equal(out[:, i], oracle.bfs(g.rowptr, g.col, int(roots[i]))[0])
