@@ -354,58 +354,83 @@ __global__ void k_widths(int64_t n, int64_t nslices, int32_t C, int32_t long_row
     ssize[s] = (int64_t)C * ((w + 3) & ~3);
 }
 
-// Fill the 4-interleaved SELL columns, one warp per (padded) row: lanes
-// stride over the CSR row, a ballot prefix drops self-loops in order.
+// Fill the 4-interleaved SELL columns, one thread per (padded) row, so that
+// a warp keeps 32 rows' loads in flight instead of one row's: each thread
+// reads its CSR row four entries at a time (the four column loads, then the
+// four inv gathers, each group independent of the next), drops self-loops,
+// and writes every group of four kept entries as one int4; the C rows of a
+// slice write group g as C contiguous int4 (coalesced). The slice is padded
+// with the row's own position up to its width.
 __global__ void k_fill_sell(int64_t n, int64_t npad, int32_t C, int32_t log2C, int32_t long_row,
                             const int32_t *perm, const int32_t *inv, const int32_t *ideg,
                             const int32_t *width, const int64_t *slice_off, const int64_t *rp,
                             const int32_t *col, int32_t *scol) {
-    const int lane = threadIdx.x & 31;
-    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t p = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); p < npad;
-         p += nw) {
+    const int64_t str = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npad; p += str) {
         const int64_t s = p >> log2C;
         const int32_t r = (int32_t)(p & (C - 1));
-        const int32_t w4 = (width[s] + 3) & ~3;
-        int32_t *base = scol + slice_off[s] + r * 4;
-        int32_t k = 0;
+        const int32_t ng = (width[s] + 3) >> 2;
+        // slice_off is a multiple of 4 (every slice holds C * w4 entries)
+        int4 *base = reinterpret_cast<int4 *>(scol + slice_off[s]) + r;
+        const int32_t pad = p < n ? (int32_t)p : 0;
+        int32_t g = 0, nb = 0;
+        int4 cur = make_int4(pad, pad, pad, pad);
+        auto put = [&](int32_t x) {
+            if (nb == 0) cur.x = x;
+            else if (nb == 1) cur.y = x;
+            else if (nb == 2) cur.z = x;
+            else cur.w = x;
+            if (++nb == 4) {
+                base[(int64_t)g * C] = cur;
+                g++;
+                nb = 0;
+                cur = make_int4(pad, pad, pad, pad);
+            }
+        };
         if (p < n && !is_long(ideg[p], long_row)) {
             const int32_t v = perm[p];
             const int64_t b = rp[v], e = rp[v + 1];
-            for (int64_t i = b + lane; i - lane < e; i += 32) {
-                const int32_t c = i < e ? col[i] : v;
-                const bool keep = c != v;
-                const unsigned m = __ballot_sync(kFull, keep);
-                if (keep) {
-                    const int32_t kk = k + __popc(m & lanemask_lt());
-                    base[(int64_t)(kk >> 2) * 4 * C + (kk & 3)] = inv[c];
-                }
-                k += __popc(m);
+            for (int64_t i = b; i < e; i += 4) {
+                int32_t c[4], q[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) c[k] = i + k < e ? __ldg(col + i + k) : v;
+#pragma unroll
+                for (int k = 0; k < 4; k++) q[k] = c[k] != v ? __ldg(inv + c[k]) : 0;
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    if (c[k] != v) put(q[k]);
             }
         }
-        const int32_t pad = p < n ? (int32_t)p : 0;
-        for (int32_t kk = k + lane; kk < w4; kk += 32) base[(int64_t)(kk >> 2) * 4 * C + (kk & 3)] = pad;
+        if (nb > 0) {  // the last partial group, padded
+            base[(int64_t)g * C] = cur;
+            g++;
+        }
+        const int4 pads = make_int4(pad, pad, pad, pad);
+        for (; g < ng; g++) base[(int64_t)g * C] = pads;
     }
 }
 
-// Push-side CSR in position space, one warp per row.
-// Rows with more than kFillChunk raw entries are left to k_fill_chunks.
+// Push-side CSR in position space, one thread per row (as k_fill_sell: four
+// column loads, then four inv gathers, per step). Rows with more than
+// kFillChunk raw entries are left to k_fill_chunks.
 __global__ void k_fill_push(int64_t n, const int32_t *perm, const int32_t *inv,
                             const int64_t *prow, const int64_t *rp, const int32_t *col,
                             int32_t *pcol) {
-    const int lane = threadIdx.x & 31;
-    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t p = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); p < n; p += nw) {
+    const int64_t str = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += str) {
         const int32_t v = perm[p];
         int64_t at = prow[p];
         const int64_t b = rp[v], e = rp[v + 1];
         if (e - b > kFillChunk) continue;
-        for (int64_t i = b + lane; i - lane < e; i += 32) {
-            const int32_t c = i < e ? col[i] : v;
-            const bool keep = c != v;
-            const unsigned m = __ballot_sync(kFull, keep);
-            if (keep) pcol[at + __popc(m & lanemask_lt())] = inv[c];
-            at += __popc(m);
+        for (int64_t i = b; i < e; i += 4) {
+            int32_t c[4], q[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) c[k] = i + k < e ? __ldg(col + i + k) : v;
+#pragma unroll
+            for (int k = 0; k < 4; k++) q[k] = c[k] != v ? __ldg(inv + c[k]) : 0;
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                if (c[k] != v) pcol[at++] = q[k];
         }
     }
 }
