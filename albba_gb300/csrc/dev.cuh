@@ -43,6 +43,12 @@ __device__ __forceinline__ uint64_t l2_evict_first() {
     asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
     return p;
 }
+// One 4-byte read-only load with an L2 policy (L1 allocation left as usual).
+__device__ __forceinline__ int32_t ld_hint(const int32_t *ptr, uint64_t pol) {
+    int32_t r;
+    asm volatile("ld.global.nc.L2::cache_hint.s32 %0, [%1], %2;" : "=r"(r) : "l"(ptr), "l"(pol));
+    return r;
+}
 __device__ __forceinline__ int4 ld_stream(const int4 *ptr, uint64_t pol) {
     int4 r;
     asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.s32 {%0,%1,%2,%3}, [%4], %5;"

@@ -360,12 +360,15 @@ __global__ void k_widths(int64_t n, int64_t nslices, int32_t C, int32_t long_row
 // four inv gathers, each group independent of the next), drops self-loops,
 // and writes every group of four kept entries as one int4; the C rows of a
 // slice write group g as C contiguous int4 (coalesced). The slice is padded
-// with the row's own position up to its width.
+// with the row's own position up to its width. The CSR columns are read once
+// (L2 evict-first) and the slices written with streaming stores, so that inv,
+// gathered at random, keeps its lines in L2.
 __global__ void k_fill_sell(int64_t n, int64_t npad, int32_t C, int32_t log2C, int32_t long_row,
                             const int32_t *perm, const int32_t *inv, const int32_t *ideg,
                             const int32_t *width, const int64_t *slice_off, const int64_t *rp,
                             const int32_t *col, int32_t *scol) {
     const int64_t str = (int64_t)gridDim.x * blockDim.x;
+    const uint64_t pstream = l2_evict_first();
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npad; p += str) {
         const int64_t s = p >> log2C;
         const int32_t r = (int32_t)(p & (C - 1));
@@ -381,7 +384,7 @@ __global__ void k_fill_sell(int64_t n, int64_t npad, int32_t C, int32_t log2C, i
             else if (nb == 2) cur.z = x;
             else cur.w = x;
             if (++nb == 4) {
-                base[(int64_t)g * C] = cur;
+                __stcs(base + (int64_t)g * C, cur);
                 g++;
                 nb = 0;
                 cur = make_int4(pad, pad, pad, pad);
@@ -393,7 +396,7 @@ __global__ void k_fill_sell(int64_t n, int64_t npad, int32_t C, int32_t log2C, i
             for (int64_t i = b; i < e; i += 4) {
                 int32_t c[4], q[4];
 #pragma unroll
-                for (int k = 0; k < 4; k++) c[k] = i + k < e ? __ldg(col + i + k) : v;
+                for (int k = 0; k < 4; k++) c[k] = i + k < e ? ld_hint(col + i + k, pstream) : v;
 #pragma unroll
                 for (int k = 0; k < 4; k++) q[k] = c[k] != v ? __ldg(inv + c[k]) : 0;
 #pragma unroll
@@ -402,21 +405,23 @@ __global__ void k_fill_sell(int64_t n, int64_t npad, int32_t C, int32_t log2C, i
             }
         }
         if (nb > 0) {  // the last partial group, padded
-            base[(int64_t)g * C] = cur;
+            __stcs(base + (int64_t)g * C, cur);
             g++;
         }
         const int4 pads = make_int4(pad, pad, pad, pad);
-        for (; g < ng; g++) base[(int64_t)g * C] = pads;
+        for (; g < ng; g++) __stcs(base + (int64_t)g * C, pads);
     }
 }
 
 // Push-side CSR in position space, one thread per row (as k_fill_sell: four
-// column loads, then four inv gathers, per step). Rows with more than
+// column loads, then four inv gathers, per step, with the same L2
+// policies). Rows with more than
 // kFillChunk raw entries are left to k_fill_chunks.
 __global__ void k_fill_push(int64_t n, const int32_t *perm, const int32_t *inv,
                             const int64_t *prow, const int64_t *rp, const int32_t *col,
                             int32_t *pcol) {
     const int64_t str = (int64_t)gridDim.x * blockDim.x;
+    const uint64_t pstream = l2_evict_first();
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += str) {
         const int32_t v = perm[p];
         int64_t at = prow[p];
@@ -425,12 +430,12 @@ __global__ void k_fill_push(int64_t n, const int32_t *perm, const int32_t *inv,
         for (int64_t i = b; i < e; i += 4) {
             int32_t c[4], q[4];
 #pragma unroll
-            for (int k = 0; k < 4; k++) c[k] = i + k < e ? __ldg(col + i + k) : v;
+            for (int k = 0; k < 4; k++) c[k] = i + k < e ? ld_hint(col + i + k, pstream) : v;
 #pragma unroll
             for (int k = 0; k < 4; k++) q[k] = c[k] != v ? __ldg(inv + c[k]) : 0;
 #pragma unroll
             for (int k = 0; k < 4; k++)
-                if (c[k] != v) pcol[at++] = q[k];
+                if (c[k] != v) __stcs(pcol + at++, q[k]);
         }
     }
 }
@@ -513,6 +518,7 @@ __global__ void k_fill_chunks(int64_t nchunks, const int32_t *crow, const int32_
                               int32_t *out) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const uint64_t pstream = l2_evict_first();
     for (int64_t k = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); k < nchunks;
          k += nw) {
         const int32_t i = crow[k];
@@ -524,8 +530,8 @@ __global__ void k_fill_chunks(int64_t nchunks, const int32_t *crow, const int32_
         const int64_t lo = slo[i], hi = shi[i];
         const int64_t o = by_pos ? obase[p] : obase[i];
         for (int64_t j = s0 + lane; j < s1; j += 32) {
-            const int32_t c = col[j];
-            if (c != v) out[o + (j - b) - (min(max(j, lo), hi) - lo)] = inv[c];
+            const int32_t c = ld_hint(col + j, pstream);
+            if (c != v) __stcs(out + o + (j - b) - (min(max(j, lo), hi) - lo), __ldg(inv + c));
         }
     }
 }
