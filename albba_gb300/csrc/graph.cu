@@ -31,24 +31,56 @@
 
 namespace alb {
 
+// Device buffers come from the device's default memory pool, which keeps
+// freed memory (release threshold: unlimited) instead of returning it to the
+// driver: the gigabytes of a graph's CSR, SELL and traversal state are
+// reused by the next graph built in the process without new driver
+// allocations, and a destroy does not wait on driver frees.
+namespace {
+void keep_pool_memory() {
+    static std::mutex mu;
+    static bool done[256] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return;
+    std::lock_guard<std::mutex> lk(mu);
+    if (done[dev]) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    cudaGetLastError();
+    done[dev] = true;
+}
+}  // namespace
+
 alb_status dmalloc(void **p, size_t bytes, const char *what) {
     *p = nullptr;
     if (injected_alloc_failure())
         return fail(ALB_ERR_OOM, "device allocation of %zu bytes for %s failed (injected)", bytes,
                     what);
-    cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+    keep_pool_memory();
+    // allocated in the legacy stream's order, then waited for, so that the
+    // buffer can be used from any stream at once
+    cudaError_t e = cudaMallocAsync(p, bytes ? bytes : 16, 0);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
     if (e != cudaSuccess) {
         cudaGetLastError();
         *p = nullptr;
         if (e == cudaErrorMemoryAllocation)
             return fail(ALB_ERR_OOM, "device allocation of %zu bytes for %s failed", bytes, what);
-        return fail(ALB_ERR_CUDA, "cudaMalloc for %s: %s", what, cudaGetErrorString(e));
+        return fail(ALB_ERR_CUDA, "cudaMallocAsync for %s: %s", what, cudaGetErrorString(e));
     }
     return ALB_OK;
 }
 
 void dfree(void *p) {
-    if (p) cudaFree(p);
+    if (!p) return;
+    // work on any stream may still use the buffer (cudaFree waited for the
+    // device too); it then goes back to the pool
+    cudaDeviceSynchronize();
+    cudaFreeAsync(p, 0);
+    cudaStreamSynchronize(0);
 }
 
 int resident_blocks(const void *func, int block) {
