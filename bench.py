@@ -304,22 +304,26 @@ def run_ours(args, rank: int, world: int, dist) -> None:
     emit(line, args)
 
 
-# DRAM traffic per bottom-up level from the committed ncu summary, which was
-# captured on this workload (RMAT s24 ef16, 64 roots, C 32, sigma 1024,
+# DRAM traffic of each bottom-up level from the committed ncu summary, which
+# was captured on this workload (RMAT s24 ef16, 64 roots, C 32, sigma 1024,
 # long_row 1024); other workloads report null.
 TRAFFIC_PROFILE = Path(__file__).resolve().parent / "profiles" / "k_ms_bu_rmat22_rmat24.md"
 
 
 def profiled_traffic(args):
+    """Per-level DRAM bytes {level: bytes} from the committed ncu summary of
+    this workload, or None for other workloads."""
     if (args.scale, args.edgefactor, args.roots, args.sigma, args.long_row) != (24, 16, 64, 1024, 1024):
         return None
+    out = {}
     try:
         for line in TRAFFIC_PROFILE.read_text().splitlines():
-            if line.startswith("roofline.traffic:"):
-                return int(line.split(":", 1)[1])
+            if line.startswith("roofline.traffic.level"):
+                key, val = line[len("roofline.traffic.level"):].split(":", 1)
+                out[int(key)] = int(val)
     except (OSError, ValueError):
-        pass
-    return None
+        return None
+    return out or None
 
 
 def roofline(dg, roots, d_ms, policy, traffic=None) -> dict:
@@ -343,6 +347,9 @@ def roofline(dg, roots, d_ms, policy, traffic=None) -> dict:
             per_level.append({"level": t.level, "bytes": t.bytes, "us": round(t.step_us, 1),
                               "gbs": round(t.bytes / t.step_us / 1e3, 1)})
     gbs = byts / us / 1e3 if us > 0 else 0.0
+    lv = [x["level"] for x in per_level]
+    traffic = (sum(traffic[L] for L in lv) / len(lv)
+               if traffic and lv and all(L in traffic for L in lv) else None)
     return {"bound": "hbm",
             "kernel": "k_ms_bu + k_ms_bu_long + k_ms_bu_long_tail + k_ms_bu_long_fin "
                       "+ k_ms_tq + k_ms_td<push> + k_ms_td_big<push> + k_ms_sample "
@@ -352,7 +359,7 @@ def roofline(dg, roots, d_ms, policy, traffic=None) -> dict:
             "bytes_per_launch": byts / max(nlev, 1), "us_per_launch": us / max(nlev, 1),
             "launches": nlev, "levels": per_level, "traffic": traffic,
             "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum over all launches "
-                               "of the step's bottom-up levels, per level "
+                               "of each bottom-up level this run took, averaged per level "
                                "(profiles/k_ms_bu_rmat22_rmat24.md)") if traffic else None}
 
 
