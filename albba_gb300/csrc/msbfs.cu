@@ -247,13 +247,14 @@ __global__ void k_ms_roots(MsArgs a, MsInit in) {
     }
 }
 
-// Words of a bottom-up level in runs of kGrabWords from the level's counter
-// (dynamic distribution, as WordRuns). The done words of a run are loaded
-// together, one per lane, a run ahead of use. kSkip: words whose rows are all
-// done are not yielded; their next-frontier words and nonzero bits are
-// cleared when the run comes up, one coalesced store per word, so a warp
-// does not walk them one dependent round trip at a time (at late levels most
-// words are such). Call from all lanes of a warp.
+// Words of a bottom-up level in runs of `grab` words (8 to 32, set by the
+// host from the word count: about three runs per resident warp) taken from
+// the level's counter (dynamic distribution, as WordRuns). The done words of
+// a run are loaded together, one per lane, a run ahead of use. kSkip: words
+// whose rows are all done are not yielded; their next-frontier words and
+// nonzero bits are cleared when the run comes up, one coalesced store per
+// word, so a warp does not walk them one dependent round trip at a time (at
+// late levels most words are such). Call from all lanes of a warp.
 __device__ __forceinline__ int64_t grab_n(unsigned long long *ctr, int step) {
     unsigned long long v = 0;
     if ((threadIdx.x & 31) == 0) v = atomicAdd(ctr, (unsigned long long)step);
