@@ -348,7 +348,7 @@ def roofline(dg, roots, d_ms, policy, traffic=None) -> dict:
                               "gbs": round(t.bytes / t.step_us / 1e3, 1)})
     gbs = byts / us / 1e3 if us > 0 else 0.0
     lv = [x["level"] for x in per_level]
-    traffic = (sum(traffic[L] for L in lv) / len(lv)
+    traffic = (round(sum(traffic[L] for L in lv) / len(lv))
                if traffic and lv and all(L in traffic for L in lv) else None)
     return {"bound": "hbm",
             "kernel": "k_ms_bu + k_ms_bu_long + k_ms_bu_long_tail + k_ms_bu_long_fin "
