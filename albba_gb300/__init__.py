@@ -51,7 +51,8 @@ EXPORTED = [
     "alb_sell_export", "alb_sell_long_export", "alb_bfs_opts_default", "alb_bfs", "alb_bfs_device",
     "alb_level_trace", "alb_debug_fail_alloc_after", "alb_gen_rmat", "alb_gen_grid",
     "alb_gen_er", "alb_csr_from_edges", "alb_pick_roots", "alb_host_csr_free",
-    "alb_cbd_write", "alb_cbd_read", "alb_selector_load", "alb_selector_clear",
+    "alb_cbd_write", "alb_cbd_read", "alb_mtx_read", "alb_csr_undirected", "alb_graph_read",
+    "alb_selector_load", "alb_selector_clear",
     "alb_msbfs64", "alb_msbfs64_device", "alb_bfs_profile", "alb_msbfs64_profile",
     "alb_mlp_forward", "alb_mlp_loss_grad", "alb_adam_step", "alb_selector_train",
     "alb_worklist_create", "alb_worklist_destroy", "alb_worklist_add", "alb_worklist_size",
@@ -133,6 +134,9 @@ _sigs = {
     "alb_host_csr_free": (None, [C.POINTER(HostCsr)]),
     "alb_cbd_write": (C.c_int32, [C.c_char_p, C.POINTER(HostCsr)]),
     "alb_cbd_read": (C.c_int32, [C.c_char_p, C.POINTER(HostCsr)]),
+    "alb_mtx_read": (C.c_int32, [C.c_char_p, C.POINTER(HostCsr), _i32p]),
+    "alb_csr_undirected": (C.c_int32, [C.POINTER(HostCsr), C.POINTER(HostCsr)]),
+    "alb_graph_read": (C.c_int32, [C.c_char_p, C.POINTER(HostCsr)]),
     "alb_msbfs64": (C.c_int32, [_P, _P, C.c_int32, C.POINTER(BfsOpts), _P, C.POINTER(Stats)]),
     "alb_msbfs64_device": (C.c_int32, [_P, _P, C.c_int32, C.POINTER(BfsOpts), _P,
                                        C.POINTER(Stats)]),
@@ -271,6 +275,31 @@ def csr_from_edges(n: int, u: np.ndarray, v: np.ndarray) -> Csr:
 def read_cbd(path: str | os.PathLike) -> Csr:
     h = HostCsr()
     check(_lib.alb_cbd_read(str(path).encode(), C.byref(h)))
+    return _wrap(h)
+
+
+def read_mtx(path: str | os.PathLike) -> tuple[Csr, bool]:
+    """Matrix Market file -> (CSR as the reference's reader builds it,
+    symmetric flag); see alb_mtx_read."""
+    h = HostCsr()
+    sym = C.c_int32()
+    check(_lib.alb_mtx_read(str(path).encode(), C.byref(h), C.byref(sym)))
+    return _wrap(h), bool(sym.value)
+
+
+def csr_undirected(g: Csr) -> Csr:
+    """The reference driver's undirected conversion (alb_csr_undirected)."""
+    src = g._as_host()
+    h = HostCsr()
+    check(_lib.alb_csr_undirected(C.byref(src), C.byref(h)))
+    return _wrap(h)
+
+
+def read_graph(path: str | os.PathLike) -> Csr:
+    """Graph load of the reference driver: .cbd as is, .mtx made undirected
+    unless symmetric (alb_graph_read)."""
+    h = HostCsr()
+    check(_lib.alb_graph_read(str(path).encode(), C.byref(h)))
     return _wrap(h)
 
 

@@ -7,8 +7,11 @@
 #include <algorithm>
 #include <atomic>
 #include <cstdlib>
+#include <cctype>
+#include <cstdio>
 #include <cstring>
 #include <new>
+#include <string>
 #include <vector>
 
 #include "albba_gen.h"
@@ -322,6 +325,227 @@ alb_status alb_cbd_read(const char *path, alb_host_csr *out) {
         out->col = col;
         return ALB_OK;
     });
+}
+
+
+}  // extern "C"
+
+// ------------------------------------------------------------ Matrix Market
+// Reader of coordinate Matrix Market files with the reference's semantics
+// (bfs/src/mmio_highlevel.h:140-263, banner rules of mmio.h:248-330): the
+// banner's type (real, integer, complex, pattern) only decides how many
+// numbers follow the two 1-based indices, and values are dropped (the
+// reference overwrites them with 1.0, main.c:106-109); a symmetric or
+// hermitian file stores each off-diagonal entry once and the CSR receives it
+// in both rows; entries go into their rows in file order, the mirrored copy
+// at its source entry's turn. Skew-symmetric files are read as general, as
+// the reference does. Dense (array) files, non-square matrices and indices
+// out of range are refused, where the reference would misread them.
+namespace {
+
+struct MtxFile {
+    FILE *fp = nullptr;
+    ~MtxFile() {
+        if (fp) std::fclose(fp);
+    }
+};
+
+bool next_data_line(FILE *fp, std::vector<char> &buf) {
+    for (;;) {
+        if (!std::fgets(buf.data(), (int)buf.size(), fp)) return false;
+        const char *c = buf.data();
+        while (*c == ' ' || *c == '\t') c++;
+        if (*c == '%' || *c == '\n' || *c == '\r' || *c == '\0') continue;  // comment, blank
+        return true;
+    }
+}
+
+std::string lower(const char *s) {
+    std::string r(s);
+    for (char &ch : r) ch = (char)std::tolower((unsigned char)ch);
+    return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+alb_status alb_mtx_read(const char *path, alb_host_csr *out, int32_t *is_symmetric) {
+    if (!path || !out) return fail(ALB_ERR_INVALID, "alb_mtx_read: bad arguments");
+    std::memset(out, 0, sizeof(*out));
+    if (is_symmetric) *is_symmetric = 0;
+    MtxFile f;
+    f.fp = std::fopen(path, "r");
+    if (!f.fp) return fail(ALB_ERR_IO, "alb_mtx_read: cannot open %s", path);
+    return guarded([&]() -> alb_status {
+        std::vector<char> line(1 << 16);
+        if (!std::fgets(line.data(), (int)line.size(), f.fp))
+            return fail(ALB_ERR_IO, "alb_mtx_read: %s is empty", path);
+        char banner[64] = {0}, obj[64] = {0}, fmt[64] = {0}, type[64] = {0}, sym[64] = {0};
+        if (std::sscanf(line.data(), "%63s %63s %63s %63s %63s", banner, obj, fmt, type, sym) != 5 ||
+            std::strncmp(banner, "%%MatrixMarket", 14) != 0 || lower(obj) != "matrix")
+            return fail(ALB_ERR_IO, "alb_mtx_read: %s has no Matrix Market banner", path);
+        const std::string sf = lower(fmt), st = lower(type), ss = lower(sym);
+        if (sf == "array")
+            return fail(ALB_ERR_UNSUPPORTED, "alb_mtx_read: %s is a dense (array) file", path);
+        int extra;  // numbers after the two indices
+        if (st == "pattern") extra = 0;
+        else if (st == "real" || st == "integer") extra = 1;
+        else if (st == "complex") extra = 2;
+        else return fail(ALB_ERR_IO, "alb_mtx_read: %s: unknown type %s", path, type);
+        bool mirror;
+        if (ss == "symmetric" || ss == "hermitian") mirror = true;
+        else if (ss == "general" || ss == "skew-symmetric") mirror = false;
+        else return fail(ALB_ERR_IO, "alb_mtx_read: %s: unknown symmetry %s", path, sym);
+        if (sf != "coordinate")
+            return fail(ALB_ERR_IO, "alb_mtx_read: %s: unknown format %s", path, fmt);
+        long long rows = 0, cols = 0, entries = 0;
+        if (!next_data_line(f.fp, line) ||
+            std::sscanf(line.data(), "%lld %lld %lld", &rows, &cols, &entries) != 3 || rows < 0 ||
+            cols < 0 || entries < 0)
+            return fail(ALB_ERR_IO, "alb_mtx_read: %s: bad size line", path);
+        if (rows != cols)
+            return fail(ALB_ERR_UNSUPPORTED, "alb_mtx_read: %s is %lld x %lld, not square", path,
+                        rows, cols);
+        if (rows > INT32_MAX)
+            return fail(ALB_ERR_UNSUPPORTED, "alb_mtx_read: %s: %lld rows exceed int32 ids", path,
+                        rows);
+        const int64_t n = rows;
+        std::vector<int32_t> ei((size_t)entries), ej((size_t)entries);
+        for (long long e = 0; e < entries; e++) {
+            if (!next_data_line(f.fp, line))
+                return fail(ALB_ERR_IO, "alb_mtx_read: %s ends after %lld of %lld entries", path, e,
+                            entries);
+            char *c = line.data(), *end = nullptr;
+            const long long i = std::strtoll(c, &end, 10);
+            if (end == c) return fail(ALB_ERR_IO, "alb_mtx_read: %s: bad entry %lld", path, e + 1);
+            c = end;
+            const long long j = std::strtoll(c, &end, 10);
+            if (end == c) return fail(ALB_ERR_IO, "alb_mtx_read: %s: bad entry %lld", path, e + 1);
+            c = end;
+            for (int k = 0; k < extra; k++) {  // the value(s): checked, then dropped
+                std::strtod(c, &end);
+                if (end == c)
+                    return fail(ALB_ERR_IO, "alb_mtx_read: %s: entry %lld lacks its value", path,
+                                e + 1);
+                c = end;
+            }
+            if (i < 1 || i > rows || j < 1 || j > cols)
+                return fail(ALB_ERR_IO, "alb_mtx_read: %s: entry %lld (%lld, %lld) outside %lld x %lld",
+                            path, e + 1, i, j, rows, cols);
+            ei[(size_t)e] = (int32_t)(i - 1);
+            ej[(size_t)e] = (int32_t)(j - 1);
+        }
+        // rows counted, then filled in file order (the mirrored copy at its
+        // source entry's turn)
+        std::vector<int64_t> cnt((size_t)n + 1, 0);
+        for (long long e = 0; e < entries; e++) {
+            cnt[(size_t)ei[(size_t)e]]++;
+            if (mirror && ei[(size_t)e] != ej[(size_t)e]) cnt[(size_t)ej[(size_t)e]]++;
+        }
+        exclusive_scan_inplace(cnt.data(), n);
+        const int64_t nnz = cnt[(size_t)n];
+        int64_t *rp = xmalloc<int64_t>((size_t)n + 1);
+        int32_t *col = xmalloc<int32_t>((size_t)nnz);
+        std::memcpy(rp, cnt.data(), sizeof(int64_t) * ((size_t)n + 1));
+        std::vector<int64_t> at(cnt.begin(), cnt.end() - 1);
+        for (long long e = 0; e < entries; e++) {
+            const int32_t i = ei[(size_t)e], j = ej[(size_t)e];
+            col[at[(size_t)i]++] = j;
+            if (mirror && i != j) col[at[(size_t)j]++] = i;
+        }
+        out->n = n;
+        out->nnz = nnz;
+        out->rowptr = rp;
+        out->col = col;
+        if (is_symmetric) *is_symmetric = mirror ? 1 : 0;
+        return ALB_OK;
+    });
+}
+
+// The reference driver's conversion of a non-symmetric graph to an
+// undirected one (bfs/src/main.c:127-163): row i of the result merges row i
+// of the transpose (ascending: the transpose is filled row by row of the
+// input) with row i of the input by the two-pointer merge of
+// bfs/src/utils.c:351-380, which emits an element once when both heads are
+// equal. On ascending rows that is the sorted union; on unsorted input rows
+// the result keeps the reference's order and repeats.
+alb_status alb_csr_undirected(const alb_host_csr *in, alb_host_csr *out) {
+    if (!in || !out || in->n < 0 || (in->n > 0 && (!in->rowptr || (in->nnz > 0 && !in->col))))
+        return fail(ALB_ERR_INVALID, "alb_csr_undirected: bad arguments");
+    std::memset(out, 0, sizeof(*out));
+    return guarded([&]() -> alb_status {
+        const int64_t n = in->n, nnz = in->nnz;
+        if (in->rowptr[0] != 0 || in->rowptr[n] != nnz)
+            return fail(ALB_ERR_INVALID, "alb_csr_undirected: row offsets do not span the entries");
+        for (int64_t i = 0; i < n; i++)
+            if (in->rowptr[i] > in->rowptr[i + 1])
+                return fail(ALB_ERR_INVALID, "alb_csr_undirected: row offsets decrease at %lld",
+                            (long long)i);
+        for (int64_t e = 0; e < nnz; e++)
+            if (in->col[e] < 0 || in->col[e] >= n)
+                return fail(ALB_ERR_INVALID, "alb_csr_undirected: column outside [0, %lld)",
+                            (long long)n);
+        // transpose: tp / trow, rows of the transpose ascending
+        std::vector<int64_t> tp((size_t)n + 1, 0);
+        for (int64_t e = 0; e < nnz; e++) tp[(size_t)in->col[e]]++;
+        exclusive_scan_inplace(tp.data(), n);
+        std::vector<int32_t> trow((size_t)nnz);
+        {
+            std::vector<int64_t> at(tp.begin(), tp.end() - 1);
+            for (int64_t i = 0; i < n; i++)
+                for (int64_t e = in->rowptr[i]; e < in->rowptr[i + 1]; e++)
+                    trow[(size_t)at[(size_t)in->col[e]]++] = (int32_t)i;
+        }
+        int64_t *rp = xmalloc<int64_t>((size_t)n + 1);
+        int32_t *col = xmalloc<int32_t>((size_t)(2 * nnz));
+        int64_t len = 0;
+        for (int64_t i = 0; i < n; i++) {
+            const int32_t *a = trow.data() + tp[(size_t)i], *b = in->col + in->rowptr[i];
+            const int64_t al = tp[(size_t)i + 1] - tp[(size_t)i], bl = in->rowptr[i + 1] - in->rowptr[i];
+            int64_t x = 0, y = 0;
+            rp[i] = len;
+            while (x < al && y < bl) {
+                if (a[x] < b[y]) col[len++] = a[x++];
+                else if (a[x] == b[y]) {
+                    col[len++] = b[y++];
+                    x++;
+                } else col[len++] = b[y++];
+            }
+            while (x < al) col[len++] = a[x++];
+            while (y < bl) col[len++] = b[y++];
+        }
+        rp[n] = len;
+        out->n = n;
+        out->nnz = len;
+        out->rowptr = rp;
+        out->col = col;
+        return ALB_OK;
+    });
+}
+
+// Graph load as the reference driver does it (bfs/src/main.c:86-163,
+// biio.h:127-149): .cbd read as is; .mtx read, then made undirected when the
+// file is not symmetric.
+alb_status alb_graph_read(const char *path, alb_host_csr *out) {
+    if (!path || !out) return fail(ALB_ERR_INVALID, "alb_graph_read: bad arguments");
+    std::memset(out, 0, sizeof(*out));
+    const size_t len = std::strlen(path);
+    auto ends = [&](const char *ext) { return len >= 4 && std::strcmp(path + len - 4, ext) == 0; };
+    if (ends(".cbd")) return alb_cbd_read(path, out);
+    if (!ends(".mtx"))
+        return fail(ALB_ERR_UNSUPPORTED, "alb_graph_read: %s is neither .mtx nor .cbd", path);
+    alb_host_csr raw;
+    int32_t sym = 0;
+    alb_status rc = alb_mtx_read(path, &raw, &sym);
+    if (rc != ALB_OK) return rc;
+    if (sym) {
+        *out = raw;
+        return ALB_OK;
+    }
+    rc = alb_csr_undirected(&raw, out);
+    alb_host_csr_free(&raw);
+    return rc;
 }
 
 }  // extern "C"

@@ -58,6 +58,26 @@ void alb_host_csr_free(alb_host_csr *g);
 alb_status alb_cbd_write(const char *path, const alb_host_csr *g);
 alb_status alb_cbd_read(const char *path, alb_host_csr *out);
 
+/* Coordinate Matrix Market (.mtx) file -> CSR, as the reference's reader
+ * builds it (replaces mmio_info + mmio_data, bfs/src/mmio_highlevel.h:11-263):
+ * values dropped; symmetric and hermitian files have every off-diagonal entry
+ * placed in both rows; entries in file order within a row (the mirrored copy
+ * at its source entry's turn); skew-symmetric read as general. Refuses dense
+ * files and non-square matrices (ALB_ERR_UNSUPPORTED), malformed files and
+ * indices out of range (ALB_ERR_IO). *is_symmetric (may be NULL) = 1 for
+ * symmetric or hermitian files. */
+alb_status alb_mtx_read(const char *path, alb_host_csr *out, int32_t *is_symmetric);
+
+/* The reference driver's undirected conversion of a non-symmetric graph
+ * (bfs/src/main.c:127-163): row i = the two-pointer merge of row i of the
+ * transpose and row i of the input (bfs/src/utils.c:351-380). */
+alb_status alb_csr_undirected(const alb_host_csr *in, alb_host_csr *out);
+
+/* Graph load of the reference driver (bfs/src/main.c:86-163, biio.h:127-149):
+ * path ending in .cbd -> alb_cbd_read; .mtx -> alb_mtx_read, then
+ * alb_csr_undirected unless the file is symmetric. */
+alb_status alb_graph_read(const char *path, alb_host_csr *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -12,6 +12,11 @@
  *   convert_csr_to_sellcs        bfs/src/sparse_matrix.c:435-521
  *   convert_csr_to_sellcs_dfc    bfs/src/sparse_matrix.c:523-623
  *   run_custom_bfs_test          bfs/src/bfs_SELLCSv2.c:126-820 (root row 0)
+ *   mmio_info, mmio_data         bfs/src/mmio_highlevel.h:11-263 (.mtx -> CSR)
+ *   the undirected conversion    bfs/src/main.c:127-163 (CSR merged with its
+ *                                CSC by MergeArr, utils.c:351-380), restated
+ *                                here as a call sequence of the reference's
+ *                                convert_csr_to_csc and MergeArr
  */
 #include "common.h"
 #include "sparse_matrix.h"
@@ -25,6 +30,7 @@ int verify = 0;
 int bypass_record = 0;
 
 #include "bfs_ref.h"
+#include "mmio_highlevel.h"
 
 extern int sigma_window;
 extern int ve_scalar_dead_calls;
@@ -180,4 +186,48 @@ int refh_custom_bfs(int n, const int *rowptr, const int *col, int sigma,
     free(iter_times);
     free_csr(&m);
     return num_iter;
+}
+
+
+/* .mtx header through the reference reader: rows, columns, CSR entry count
+ * (after the symmetric mirroring), symmetric flag; nonzero on failure. */
+int refh_mtx_info(const char *path, int *m, int *n, int *nnz, int *sym)
+{
+    return mmio_info(m, n, nnz, sym, (char *)path);
+}
+
+/* The CSR the reference reader builds (values dropped). */
+int refh_mtx_data(const char *path, int m, int nnz, int *rowptr, int *col)
+{
+    double *val = (double *)malloc(sizeof(double) * (nnz > 0 ? nnz : 1));
+    int rc = mmio_data(rowptr, col, val, (char *)path);
+    free(val);
+    (void)m;
+    return rc;
+}
+
+/* The reference driver's conversion of a non-symmetric CSR to an undirected
+ * graph: row i of the result is MergeArr(row i of the CSC, row i of the
+ * CSR). out_col needs 2 * nnz entries; returns the result's entry count. */
+int refh_undirected(int n, const int *rowptr, const int *col, int *out_rowptr, int *out_col)
+{
+    SparseMatrixCSR m;
+    make_csr(&m, n, rowptr, col);
+    SparseMatrixCSC t;
+    convert_csr_to_csc(&m, &t);
+    int len = 0;
+    for (int i = 0; i < n; i++) {
+        const int l1 = t.column_pointers[i + 1] - t.column_pointers[i];
+        const int l2 = m.row_pointers[i + 1] - m.row_pointers[i];
+        out_rowptr[i] = MergeArr(t.row_indices + t.column_pointers[i], l1,
+                                 m.column_indices + m.row_pointers[i], l2, out_col + len);
+        len += out_rowptr[i];
+    }
+    out_rowptr[n] = 0;
+    exclusive_scan(out_rowptr, n + 1);
+    free(t.column_pointers);
+    free(t.row_indices);
+    free(t.values);
+    free_csr(&m);
+    return len;
 }
