@@ -264,7 +264,7 @@ __device__ __forceinline__ int64_t grab_n(unsigned long long *ctr, int step) {
 template <bool kSkip>
 struct MsWords {
     int64_t cur, nxt;     // first word of the current run and of the next one
-    uint32_t dcur, dnxt;  // lane l < kGrabWords: done word of word cur + l / nxt + l
+    uint32_t dcur, dnxt;  // lane l < step: done word of word cur + l / nxt + l
     unsigned left;        // words of the current run not yet yielded
     int step;             // words per run (<= 32)
     __device__ __forceinline__ uint32_t load(const MsArgs &a, int64_t r) const {
