@@ -35,22 +35,32 @@ namespace alb {
 // freed memory (release threshold: unlimited) instead of returning it to the
 // driver: the gigabytes of a graph's CSR, SELL and traversal state are
 // reused by the next graph built in the process without new driver
-// allocations, and a destroy does not wait on driver frees.
+// allocations, and a destroy does not wait on driver frees. A device without
+// memory pools gets plain cudaMalloc / cudaFree.
 namespace {
-void keep_pool_memory() {
+bool use_pool() {
     static std::mutex mu;
-    static bool done[256] = {};
+    static int state[256] = {};  // 0 unknown, 1 pool, 2 plain
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return;
-    std::lock_guard<std::mutex> lk(mu);
-    if (done[dev]) return;
-    cudaMemPool_t pool;
-    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
-        uint64_t thr = UINT64_MAX;
-        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) {
+        cudaGetLastError();
+        return false;
     }
-    cudaGetLastError();
-    done[dev] = true;
+    std::lock_guard<std::mutex> lk(mu);
+    if (state[dev] == 0) {
+        int ok = 0;
+        cudaMemPool_t pool;
+        if (cudaDeviceGetAttribute(&ok, cudaDevAttrMemoryPoolsSupported, dev) == cudaSuccess && ok &&
+            cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t thr = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+            state[dev] = 1;
+        } else {
+            state[dev] = 2;
+        }
+        cudaGetLastError();
+    }
+    return state[dev] == 1;
 }
 }  // namespace
 
@@ -59,23 +69,31 @@ alb_status dmalloc(void **p, size_t bytes, const char *what) {
     if (injected_alloc_failure())
         return fail(ALB_ERR_OOM, "device allocation of %zu bytes for %s failed (injected)", bytes,
                     what);
-    keep_pool_memory();
-    // allocated in the legacy stream's order, then waited for, so that the
-    // buffer can be used from any stream at once
-    cudaError_t e = cudaMallocAsync(p, bytes ? bytes : 16, 0);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+    cudaError_t e;
+    if (use_pool()) {
+        // allocated in the legacy stream's order, then waited for, so that the
+        // buffer can be used from any stream at once
+        e = cudaMallocAsync(p, bytes ? bytes : 16, 0);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+    } else {
+        e = cudaMalloc(p, bytes ? bytes : 16);
+    }
     if (e != cudaSuccess) {
         cudaGetLastError();
         *p = nullptr;
         if (e == cudaErrorMemoryAllocation)
             return fail(ALB_ERR_OOM, "device allocation of %zu bytes for %s failed", bytes, what);
-        return fail(ALB_ERR_CUDA, "cudaMallocAsync for %s: %s", what, cudaGetErrorString(e));
+        return fail(ALB_ERR_CUDA, "device allocation for %s: %s", what, cudaGetErrorString(e));
     }
     return ALB_OK;
 }
 
 void dfree(void *p) {
     if (!p) return;
+    if (!use_pool()) {
+        cudaFree(p);
+        return;
+    }
     // work on any stream may still use the buffer (cudaFree waited for the
     // device too); it then goes back to the pool
     cudaDeviceSynchronize();
