@@ -772,6 +772,11 @@ __global__ void __launch_bounds__(kBuSmemBlock, 1) k_bu_smem(BfsArgs a) {
     while (!mbar_try_wait(&s_bar, 0)) {
         if (globaltimer_ns() - t0 > kBulkWaitNs) {
             if (threadIdx.x == 0) atomicExch(&a.ctl->err, ALB_ERR_TIMEOUT);
+            // the copy may still be writing this CTA's shared memory: stay
+            // resident until it lands (second, longer bound) before leaving
+            const uint64_t t1 = globaltimer_ns();
+            while (!mbar_try_wait(&s_bar, 0) && globaltimer_ns() - t1 < 4 * kBulkWaitNs)
+                __nanosleep(1024);
             return;
         }
     }

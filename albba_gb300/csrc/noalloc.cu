@@ -2,20 +2,22 @@
 //
 // Some callers cannot call cudaMalloc: a plug-in living inside a host process
 // whose device memory belongs to another allocator (a framework's caching
-// allocator that must account for every byte, a fixed-budget serving
-// process), or a latency-critical caller that cannot afford cudaMalloc's
-// implicit device synchronisation. For them this entry point runs a BFS on a
-// CSR the caller already holds on the device, writes levels and parents to
-// caller buffers, and keeps every temporary in one file-scope device array
-// (kNoAllocScratchBytes = 8,782,080 bytes) that each GPU loading the library
-// holds until the process exits.
+// allocator that must account for every byte, a fixed-budget serving process
+// that reserves all device memory up front). For them this entry point runs a
+// BFS on a CSR the caller already holds on the device, writes levels and
+// parents to caller buffers, and keeps every temporary in one file-scope
+// device array (kNoAllocScratchBytes = 8,782,080 bytes) that each GPU loading
+// the library holds until the process exits.
 //
 // The array is shared by all calls on a device and keeps the last call's
 // contents; each call clears what must start at zero. Calls that overlap on
 // the GPU (two streams, two threads) race on the array: serialise them.
 // In host code the array's name is not a device address: the first call on a
-// device looks up its address with cudaGetSymbolAddress (with that device
-// current) and caches it, so make that first call before any stream capture.
+// device (and the first call after that device's context was destroyed and
+// recreated, e.g. by cudaDeviceReset) looks up its address with
+// cudaGetSymbolAddress, with that device current, and caches it keyed on the
+// context's unique id; make that first call before any stream capture.
+// Each call waits for the given stream once, to read the traversal's status.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -54,7 +56,7 @@ static_assert(sizeof(NaCtl) <= kCtlBytes, "control block");
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 struct NaArgs {
-    int64_t n, m;
+    int64_t n;
     const int64_t *rp;
     const int32_t *col;
     int32_t root;
@@ -92,8 +94,9 @@ __device__ bool na_sync(NaCtl *c, unsigned nblocks) {
 
 // One cooperative kernel for the whole traversal: clear, seed, then per level
 // a top-down push (queue, atomicMin parents, atomicOr claims) or, for a
-// symmetric graph, a bottom-up pull (first frontier source in the ascending
-// row); Beamer alpha/beta picks the direction.
+// symmetric graph, a bottom-up pull (first frontier source in the row, which
+// is the smallest when the row is ascending); Beamer alpha/beta picks the
+// direction.
 __global__ void k_bfs_noalloc(NaArgs a) {
     NaCtl *c = (NaCtl *)a.scratch;
     uint32_t *V = (uint32_t *)(a.scratch + kOffVis);
@@ -106,6 +109,7 @@ __global__ void k_bfs_noalloc(NaArgs a) {
     const int lane = threadIdx.x & 31;
     const int64_t gw = tid >> 5, nwarps = nth >> 5;
     const int64_t nwords = (a.n + 31) / 32;
+    const int64_t m = a.rp[a.n];
     for (int64_t w = tid; w < nwords; w += nth) {
         V[w] = 0;
         F[w] = 0;
@@ -133,7 +137,7 @@ __global__ void k_bfs_noalloc(NaArgs a) {
     if (!na_sync(c, nb)) return;
     int64_t nf = 1, prev_nf = 0;
     int64_t mf = a.rp[a.root + 1] - a.rp[a.root];
-    int64_t mu = a.m - mf;
+    int64_t mu = m - mf;
     int prev_dir = 0;
     bool dense = false;  // F holds the frontier (true) or only Q does (false)
     for (int L = 0; nf > 0 && L <= a.n; L++) {
@@ -240,8 +244,43 @@ __global__ void k_bfs_noalloc(NaArgs a) {
     if (tid == 0) c->done = 1;
 }
 
+// Device address of g_noalloc_scratch per device ordinal, valid for the
+// context whose unique id is stored beside it: a context destroyed and
+// recreated (cudaDeviceReset) may load the module at another address.
+struct NaCache {
+    unsigned long long ctx_id;
+    unsigned char *ptr;
+};
 std::mutex g_na_mu;
-unsigned char *g_na_ptr[64] = {nullptr};
+NaCache g_na_cache[64] = {};
+
+typedef int (*PfnCtxGetCurrent)(void **);
+typedef int (*PfnCtxGetId)(void *, unsigned long long *);
+
+// Unique id of the calling thread's current context (driver API through the
+// runtime's entry-point query, so the library does not link libcuda).
+cudaError_t current_ctx_id(unsigned long long *id) {
+    static PfnCtxGetCurrent get_cur = nullptr;
+    static PfnCtxGetId get_id = nullptr;
+    if (!get_cur || !get_id) {
+        cudaDriverEntryPointQueryResult q1, q2;
+        void *f1 = nullptr, *f2 = nullptr;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000,
+                                                         cudaEnableDefault, &q1);
+        if (e == cudaSuccess)
+            e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+        if (e != cudaSuccess) return e;
+        if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            return cudaErrorNotSupported;
+        get_cur = (PfnCtxGetCurrent)f1;
+        get_id = (PfnCtxGetId)f2;
+    }
+    void *ctx = nullptr;
+    if (get_cur(&ctx) != 0) return cudaErrorInitializationError;
+    if (!ctx) return cudaErrorDeviceUninitialized;
+    if (get_id(ctx, id) != 0) return cudaErrorInitializationError;
+    return cudaSuccess;
+}
 
 }  // namespace
 }  // namespace alb
@@ -260,10 +299,26 @@ extern "C" alb_status alb_bfs_csr_noalloc(int64_t n, const int64_t *d_rowptr, co
     int dev = 0;
     ALB_CK(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64) return fail(ALB_ERR_UNSUPPORTED, "alb_bfs_csr_noalloc: device id %d", dev);
+    unsigned long long ctx_id = 0;
+    {
+        cudaError_t e = current_ctx_id(&ctx_id);
+        if (e == cudaErrorDeviceUninitialized) {
+            // no context yet on this thread: make the device's primary context
+            // current (initialising it if needed), then ask again
+            ALB_CK(cudaSetDevice(dev));
+            e = current_ctx_id(&ctx_id);
+        }
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(ALB_ERR_CUDA, "alb_bfs_csr_noalloc: current context: %s",
+                        cudaGetErrorString(e));
+        }
+    }
     unsigned char *scratch;
     {
         std::lock_guard<std::mutex> lk(g_na_mu);
-        if (!g_na_ptr[dev]) {
+        NaCache &c = g_na_cache[dev];
+        if (!c.ptr || c.ctx_id != ctx_id) {
             void *p = nullptr;
             cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
             if (e != cudaSuccess) {
@@ -271,20 +326,17 @@ extern "C" alb_status alb_bfs_csr_noalloc(int64_t n, const int64_t *d_rowptr, co
                 return fail(ALB_ERR_CUDA, "alb_bfs_csr_noalloc: cudaGetSymbolAddress: %s",
                             cudaGetErrorString(e));
             }
-            g_na_ptr[dev] = (unsigned char *)p;
+            c.ptr = (unsigned char *)p;
+            c.ctx_id = ctx_id;
         }
-        scratch = g_na_ptr[dev];
+        scratch = c.ptr;
     }
     cudaStream_t st = (cudaStream_t)stream;
-    int64_t m = 0;
-    ALB_CK(cudaMemcpyAsync(&m, d_rowptr + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-    ALB_CK(cudaStreamSynchronize(st));
     // the barrier counter must start at zero (the previous call leaves it so,
     // unless it was interrupted)
     ALB_CK(cudaMemsetAsync(scratch, 0, kCtlBytes, st));
     NaArgs a;
     a.n = n;
-    a.m = m;
     a.rp = d_rowptr;
     a.col = d_col;
     a.root = root;

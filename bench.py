@@ -153,9 +153,25 @@ def config(args, g, extra=None):
 
 
 # ----------------------------------------------------------------- CPU side
+# The reference's level loop runs on a SELL-256 matrix with sigma 16384 (its
+# defaults, bfs/src/bfs_SELLCSv2.c:29) and splits every level into 8 tasks
+# (chunk_size forced to 8, bfs/src/bfs_SELLCSv2.c:214); the CPU port does the
+# same, on all host threads (OpenMP).
+REF_C, REF_SIGMA, REF_TASKS = 256, 16384, 8
+
+
+def ref_config(threads: int) -> dict:
+    return {"C": REF_C, "sigma": REF_SIGMA, "long_row": None, "tasks_per_level": REF_TASKS,
+            "threads": threads,
+            "kernels": "pull (bfs_kernel_SELLCS_DFC_bitmap) + sparse-x "
+                       "(bfs_kernel_spmspv_SELLCS_DFC_bitmap) restated in C",
+            "input": "graph generated by albba_gb300's host generator (CPU only, before "
+                     "the timed region); the timed region runs oracle/refalgo.c only"}
+
+
 def cpu_baseline(g, roots, nroots: int) -> dict:
     import oracle
-    ra = oracle.RefAlgo(g.rowptr, g.col, sigma=16384, ntasks=0)
+    ra = oracle.RefAlgo(g.rowptr, g.col, sigma=REF_SIGMA, ntasks=REF_TASKS)
     deg = g.degrees()
     edges, ms = 0, 0.0
     for r in roots[:nroots]:
@@ -166,8 +182,10 @@ def cpu_baseline(g, roots, nroots: int) -> dict:
     ra.close()
     threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     return {"value": edges / ms / 1e6, "unit": "GTEPS", "cores": threads, "kind": "port",
-            "sample": f"{nroots} of {len(roots)} roots, level loop only (SELL-256 build "
-                      f"{ra.conv_ms:.0f} ms excluded, as the reference times it)"}
+            "sample": f"{nroots} of {len(roots)} roots, level loop only (SELL-{REF_C} build "
+                      f"{ra.conv_ms:.0f} ms excluded, as the reference times it), "
+                      f"{REF_TASKS} tasks per level as in the reference",
+            "config": ref_config(threads)}
 
 
 def run_reference(args, rank: int, world: int) -> None:
@@ -175,7 +193,7 @@ def run_reference(args, rank: int, world: int) -> None:
         return
     g, roots, _ = make_graph(args)
     import oracle
-    ra = oracle.RefAlgo(g.rowptr, g.col, sigma=16384, ntasks=0)
+    ra = oracle.RefAlgo(g.rowptr, g.col, sigma=REF_SIGMA, ntasks=REF_TASKS)
     deg = g.degrees()
     comp = {}
     times = []
@@ -196,9 +214,11 @@ def run_reference(args, rank: int, world: int) -> None:
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / max(len(times), 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic RMAT (seeded), reference level loop restated in C (OpenMP)",
-            "config": config(args, g, {"step": "one root per step (bounded CPU sample)"}),
+            "config": config(args, g, {"step": "one root per step (bounded CPU sample)",
+                                       **ref_config(threads)}),
             "cpu_baseline": {"value": v, "unit": "GTEPS", "cores": threads, "kind": "port",
-                             "sample": f"{args.steps} timed roots, one per step"},
+                             "sample": f"{args.steps} timed roots, one per step, level loop "
+                                       f"only, {REF_TASKS} tasks per level"},
             "e2e": {"value": v, "unit": "GTEPS", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     ra.close()
@@ -276,8 +296,9 @@ def run_ours(args, rank: int, world: int, dist) -> None:
     plain = world * pedges / pms / 1e6
     hm = len(per_root) / sum(m / (e / 1e6) for e, m in per_root if e > 0) if per_root else None
 
-    roof = None if args.no_roofline else roofline(dg, roots, d_ms, policy, profiled_traffic(args))
+    roof = None if args.no_roofline else roofline(dg, roots, d_ms, policy)
     roof_plain = None if args.no_roofline else roofline_plain(dg, roots[:8])
+    heldout = selector_heldout(dg, g, roots, loaded)
     e2e = None if args.no_e2e else e2e_batched(args, g, roots, ab, torch, bopts)
     cpu = cpu_baseline(g, roots, args.cpu_roots) if rank == 0 and args.cpu_roots > 0 else None
     if rank != 0:
@@ -296,7 +317,9 @@ def run_ours(args, rank: int, world: int, dist) -> None:
                               f"({'learned' if loaded.get('plain') else 'beamer'}, {args.loop} loop)"},
             "batched_over_plain": value / plain if plain else None,
             "selector": {"batched": policy, "weights": {f: bool(loaded.get(f)) for f in loaded},
-                         "heldout": {f: (m or {}).get("heldout") for f, m in meta.items()}},
+                         "heldout_measured": heldout,
+                         "heldout_at_training": {f: (m or {}).get("heldout")
+                                                 for f, m in meta.items()}},
             "sell_build_ms": build_ms, "graph_gen_s": gen_s,
             "gpu_launches": launches, "clocks": clk.summary(), "roofline": roof,
             "roofline_plain": roof_plain,
@@ -304,29 +327,7 @@ def run_ours(args, rank: int, world: int, dist) -> None:
     emit(line, args)
 
 
-# DRAM traffic of each bottom-up level from the committed ncu summary, which
-# was captured on this workload (RMAT s24 ef16, 64 roots, C 32, sigma 1024,
-# long_row 1024); other workloads report null.
-TRAFFIC_PROFILE = Path(__file__).resolve().parent / "profiles" / "k_ms_bu_rmat22_rmat24.md"
-
-
-def profiled_traffic(args):
-    """Per-level DRAM bytes {level: bytes} from the committed ncu summary of
-    this workload, or None for other workloads."""
-    if (args.scale, args.edgefactor, args.roots, args.sigma, args.long_row) != (24, 16, 64, 1024, 1024):
-        return None
-    out = {}
-    try:
-        for line in TRAFFIC_PROFILE.read_text().splitlines():
-            if line.startswith("roofline.traffic.level"):
-                key, val = line[len("roofline.traffic.level"):].split(":", 1)
-                out[int(key)] = int(val)
-    except (OSError, ValueError):
-        return None
-    return out or None
-
-
-def roofline(dg, roots, d_ms, policy, traffic=None) -> dict:
+def roofline(dg, roots, d_ms, policy) -> dict:
     """Dominant kernel of the batched step: the bottom-up level of the 64-root
     BFS (k_ms_bu over the slices, then the long-row head/tail passes and their
     fold-in, the push of the pushed roots and the frontier sampling). Bytes
@@ -347,9 +348,6 @@ def roofline(dg, roots, d_ms, policy, traffic=None) -> dict:
             per_level.append({"level": t.level, "bytes": t.bytes, "us": round(t.step_us, 1),
                               "gbs": round(t.bytes / t.step_us / 1e3, 1)})
     gbs = byts / us / 1e3 if us > 0 else 0.0
-    lv = [x["level"] for x in per_level]
-    traffic = (round(sum(traffic[L] for L in lv) / len(lv))
-               if traffic and lv and all(L in traffic for L in lv) else None)
     return {"bound": "hbm",
             "kernel": "k_ms_bu + k_ms_bu_long + k_ms_bu_long_tail + k_ms_bu_long_fin "
                       "+ k_ms_tq + k_ms_td<push> + k_ms_td_big<push> + k_ms_sample "
@@ -357,10 +355,39 @@ def roofline(dg, roots, d_ms, policy, traffic=None) -> dict:
             "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
             "peak_kind": f"{kind} HBM copy bandwidth (burst)",
             "bytes_per_launch": byts / max(nlev, 1), "us_per_launch": us / max(nlev, 1),
-            "launches": nlev, "levels": per_level, "traffic": traffic,
-            "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum over all launches "
-                               "of each bottom-up level this run took, averaged per level "
-                               "(profiles/k_ms_bu_rmat22_rmat24.md)") if traffic else None}
+            "launches": nlev, "levels": per_level,
+            # DRAM bytes need an ncu capture, which this run does not take
+            # (one-kernel captures of a smaller graph are summarised under
+            # profiles/)
+            "traffic": None}
+
+
+def selector_heldout(dg, g, roots, loaded, plain_roots: int = 4) -> dict:
+    """The selector's per-level regret on this run's graph, measured here:
+    every level of the traversal is run with each of the three variants from
+    the same state and timed (alb_msbfs64_profile / alb_bfs_profile); the
+    regret of a rule is its choices' time over the fastest variant's. The
+    networks were trained on other graphs, so this graph is held out."""
+    import albba_gb300 as ab
+    from albba_gb300 import selector
+    out = {"graph": "this run's graph (held out from training)"}
+    for form in ("batched", "plain"):
+        if not loaded.get(form):
+            continue
+        prof = selector.Profiles()
+        if form == "batched":
+            prof.add(dg.msbfs64_profile(roots, ab.bfs_opts("beamer")), g.n, 0)
+        else:
+            for i, r in enumerate(roots[:plain_roots]):
+                prof.add(dg.bfs_profile(int(r), ab.bfs_opts("beamer", "host")), g.n, i)
+        feat, us, state, group = prof.arrays()
+        best = us.argmin(axis=1)
+        w = selector.load(form)
+        out[form] = {"levels": int(len(us)),
+                     "roots": len(roots) if form == "batched" else min(plain_roots, len(roots)),
+                     "mlp": selector.regret(us, selector.mlp_choices(w, feat)),
+                     "beamer": selector.regret(us, selector.beamer_choices(state, group, best))}
+    return out
 
 
 def roofline_plain(dg, roots) -> dict:
@@ -384,7 +411,29 @@ def roofline_plain(dg, roots) -> dict:
             "launches": nlev, "roots": len(roots)}
 
 
-def e2e_batched(args, g, roots, ab, torch, opts) -> dict:
+def copy_floor(torch, nbytes: int = 1 << 30) -> dict:
+    """Page-locked host <-> device copy bandwidth on this machine (CUDA events,
+    best of 5 copies of 1 GiB each way): the floor under e2e's copies."""
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    st = torch.cuda.current_stream()
+    out = {}
+    for name, dst, src in (("h2d_gbs", d, h), ("d2h_gbs", h, d)):
+        best = None
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            dst.copy_(src, non_blocking=True)
+            e1.record(st)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        out[name] = nbytes / best / 1e6
+    del h, d
+    return out
+
+
+def e2e_batched(args, g, roots, ab, torch, opts, steps: int = 5) -> dict:
     """Host CSR in, host levels out, through the C ABI: alb_graph_create +
     alb_sell_build + alb_msbfs64 (n x 64 int32 levels copied back)."""
     # page-locked host buffers: the graph the caller hands over and the levels
@@ -400,21 +449,20 @@ def e2e_batched(args, g, roots, ab, torch, opts) -> dict:
     levels = pinned((g.n, 64), torch.int32)
     h2d = rp.nbytes + col.nbytes
     d2h = levels.nbytes
+    flags = ab.CSR_SYMMETRIC | ab.CSR_SORTED
 
     def step():
-        with ab.Graph(hg, flags=ab.CSR_SYMMETRIC | ab.CSR_SORTED) as dg:
+        with ab.Graph(hg, flags=flags) as dg:
             dg.sell_build(32, args.sigma, args.long_row)
-            st = ab.check(ab.lib().alb_msbfs64(dg.handle, roots.ctypes.data, len(roots),
-                                                ab.C.byref(opts), levels.ctypes.data,
-                                                ab.C.byref(ab.Stats())))
-            del st
+            ab.check(ab.lib().alb_msbfs64(dg.handle, roots.ctypes.data, len(roots),
+                                          ab.C.byref(opts), levels.ctypes.data,
+                                          ab.C.byref(ab.Stats())))
         return 0
 
     step()
     torch.cuda.synchronize()
-    k = 2
     t0 = time.perf_counter()
-    for _ in range(k):
+    for _ in range(steps):
         step()
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
@@ -422,8 +470,33 @@ def e2e_batched(args, g, roots, ab, torch, opts) -> dict:
     edges = 0
     for i in range(len(roots)):
         edges += int(deg[levels[:, i] >= 0].sum()) // 2
-    return {"value": k * edges / dt / 1e9, "unit": "GTEPS", "h2d_bytes_per_step": h2d,
-            "d2h_bytes_per_step": d2h, "steps": k,
+    # phase split of one more step (wall clock, a synchronize after each call)
+    ph = {}
+    t = time.perf_counter()
+    dg = ab.Graph(hg, flags=flags)
+    torch.cuda.synchronize()
+    ph["graph_create_ms"] = (time.perf_counter() - t) * 1e3
+    t = time.perf_counter()
+    dg.sell_build(32, args.sigma, args.long_row)
+    torch.cuda.synchronize()
+    ph["sell_build_ms"] = (time.perf_counter() - t) * 1e3
+    t = time.perf_counter()
+    ab.check(ab.lib().alb_msbfs64(dg.handle, roots.ctypes.data, len(roots), ab.C.byref(opts),
+                                  levels.ctypes.data, ab.C.byref(ab.Stats())))
+    torch.cuda.synchronize()
+    ph["msbfs64_with_level_copy_ms"] = (time.perf_counter() - t) * 1e3
+    t = time.perf_counter()
+    dg.close()
+    torch.cuda.synchronize()
+    ph["graph_destroy_ms"] = (time.perf_counter() - t) * 1e3
+    fl = copy_floor(torch)
+    floor_ms = h2d / fl["h2d_gbs"] / 1e6 + d2h / fl["d2h_gbs"] / 1e6
+    return {"value": steps * edges / dt / 1e9, "unit": "GTEPS", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "steps": steps, "ms_per_step": dt / steps * 1e3,
+            "phases": {k: round(v, 2) for k, v in ph.items()},
+            "copy_floor": {"h2d_gbs": round(fl["h2d_gbs"], 1), "d2h_gbs": round(fl["d2h_gbs"], 1),
+                           "ms_per_step": round(floor_ms, 2),
+                           "how": "page-locked 1 GiB copies, best of 5, CUDA events"},
             "path": "alb_graph_create (host CSR) + alb_sell_build + alb_msbfs64 (host n x 64 "
                     "levels), wall clock"}
 

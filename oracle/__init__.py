@@ -9,6 +9,7 @@ vectors produced by the reference's own code that pin it.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import subprocess
 from pathlib import Path
 
@@ -25,11 +26,27 @@ def build() -> Path:
     return LIB
 
 
-def build_reference(ref_root: str = "/root/reference") -> Path | None:
+def reference_root() -> Path | None:
+    """The reference source tree used by the checker builds: the environment
+    variable ALB_REFERENCE_ROOT, else the default of oracle/Makefile.ref;
+    None when no reference tree is there (e.g. on a machine that only runs
+    the prebuilt checker)."""
+    root = os.environ.get("ALB_REFERENCE_ROOT")
+    if not root:
+        r = subprocess.run(["make", "-s", "-f", str(HERE / "Makefile.ref"), "print-ref"],
+                           capture_output=True, text=True)
+        root = r.stdout.strip() if r.returncode == 0 else ""
+    if root and Path(root, "bfs", "src", "bfs_ref.h").exists():
+        return Path(root)
+    return None
+
+
+def build_reference(ref_root: str | os.PathLike | None = None) -> Path | None:
     """Compile the reference's own sources + harness into oracle/_ref (if present)."""
-    if not Path(ref_root, "bfs", "src", "bfs_ref.h").exists():
+    root = Path(ref_root) if ref_root else reference_root()
+    if root is None or not Path(root, "bfs", "src", "bfs_ref.h").exists():
         return None
-    subprocess.run(["make", "-s", "-f", str(HERE / "Makefile.ref"), f"REF={ref_root}"], check=True)
+    subprocess.run(["make", "-s", "-f", str(HERE / "Makefile.ref"), f"REF={root}"], check=True)
     return REF_LIB
 
 

@@ -15,7 +15,8 @@ import oracle
 from conftest import ROOT
 
 PLUGIN = ROOT / "albba_gb300" / "libbfs_gb300.so"
-REF_SRC = Path("/root/reference/bfs/src")
+_REF_ROOT = oracle.reference_root()
+REF_SRC = (_REF_ROOT / "bfs" / "src") if _REF_ROOT else Path("/nonexistent")
 
 
 class SparseMatrixCSR(C.Structure):
