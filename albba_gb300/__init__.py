@@ -112,6 +112,10 @@ _sigs = {
     "alb_version": (C.c_char_p, []),
     "alb_graph_create": (C.c_int32, [C.c_int64, _P, _P, C.c_uint32, C.POINTER(_P)]),
     "alb_graph_create32": (C.c_int32, [C.c_int32, _P, _P, C.c_uint32, C.POINTER(_P)]),
+    "alb_graph_create_undirected": (C.c_int32, [C.c_int64, _P, _P, C.POINTER(_P)]),
+    "alb_graph_load": (C.c_int32, [C.c_char_p, C.POINTER(_P)]),
+    "alb_graph_export_csr": (C.c_int32, [_P, C.c_int32, _P, _P]),
+    "alb_graph_is_symmetric": (C.c_int32, [_P, _i32p]),
     "alb_graph_destroy": (None, [_P]),
     "alb_graph_info": (C.c_int32, [_P, _i64p, _i64p]),
     "alb_graph_set_stream": (C.c_int32, [_P, _P]),
@@ -344,6 +348,46 @@ class Graph:
         check(_lib.alb_graph_create32(n, rp.ctypes.data, cc.ctypes.data, flags, C.byref(g._h)))
         g.n, g.nnz = n, int(rp[-1])
         return g
+
+    @classmethod
+    def _from_handle(cls, h: C.c_void_p) -> "Graph":
+        g = cls.__new__(cls)
+        g._h = h
+        n, nnz = C.c_int64(), C.c_int64()
+        check(_lib.alb_graph_info(h, C.byref(n), C.byref(nnz)))
+        g.n, g.nnz = n.value, nnz.value
+        return g
+
+    @classmethod
+    def undirected(cls, csr: Csr) -> "Graph":
+        """The reference driver's undirected graph of csr, built on the device."""
+        h = _P()
+        rp = np.ascontiguousarray(csr.rowptr, dtype=np.int64)
+        col = np.ascontiguousarray(csr.col, dtype=np.int32)
+        check(_lib.alb_graph_create_undirected(csr.n, rp.ctypes.data, col.ctypes.data,
+                                               C.byref(h)))
+        return cls._from_handle(h)
+
+    @classmethod
+    def load(cls, path: str | os.PathLike) -> "Graph":
+        """A .cbd or .mtx file as the reference driver loads it, onto the device."""
+        h = _P()
+        check(_lib.alb_graph_load(str(path).encode(), C.byref(h)))
+        return cls._from_handle(h)
+
+    def export_csr(self, side: int = 0) -> Csr:
+        """The device CSR (side 0: pull side, 1: push side) copied to the host."""
+        rp = np.empty(self.n + 1, np.int64)
+        check(_lib.alb_graph_export_csr(self._h, side, rp.ctypes.data, None))
+        col = np.empty(max(int(rp[-1]), 1), np.int32)
+        check(_lib.alb_graph_export_csr(self._h, side, None, col.ctypes.data))
+        return Csr(rp, col[: int(rp[-1])])
+
+    @property
+    def symmetric(self) -> bool:
+        s = C.c_int32()
+        check(_lib.alb_graph_is_symmetric(self._h, C.byref(s)))
+        return bool(s.value)
 
     def close(self) -> None:
         if getattr(self, "_h", None) and self._h.value:

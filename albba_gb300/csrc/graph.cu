@@ -22,7 +22,9 @@
 #include <new>
 #include <vector>
 
+#include "albba_gen.h"
 #include "graph.h"
+#include "ingest.h"
 #include "scan.cuh"
 
 #ifdef _OPENMP
@@ -118,55 +120,7 @@ int resident_blocks(const void *func, int block) {
 
 namespace {
 
-// ------------------------------------------------------------ host prep
-
-bool rows_sorted(int64_t n, const int64_t *rp, const int32_t *col) {
-    int bad = 0;
-#pragma omp parallel for schedule(dynamic, 4096) reduction(| : bad)
-    for (int64_t r = 0; r < n; r++)
-        for (int64_t e = rp[r] + 1; e < rp[r + 1]; e++)
-            if (col[e - 1] > col[e]) {
-                bad = 1;
-                break;
-            }
-    return !bad;
-}
-
-alb_status validate_csr(int64_t n, const int64_t *rp, const int32_t *col) {
-    if (rp[0] != 0) return fail(ALB_ERR_INVALID, "rowptr[0] must be 0");
-    int bad = 0;
-#pragma omp parallel for schedule(static) reduction(| : bad)
-    for (int64_t r = 0; r < n; r++)
-        if (rp[r + 1] < rp[r]) bad |= 1;
-    if (bad) return fail(ALB_ERR_INVALID, "rowptr must be non-decreasing");
-    const int64_t nnz = rp[n];
-#pragma omp parallel for schedule(static) reduction(| : bad)
-    for (int64_t e = 0; e < nnz; e++)
-        if (col[e] < 0 || col[e] >= n) bad |= 1;
-    if (bad) return fail(ALB_ERR_INVALID, "column index outside [0, n)");
-    return ALB_OK;
-}
-
-// Copy of a CSR with every row sorted ascending.
-void sorted_copy(int64_t n, const int64_t *rp, const int32_t *col, std::vector<int32_t> &out) {
-    out.assign(col, col + rp[n]);
-#pragma omp parallel for schedule(dynamic, 1024)
-    for (int64_t r = 0; r < n; r++) std::sort(out.begin() + rp[r], out.begin() + rp[r + 1]);
-}
-
-// Transpose by counting; iterating source rows in order leaves every
-// transposed row ascending.
-void transpose(int64_t n, const int64_t *rp, const int32_t *col, std::vector<int64_t> &trp,
-               std::vector<int32_t> &tcol) {
-    const int64_t nnz = rp[n];
-    trp.assign((size_t)n + 1, 0);
-    for (int64_t e = 0; e < nnz; e++) trp[(size_t)col[e] + 1]++;
-    for (int64_t i = 0; i < n; i++) trp[i + 1] += trp[i];
-    std::vector<int64_t> cur(trp.begin(), trp.end() - 1);
-    tcol.resize((size_t)nnz);
-    for (int64_t r = 0; r < n; r++)
-        for (int64_t e = rp[r]; e < rp[r + 1]; e++) tcol[cur[col[e]]++] = (int32_t)r;
-}
+// ------------------------------------------------------------ ingest
 
 alb_status upload(int64_t n, const int64_t *rp, const int32_t *col, int64_t **d_rp,
                   int32_t **d_col, cudaStream_t st) {
@@ -194,18 +148,12 @@ void free_sell(Sell &s) {
     s = Sell();
 }
 
-alb_status create_impl(int64_t n, const int64_t *rowptr, const int32_t *col, uint32_t flags,
-                       alb_graph **out) {
-    ALB_TRY(validate_csr(n, rowptr, col));
+alb_status graph_shell(int64_t n, alb_graph **out) {
     int dev = 0;
     ALB_CK(cudaGetDevice(&dev));
     alb_graph *g = new alb_graph();
     g->device = dev;
     g->n = n;
-    auto cleanup = [&](alb_status s) {
-        alb_graph_destroy(g);
-        return s;
-    };
     cudaError_t e = cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->own_stream, cudaStreamNonBlocking);
     g->stream = g->own_stream;
@@ -213,46 +161,73 @@ alb_status create_impl(int64_t n, const int64_t *rowptr, const int32_t *col, uin
     if (e == cudaSuccess) e = cudaEventCreate(&g->ev1);
     if (e != cudaSuccess) {
         cudaGetLastError();
-        return cleanup(fail(ALB_ERR_CUDA, "stream/event setup: %s", cudaGetErrorString(e)));
+        alb_graph_destroy(g);
+        return fail(ALB_ERR_CUDA, "stream/event setup: %s", cudaGetErrorString(e));
     }
-    const bool sorted = (flags & ALB_CSR_SORTED) || rows_sorted(n, rowptr, col);
-    std::vector<int32_t> scol;
-    const int32_t *given = col;
-    if (!sorted) {
-        sorted_copy(n, rowptr, col, scol);
-        given = scol.data();
-    }
-    alb_status st = ALB_OK;
+    *out = g;
+    return ALB_OK;
+}
+
+// Takes a CSR already on the device (d_rp, d_col: dmalloc'ed, owned by g from
+// here on) to the traversal's shape: checked, rows ascending, and both
+// orientations (the transpose made on the device unless the caller declared
+// the matrix symmetric; a transpose equal to the matrix is dropped).
+alb_status finish_device_csr(alb_graph *g, int64_t *d_rp, int32_t *d_col, int64_t nnz,
+                             uint32_t flags) {
+    g->rp_in = g->rp_out = d_rp;
+    g->col_in = g->col_out = d_col;
+    g->nnz_in = g->nnz_out = nnz;
+    bool sorted = true;
+    ALB_TRY(csr_check(g->n, d_rp, d_col, nnz, g->stream, &sorted));
+    if (!sorted) ALB_TRY(sort_rows(g->n, d_rp, d_col, nnz, g->stream));
     if (flags & ALB_CSR_SYMMETRIC) {
         g->symmetric = true;
-        st = upload(n, rowptr, given, &g->rp_in, &g->col_in, g->stream);
-        g->rp_out = g->rp_in;
-        g->col_out = g->col_in;
-        g->nnz_in = g->nnz_out = rowptr[n];
+        return ALB_OK;
+    }
+    int64_t *trp = nullptr;
+    int32_t *tcol = nullptr;
+    ALB_TRY(transpose(g->n, d_rp, d_col, nnz, &trp, &tcol, g->stream));
+    bool same = false;
+    alb_status s = csr_equal(g->n, d_rp, d_col, trp, tcol, nnz, g->stream, &same);
+    if (s != ALB_OK || same) {
+        dfree(trp);
+        dfree(tcol);
+        g->symmetric = same;
+        return s;
+    }
+    if (flags & ALB_CSR_IN) {
+        g->rp_out = trp;
+        g->col_out = tcol;
     } else {
-        std::vector<int64_t> trp;
-        std::vector<int32_t> tcol;
-        transpose(n, rowptr, given, trp, tcol);
-        const bool given_is_in = (flags & ALB_CSR_IN) != 0;
-        const int64_t *rin = given_is_in ? rowptr : trp.data();
-        const int32_t *cin = given_is_in ? given : tcol.data();
-        const int64_t *rout = given_is_in ? trp.data() : rowptr;
-        const int32_t *cout = given_is_in ? tcol.data() : given;
-        st = upload(n, rin, cin, &g->rp_in, &g->col_in, g->stream);
-        if (st == ALB_OK) st = upload(n, rout, cout, &g->rp_out, &g->col_out, g->stream);
-        g->nnz_in = g->nnz_out = rowptr[n];
-        if (st == ALB_OK) {
-            // host vectors die at scope exit: finish the copies first
-            cudaError_t se = cudaStreamSynchronize(g->stream);
-            if (se != cudaSuccess)
-                st = fail(ALB_ERR_CUDA, "upload: %s", cudaGetErrorString(se));
-        }
+        g->rp_in = trp;
+        g->col_in = tcol;
+    }
+    return ALB_OK;
+}
+
+alb_status create_impl(int64_t n, const int64_t *rowptr, const int32_t *col, uint32_t flags,
+                       alb_graph **out) {
+    if (rowptr[0] != 0 || rowptr[n] < 0)
+        return fail(ALB_ERR_INVALID, "row offsets must start at 0 and end at nnz >= 0");
+    alb_graph *g = nullptr;
+    ALB_TRY(graph_shell(n, &g));
+    int64_t *d_rp = nullptr;
+    int32_t *d_col = nullptr;
+    alb_status st = upload(n, rowptr, col, &d_rp, &d_col, g->stream);
+    if (st == ALB_OK) {
+        st = finish_device_csr(g, d_rp, d_col, rowptr[n], flags);
+    } else {
+        dfree(d_rp);
+        dfree(d_col);
     }
     if (st == ALB_OK) {
         cudaError_t se = cudaStreamSynchronize(g->stream);
         if (se != cudaSuccess) st = fail(ALB_ERR_CUDA, "upload: %s", cudaGetErrorString(se));
     }
-    if (st != ALB_OK) return cleanup(st);
+    if (st != ALB_OK) {
+        alb_graph_destroy(g);
+        return st;
+    }
     *out = g;
     return ALB_OK;
 }
@@ -877,6 +852,88 @@ alb_status alb_graph_create32(int32_t n, const int32_t *rowptr, const int32_t *c
     } catch (const std::bad_alloc &) {
         return fail(ALB_ERR_OOM, "alb_graph_create32: host allocation failed");
     }
+}
+
+alb_status alb_graph_create_undirected(int64_t n, const int64_t *rowptr, const int32_t *col,
+                                       alb_graph **out) {
+    if (!out) return fail(ALB_ERR_INVALID, "alb_graph_create_undirected: out is NULL");
+    *out = nullptr;
+    if (n <= 0 || n > INT32_MAX || !rowptr || (!col && rowptr[n] > 0))
+        return fail(ALB_ERR_INVALID, "alb_graph_create_undirected: bad arguments");
+    if (rowptr[0] != 0 || rowptr[n] < 0)
+        return fail(ALB_ERR_INVALID, "row offsets must start at 0 and end at nnz >= 0");
+    alb_graph *g = nullptr;
+    ALB_TRY(graph_shell(n, &g));
+    int64_t *d_rp = nullptr, *d_urp = nullptr;
+    int32_t *d_col = nullptr, *d_ucol = nullptr;
+    const int64_t nnz = rowptr[n];
+    int64_t unnz = 0;
+    alb_status st = upload(n, rowptr, col, &d_rp, &d_col, g->stream);
+    bool sorted = true;
+    if (st == ALB_OK) st = csr_check(n, d_rp, d_col, nnz, g->stream, &sorted);
+    if (st == ALB_OK) st = merge_undirected(n, d_rp, d_col, nnz, &d_urp, &d_ucol, &unnz, g->stream);
+    dfree(d_rp);
+    dfree(d_col);
+    if (st == ALB_OK) st = finish_device_csr(g, d_urp, d_ucol, unnz, ALB_CSR_SYMMETRIC);
+    else {
+        dfree(d_urp);
+        dfree(d_ucol);
+    }
+    if (st != ALB_OK) {
+        alb_graph_destroy(g);
+        return st;
+    }
+    *out = g;
+    return ALB_OK;
+}
+
+alb_status alb_graph_load(const char *path, alb_graph **out) {
+    if (!path || !out) return fail(ALB_ERR_INVALID, "alb_graph_load: bad arguments");
+    *out = nullptr;
+    const size_t len = std::strlen(path);
+    auto ends = [&](const char *ext) { return len >= 4 && std::strcmp(path + len - 4, ext) == 0; };
+    alb_host_csr h;
+    std::memset(&h, 0, sizeof(h));
+    int32_t sym = 1;
+    alb_status st;
+    if (ends(".cbd")) st = alb_cbd_read(path, &h);
+    else if (ends(".mtx")) st = alb_mtx_read(path, &h, &sym);
+    else return fail(ALB_ERR_UNSUPPORTED, "alb_graph_load: %s is neither .mtx nor .cbd", path);
+    if (st != ALB_OK) return st;
+    if (h.n <= 0) {
+        alb_host_csr_free(&h);
+        return fail(ALB_ERR_IO, "alb_graph_load: %s holds no vertices", path);
+    }
+    // a .cbd file is taken as the reference takes it (its CSR as is, rows
+    // and their transpose on the device); a non-symmetric .mtx becomes the
+    // reference driver's undirected graph
+    if (ends(".mtx") && !sym) st = alb_graph_create_undirected(h.n, h.rowptr, h.col, out);
+    else st = alb_graph_create(h.n, h.rowptr, h.col, ends(".mtx") ? ALB_CSR_SYMMETRIC : ALB_CSR_IN, out);
+    alb_host_csr_free(&h);
+    return st;
+}
+
+alb_status alb_graph_export_csr(const alb_graph *g, int32_t side, int64_t *rowptr, int32_t *col) {
+    if (!g || (side != 0 && side != 1))
+        return fail(ALB_ERR_INVALID, "alb_graph_export_csr: bad arguments");
+    ALB_CK(cudaSetDevice(g->device));
+    const int64_t *rp = side == 0 ? g->rp_in : g->rp_out;
+    const int32_t *cl = side == 0 ? g->col_in : g->col_out;
+    const int64_t nnz = side == 0 ? g->nnz_in : g->nnz_out;
+    if (rowptr)
+        ALB_CK(cudaMemcpyAsync(rowptr, rp, sizeof(int64_t) * (size_t)(g->n + 1),
+                               cudaMemcpyDeviceToHost, g->stream));
+    if (col && nnz > 0)
+        ALB_CK(cudaMemcpyAsync(col, cl, sizeof(int32_t) * (size_t)nnz, cudaMemcpyDeviceToHost,
+                               g->stream));
+    ALB_CK(cudaStreamSynchronize(g->stream));
+    return ALB_OK;
+}
+
+alb_status alb_graph_is_symmetric(const alb_graph *g, int32_t *symmetric) {
+    if (!g || !symmetric) return fail(ALB_ERR_INVALID, "alb_graph_is_symmetric: bad arguments");
+    *symmetric = g->symmetric ? 1 : 0;
+    return ALB_OK;
 }
 
 void alb_graph_destroy(alb_graph *g) {

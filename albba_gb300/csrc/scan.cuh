@@ -41,7 +41,7 @@ __global__ void k_scan_tile_sums(const Tin *in, int64_t count, int64_t *bsum) {
     if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
 }
 
-__global__ void k_scan_tile_offsets(int64_t *bsum, int64_t ntiles, int64_t *grand_total) {
+static __global__ void k_scan_tile_offsets(int64_t *bsum, int64_t ntiles, int64_t *grand_total) {
     __shared__ int64_t tot;
     int64_t carry = 0;
     for (int64_t b = 0; b < ntiles; b += kScanThreads) {

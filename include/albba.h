@@ -73,9 +73,34 @@ alb_status alb_graph_create(int64_t n, const int64_t *rowptr, const int32_t *col
 /* Same, from the reference's int32 CSR (bfs/src/sparse_matrix.h:18-28). */
 alb_status alb_graph_create32(int32_t n, const int32_t *rowptr, const int32_t *col,
                               uint32_t flags, alb_graph **out);
+/* Every O(nnz) step of graph creation runs on the device: the CSR is copied
+ * as given, then checked there (offsets from 0 to nnz, never decreasing;
+ * columns in [0, n): ALB_ERR_INVALID otherwise), rows sorted ascending when
+ * they are not, and -- unless ALB_CSR_SYMMETRIC -- transposed (rows of the
+ * transpose ascending, as the reference's counting transpose leaves them,
+ * bfs/src/sparse_matrix.c:230-290); a transpose equal to the matrix is
+ * dropped and the graph marked symmetric. */
+
+/* The reference driver's undirected graph of a non-symmetric input
+ * (bfs/src/main.c:127-163), built on the device: row i = MergeArr(column i of
+ * A, row i of A as given) (bfs/src/utils.c:351-379). Host CSR in (rows in
+ * any order, duplicates kept); the graph is symmetric, rows sorted. */
+alb_status alb_graph_create_undirected(int64_t n, const int64_t *rowptr, const int32_t *col,
+                                       alb_graph **out);
+/* Graph load of the reference driver (bfs/src/main.c:86-163) onto the
+ * device: .cbd files (bfs/src/biio.h:21-149) as is (ALB_CSR_IN: the
+ * reference's working matrix), .mtx files parsed on the host, then on the
+ * device either taken as symmetric or made undirected as above. */
+alb_status alb_graph_load(const char *path, alb_graph **out);
 void alb_graph_destroy(alb_graph *g);
 
 alb_status alb_graph_info(const alb_graph *g, int64_t *n, int64_t *nnz);
+/* Copy the device CSR to host buffers: side 0 = pull side (row v lists v's
+ * sources), 1 = push side (row u lists u's targets); rowptr[n+1], col[nnz]
+ * (either may be NULL). Rows are ascending. */
+alb_status alb_graph_export_csr(const alb_graph *g, int32_t side, int64_t *rowptr, int32_t *col);
+/* *symmetric = 1 when one CSR serves both sides (declared or detected). */
+alb_status alb_graph_is_symmetric(const alb_graph *g, int32_t *symmetric);
 
 /* Run the graph's work on a caller-provided cudaStream_t (NULL restores the
  * graph's own stream). Entry points still synchronise that stream before
