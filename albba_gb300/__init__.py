@@ -19,7 +19,10 @@ from pathlib import Path
 import numpy as np
 
 _PKG = Path(__file__).resolve().parent
-LIB_PATH = _PKG / "libalbba_gb300.so"
+# ALB_LIBRARY=checked loads the bounds-checked build (tests of the kernels'
+# index discipline); the default is the production library
+LIB_PATH = _PKG / ("libalbba_gb300_checked.so" if os.environ.get("ALB_LIBRARY") == "checked"
+                   else "libalbba_gb300.so")
 
 if not LIB_PATH.exists():
     raise ImportError(
@@ -90,7 +93,9 @@ class LevelRec(C.Structure):
     _fields_ = [("dir", C.c_int32), ("level", C.c_int32), ("nf", C.c_int64), ("mf", C.c_int64),
                 ("nu", C.c_int64), ("mu", C.c_int64), ("active_slices", C.c_int64),
                 ("t_ns", C.c_int64), ("bytes", C.c_int64), ("step_us", C.c_float),
-                ("pad_", C.c_int32)]
+                ("pad_", C.c_int32), ("words_bypassed", C.c_int64), ("rows_scanned", C.c_int64),
+                ("groups_read", C.c_int64), ("groups_bypassed", C.c_int64),
+                ("edges_bypassed", C.c_int64)]
 
 
 class LevelProfile(C.Structure):
@@ -128,6 +133,7 @@ _sigs = {
     "alb_bfs_device": (C.c_int32, [_P, C.c_int32, C.POINTER(BfsOpts), _P, _P, C.POINTER(Stats)]),
     "alb_level_trace": (C.c_int32, [_P, C.c_int32, C.POINTER(LevelRec), _i32p]),
     "alb_debug_fail_alloc_after": (None, [C.c_int32]),
+    "alb_debug_device_waits": (None, [C.c_int32, C.c_int32, C.c_int32, C.c_int64]),
     "alb_gen_rmat": (C.c_int32, [C.c_int32, C.c_int32, C.c_uint64, C.c_double, C.c_double,
                                  C.c_double, C.c_int32, C.POINTER(HostCsr)]),
     "alb_gen_grid": (C.c_int32, [C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_uint64,
@@ -162,6 +168,11 @@ _sigs = {
     "alb_worklist_run_device": (C.c_int32, [_P, C.c_int32, _P, C.POINTER(Stats)]),
     "alb_selector_load": (C.c_int32, [C.c_int32, _P]),
     "alb_selector_clear": (C.c_int32, [C.c_int32]),
+    "alb_sellmat_create": (C.c_int32, [C.c_int64, _P, _P, _P, C.c_int32, C.POINTER(_P)]),
+    "alb_sellmat_destroy": (None, [_P]),
+    "alb_sellmat_info": (C.c_int32, [_P, _i64p, _i64p, _i64p]),
+    "alb_sellmat_spmv": (C.c_int32, [_P, _P, _P, C.POINTER(C.c_float)]),
+    "alb_sellmat_spmv_host": (C.c_int32, [_P, _P, _P]),
 }
 for _name, (_res, _args) in _sigs.items():
     _f = getattr(_lib, _name)
@@ -502,6 +513,48 @@ class Graph:
         return list(buf[: cnt.value])
 
 
+class SellMatrix:
+    """fp64 SELL-C-sigma matrix on the current device (y = A x)."""
+
+    def __init__(self, rowptr, col, values, sigma: int = 1024):
+        self._h = _P()
+        rp = np.ascontiguousarray(rowptr, dtype=np.int64)
+        cl = np.ascontiguousarray(col, dtype=np.int32)
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        self.n = rp.shape[0] - 1
+        check(_lib.alb_sellmat_create(self.n, rp.ctypes.data, cl.ctypes.data, v.ctypes.data,
+                                      sigma, C.byref(self._h)))
+        nnz, stored = C.c_int64(), C.c_int64()
+        check(_lib.alb_sellmat_info(self._h, None, C.byref(nnz), C.byref(stored)))
+        self.nnz, self.stored = nnz.value, stored.value
+
+    def spmv(self, x) -> np.ndarray:
+        xx = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty(self.n, np.float64)
+        check(_lib.alb_sellmat_spmv_host(self._h, xx.ctypes.data, y.ctypes.data))
+        return y
+
+    def spmv_device(self, d_x, d_y) -> float:
+        """Device vectors (torch tensors or pointers); returns the kernel's microseconds."""
+        us = C.c_float()
+        check(_lib.alb_sellmat_spmv(self._h, _ptr(d_x), _ptr(d_y), C.byref(us)))
+        return us.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            _lib.alb_sellmat_destroy(self._h)
+            self._h = _P()
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
 class Worklist:
     """Persistent multi-graph BFS (alb_worklist_*). Keeps its graphs alive."""
 
@@ -604,3 +657,10 @@ def selector_clear(which: int) -> None:
 
 def debug_fail_alloc_after(k: int) -> None:
     _lib.alb_debug_fail_alloc_after(k)
+
+
+def debug_device_waits(withhold_level: int = -1, withhold_block: int = 0, short_bulk: bool = False,
+                       timeout_us: int = 0) -> None:
+    """Test hooks of the bounded device waits (alb_debug_device_waits);
+    no arguments: all off."""
+    _lib.alb_debug_device_waits(withhold_level, withhold_block, 1 if short_bulk else 0, timeout_us)

@@ -55,11 +55,14 @@ def _run(cmd: list[str]) -> None:
         sys.stderr.write(r.stdout)
 
 
-def _compile_cmd(src: Path, obj: Path, cuda: Path) -> list[str]:
+CHECKED_LIB = PKG / "libalbba_gb300_checked.so"
+
+
+def _compile_cmd(src: Path, obj: Path, cuda: Path, defs: tuple[str, ...] = ()) -> list[str]:
     inc = [f"-I{INCLUDE}", f"-I{CSRC}"]
     if src.suffix == ".cu":
         return [str(cuda / "bin" / "nvcc"), *ARCH, "-O3", "-lineinfo", "-std=c++17",
-                "-Xcompiler", "-fPIC,-fopenmp,-Wall", "--expt-relaxed-constexpr",
+                "-Xcompiler", "-fPIC,-fopenmp,-Wall", "--expt-relaxed-constexpr", *defs,
                 *inc, "-c", str(src), "-o", str(obj)]
     if src.suffix == ".cpp":
         return ["g++", "-O3", "-std=c++17", "-fPIC", "-fopenmp", "-Wall",
@@ -68,27 +71,35 @@ def _compile_cmd(src: Path, obj: Path, cuda: Path) -> list[str]:
     return ["gcc", "-O2", "-std=c11", "-fPIC", "-Wall", *inc, "-c", str(src), "-o", str(obj)]
 
 
-def build_library(jobs: int | None = None) -> Path:
-    """Compile and link libalbba_gb300.so and libbfs_gb300.so; return the former."""
+def build_library(jobs: int | None = None, checked: bool = False) -> Path:
+    """Compile and link libalbba_gb300.so and libbfs_gb300.so; return the former.
+    checked=True: the bounds-checked variant libalbba_gb300_checked.so
+    (-DALB_CHECKED: every vertex id a traversal kernel loads is checked
+    before use and a bad one reported as ALB_ERR_DEVICE), objects apart."""
     cuda = _cuda_home()
-    BUILD.mkdir(exist_ok=True)
+    bdir = BUILD / "checked" if checked else BUILD
+    bdir.mkdir(parents=True, exist_ok=True)
+    lib = CHECKED_LIB if checked else LIB
+    defs = ("-DALB_CHECKED",) if checked else ()
     hdrs = _headers()
     srcs = sorted(list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cpp")))
     plugin_src = CSRC / "bfs_plugin.c"
     todo = []
     objs = []
-    for s in srcs + ([plugin_src] if plugin_src.exists() else []):
-        o = BUILD / (s.name + ".o")
+    for s in srcs + ([plugin_src] if plugin_src.exists() and not checked else []):
+        o = bdir / (s.name + ".o")
         if s != plugin_src:
             objs.append(o)
         if _stale(o, [s, *hdrs]):
             todo.append((s, o))
     jobs = jobs or min(len(todo) or 1, os.cpu_count() or 4)
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
-        list(ex.map(lambda so: _run(_compile_cmd(so[0], so[1], cuda)), todo))
-    if _stale(LIB, objs):
-        _run([str(cuda / "bin" / "nvcc"), *ARCH, "-shared", "-o", str(LIB), *map(str, objs),
+        list(ex.map(lambda so: _run(_compile_cmd(so[0], so[1], cuda, defs)), todo))
+    if _stale(lib, objs):
+        _run([str(cuda / "bin" / "nvcc"), *ARCH, "-shared", "-o", str(lib), *map(str, objs),
               "-Xcompiler", "-fopenmp", "-lgomp"])
+    if checked:
+        return lib
     if plugin_src.exists():
         pobj = BUILD / (plugin_src.name + ".o")
         if _stale(PLUGIN, [pobj, LIB]):

@@ -87,6 +87,8 @@ __device__ void record_trace(const BfsArgs &a, const BfsCtl &c, int dir) {
         r.bytes = 0;
         r.step_us = -1.0f;
         r.pad_ = 0;
+        r.words_bypassed = r.rows_scanned = r.groups_read = r.groups_bypassed = 0;
+        r.edges_bypassed = 0;
         a.trace[c.level] = r;
     }
 }
@@ -120,9 +122,17 @@ __device__ void prep_phase(const BfsArgs &a, int L, bool compact, bool zero_next
         while (word) {
             int b = __ffs(word) - 1;
             word &= word - 1;
-            Q[pos++] = (int32_t)(w * 32 + b);
+            if (ALB_CHECK_POS(pos, a.n, &a.ctl->err)) Q[pos] = (int32_t)(w * 32 + b);
+            pos++;
         }
     }
+}
+
+// Adds a warp's count of bypass statistic `which` to level L's slot (all 32
+// lanes call it).
+__device__ __forceinline__ void add_stat(const BfsArgs &a, int L, int which, unsigned long long v) {
+    v = warp_sum(v);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(&a.ctl->acc_stat[(L + 1) % 3][which], v);
 }
 
 // Pushed edges u -> v (u's original id ou): the smallest source wins the
@@ -134,7 +144,8 @@ __device__ void prep_phase(const BfsArgs &a, int L, bool compact, bool zero_next
 // targets together, then the atomics, so one lane keeps four loads in
 // flight where one edge at a time kept one.
 __device__ __forceinline__ void push_edges4(const BfsArgs &a, uint32_t *N, const int32_t (&v)[4],
-                                            const uint32_t (&ou)[4], bool persist) {
+                                            const uint32_t (&ou)[4], bool persist,
+                                            unsigned &bypassed) {
     bool live[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
@@ -142,6 +153,7 @@ __device__ __forceinline__ void push_edges4(const BfsArgs &a, uint32_t *N, const
         if (v[k] >= 0) {
             const uint32_t w = persist ? __ldcg(a.vis + (v[k] >> 5)) : __ldg(a.vis + (v[k] >> 5));
             live[k] = !((w >> (v[k] & 31)) & 1u);
+            bypassed += !live[k];
         }
     }
     // read before writing: a hub target receives thousands of pushes in one
@@ -195,9 +207,11 @@ __device__ void td_phase(const BfsArgs &a, int L, Range r) {
     const int64_t nwarps = (int64_t)r.nblk * wpb;
     const int G = rows_per_warp(qlen, nwarps);
     const int64_t stride = nwarps * G;
+    unsigned bypassed = 0;
     for (int64_t cb = gw * G; cb < qlen; cb += stride) {
         const int64_t i = cb + lane;
         int32_t u = (lane < G && i < qlen) ? ld_state<kPersist>(Q + i) : -1;
+        if (u >= 0) ALB_CHECK_ID(u, a.n, -1, &a.ctl->err);
         int64_t st = 0, d = 0;
         int32_t ou = 0;
         if (u >= 0) {
@@ -233,13 +247,15 @@ __device__ void td_phase(const BfsArgs &a, int L, Range r) {
                     for (int step = 16; step > 0; step >>= 1)
                         if (s_ex[wib][j + step] <= e) j += step;
                     v[k] = __ldg(a.pcol + s_st[wib][j] + (e - s_ex[wib][j]));
+                    ALB_CHECK_ID(v[k], a.n, -1, &a.ctl->err);
                     ou4[k] = (uint32_t)s_ou[wib][j];
                 }
             }
-            push_edges4(a, N, v, ou4, kPersist);
+            push_edges4(a, N, v, ou4, kPersist, bypassed);
         }
         __syncwarp();
     }
+    add_stat(a, L, kStEdgesBypassed, bypassed);
 }
 
 // Long frontier rows, kBigChunk edges per chunk, chunks spread over all
@@ -259,7 +275,11 @@ __device__ void td_big_phase(const BfsArgs &a, int L, Range r) {
     const int64_t nwarps = (int64_t)r.nblk * wpb;
     const int64_t per = (total + nwarps - 1) / nwarps;
     const int64_t k0 = gw * per, k1 = min(total, k0 + per);
-    if (k0 >= k1) return;
+    unsigned bypassed = 0;
+    if (k0 >= k1) {
+        add_stat(a, L, kStEdgesBypassed, bypassed);  // keeps every lane at the shuffle
+        return;
+    }
     int64_t lo = 0, hi = nbig - 1;
     while (lo < hi) {
         const int64_t mid = (lo + hi + 1) >> 1;
@@ -290,10 +310,12 @@ __device__ void td_big_phase(const BfsArgs &a, int L, Range r) {
         for (int q = 0; q < 4; q++) {
             const int64_t e = c * kBigChunk + 32 * q + lane;
             v[q] = e < e1 ? __ldg(a.pcol + st + e) : -1;
+            if (v[q] >= 0) ALB_CHECK_ID(v[q], a.n, -1, &a.ctl->err);
             ou4[q] = ou;
         }
-        push_edges4(a, N, v, ou4, kPersist);
+        push_edges4(a, N, v, ou4, kPersist, bypassed);
     }
+    add_stat(a, L, kStEdgesBypassed, bypassed);
 }
 
 // After a top-down level: clear the old frontier over its queue; compact the
@@ -336,7 +358,8 @@ __device__ void td_finish_phase(const BfsArgs &a, int L, Range r) {
             const int b = __ffs(m) - 1;
             m &= m - 1;
             const int32_t v = (int32_t)(w * 32 + b);
-            NQ[pos++] = v;
+            if (ALB_CHECK_POS(pos, a.n, &a.ctl->err)) NQ[pos] = v;
+            pos++;
             a.level_pos[v] = lvl;
             cn++;
             cmo += (unsigned long long)__ldg(a.odeg + v);
@@ -382,6 +405,7 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r, const uint32_t *Fs = 
     const int32_t lvl = L + 1;
     unsigned cn = 0, full = 0;
     unsigned long long cmo = 0, cmi = 0, bytes = 0;
+    unsigned n_wbyp = 0, n_rows = 0, n_grp = 0, n_gtot = 0;
     const uint64_t pol = l2_evict_first();
     // words come in runs from the level's counter; the next word's visited
     // mask is requested one iteration ahead (only the warp that takes a word
@@ -390,28 +414,64 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r, const uint32_t *Fs = 
     unsigned long long *ctr = &a.ctl->work[L % 3];
     WordRuns runs;
     int64_t w = runs.first(ctr, a.nwords);
-    uint32_t vis_next = w < a.nwords ? ld_bits<kPersist>(a.vis + w) : kFull;
+    // A word's visited mask and slice geometry are requested one word ahead,
+    // and its first column group as soon as they are in, while the word
+    // before it is processed: a word starts with its columns at hand rather
+    // than three dependent round trips behind. (Only the warp that takes a
+    // word writes its visited mask during the level.)
+    auto geometry = [&](int64_t ww, uint32_t &vv, int32_t &wdv, int64_t &sov) {
+        vv = kFull;
+        wdv = 0;
+        sov = 0;
+        if (ww < a.nwords) {
+            vv = ld_bits<kPersist>(a.vis + ww);
+            const int32_t pw = (int32_t)(ww * 32 + lane);
+            // rows past n are preset visited; clamp their slice index
+            const int64_t sw = (int64_t)(pw < a.n ? pw : a.n - 1) >> log2C;
+            wdv = __ldg(a.width + sw);
+            sov = __ldg(a.slice_off + sw);
+        }
+    };
+    auto first_group = [&](int64_t ww, uint32_t vv, int32_t wdv, int64_t sov) {
+        const int32_t pw = (int32_t)(ww * 32 + lane);
+        int4 g0 = make_int4(pw, pw, pw, pw);
+        if (ww < a.nwords && !(kBypass && vv == kFull) && !((vv >> lane) & 1u) && wdv > 0)
+            g0 = ld_stream(a.col4 + (sov >> 2) + (pw & (C - 1)), pol);
+        return g0;
+    };
+    uint32_t vis_c;
+    int32_t wd_c;
+    int64_t so_c;
+    geometry(w, vis_c, wd_c, so_c);
+    int4 f0 = first_group(w, vis_c, wd_c, so_c);
     for (int64_t wn; w < a.nwords; w = wn) {
-        const uint32_t vis = vis_next;
         wn = runs.after(w, ctr, a.nwords);
-        if (wn < a.nwords) vis_next = ld_bits<kPersist>(a.vis + wn);
+        uint32_t vis_n;
+        int32_t wd_n;
+        int64_t so_n;
+        geometry(wn, vis_n, wd_n, so_n);
+        const uint32_t vis = vis_c;
         if (kBypass && vis == kFull) {
-            if (lane == 0) N[w] = 0;
+            if (lane == 0) {
+                N[w] = 0;
+                n_wbyp++;
+            }
+            f0 = first_group(wn, vis_n, wd_n, so_n);
+            vis_c = vis_n;
+            wd_c = wd_n;
+            so_c = so_n;
             continue;
         }
         const int32_t p = (int32_t)(w * 32 + lane);
-        // rows past n are preset visited; clamp their slice index
-        const int64_t s = (int64_t)(p < a.n ? p : a.n - 1) >> log2C;
-        const int32_t wd = __ldg(a.width + s);
-        const int64_t so = __ldg(a.slice_off + s);
         bool active = !((vis >> lane) & 1u);
-        const int32_t ng = active ? (wd + 3) >> 2 : 0;
-        const int4 *cp = a.col4 + (so >> 2) + (p & (C - 1));
+        const int32_t ng = active ? (wd_c + 3) >> 2 : 0;
+        n_rows += ng > 0;
+        n_gtot += ng;
+        const int4 *cp = a.col4 + (so_c >> 2) + (p & (C - 1));
         int32_t found = -1;
         // group j+1 is requested before group j's frontier tests, so each lane
         // keeps one column load in flight while it waits on the bitmap
-        int4 c = make_int4(p, p, p, p);
-        if (active && ng > 0) c = ld_stream(cp, pol);
+        int4 c = f0;
         // an unvisited row whose first entry is padding is a long row (rows
         // without sources start visited): the long-row pass has run already
         const bool long_cand = active && c.x == p;
@@ -420,8 +480,10 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r, const uint32_t *Fs = 
             if (!__any_sync(kFull, active)) break;
             if (!active) continue;
             bytes += 32;  // four columns and the four frontier words they select
+            n_grp++;
             int4 nx = make_int4(p, p, p, p);
             if (j + 1 < ng) nx = ld_stream(cp + (int64_t)(j + 1) * C, pol);
+            ALB_CHECK_ID4(c, a.nwords * 32, p, &a.ctl->err);
             const uint32_t f0 = ld_front<kSmemF, kPersist>(F, c.x >> 5);
             const uint32_t f1 = ld_front<kSmemF, kPersist>(F, c.y >> 5);
             const uint32_t f2 = ld_front<kSmemF, kPersist>(F, c.z >> 5);
@@ -460,7 +522,15 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r, const uint32_t *Fs = 
             cmo += (unsigned long long)__ldg(a.odeg + p);
             cmi += (unsigned long long)__ldg(a.ideg + p);
         }
+        f0 = first_group(wn, vis_n, wd_n, so_n);
+        vis_c = vis_n;
+        wd_c = wd_n;
+        so_c = so_n;
     }
+    add_stat(a, L, kStWordsBypassed, n_wbyp);
+    add_stat(a, L, kStRowsScanned, n_rows);
+    add_stat(a, L, kStGroupsRead, n_grp);
+    add_stat(a, L, kStGroupsTotal, n_gtot);
     cn = warp_sum(cn);
     cmo = warp_sum(cmo);
     cmi = warp_sum(cmi);
@@ -502,6 +572,7 @@ __device__ __forceinline__ int32_t long_scan(const BfsArgs &a, const uint32_t *F
         for (int u = 0; u < 4; u++) {
             const int64_t e = e0 + 32 * u + lane;
             c[u] = e < en ? __ldg(a.lcol + e) : -1;
+            if (c[u] >= 0) ALB_CHECK_ID(c[u], a.n, -1, &a.ctl->err);
         }
 #pragma unroll
         for (int u = 0; u < 4; u++) f[u] = c[u] >= 0 ? ld_bits<kPersist>(F + (c[u] >> 5)) : 0u;
@@ -607,6 +678,17 @@ __host__ __device__ inline int64_t level_bytes(const BfsCtl &c, int dir, unsigne
     return (int64_t)counted + 12 * c.nwords;
 }
 
+// The level's bypass statistics (slot k) into its trace record.
+template <class Ctl>
+__device__ inline void write_stats(alb_level_rec &r, Ctl &c, int k) {
+    r.words_bypassed = (int64_t)c.acc_stat[k][kStWordsBypassed];
+    r.rows_scanned = (int64_t)c.acc_stat[k][kStRowsScanned];
+    r.groups_read = (int64_t)c.acc_stat[k][kStGroupsRead];
+    r.groups_bypassed =
+        (int64_t)c.acc_stat[k][kStGroupsTotal] - (int64_t)c.acc_stat[k][kStGroupsRead];
+    r.edges_bypassed = (int64_t)c.acc_stat[k][kStEdgesBypassed];
+}
+
 // Level rollover from the accumulators of slot (L+1)%3 (values read with
 // coherent loads by the caller).
 __host__ __device__ inline void roll(BfsCtl &c, int dir, unsigned long long nn,
@@ -628,7 +710,7 @@ __host__ __device__ inline void roll(BfsCtl &c, int dir, unsigned long long nn,
     else
         c.levels_bu++;
     c.level++;
-    if (nn == 0 || c.level >= c.level_cap) c.done = 1;
+    if (nn == 0 || c.level >= c.level_cap || c.err) c.done = 1;
 }
 
 // ---------------------------------------------------- standalone kernels
@@ -706,6 +788,7 @@ __global__ void k_decide(BfsArgs a, int forced, cudaGraphConditionalHandle sw) {
         a.ctl->acc_mi[k] = 0;
         a.ctl->acc_full[k] = 0;
         a.ctl->acc_bytes[k] = 0;
+        for (int i = 0; i < kStatN; i++) a.ctl->acc_stat[k][i] = 0;
         a.ctl->nbig[k] = 0;
         a.ctl->work[k] = 0;
         a.ctl->qn[k] = 0;
@@ -764,18 +847,19 @@ __global__ void __launch_bounds__(kBuSmemBlock, 1) k_bu_smem(BfsArgs a) {
     const uint32_t bytes = (uint32_t)(((a.nwords * 4) + 15) & ~15ll);
     if (threadIdx.x == 0) {
         mbar_init(&s_bar, 1);
-        mbar_expect_tx(&s_bar, bytes);
+        // (short_bulk: a test hook expecting bytes the copy never delivers)
+        mbar_expect_tx(&s_bar, bytes + (a.short_bulk ? 16u : 0u));
         bulk_g2s(s_front, F, bytes, &s_bar);
     }
     __syncthreads();  // the barrier is initialised before anyone waits on it
     const uint64_t t0 = globaltimer_ns();
     while (!mbar_try_wait(&s_bar, 0)) {
-        if (globaltimer_ns() - t0 > kBulkWaitNs) {
+        if (globaltimer_ns() - t0 > a.bulk_ns) {
             if (threadIdx.x == 0) atomicExch(&a.ctl->err, ALB_ERR_TIMEOUT);
             // the copy may still be writing this CTA's shared memory: stay
             // resident until it lands (second, longer bound) before leaving
             const uint64_t t1 = globaltimer_ns();
-            while (!mbar_try_wait(&s_bar, 0) && globaltimer_ns() - t1 < 4 * kBulkWaitNs)
+            while (!mbar_try_wait(&s_bar, 0) && globaltimer_ns() - t1 < 4 * a.bulk_ns)
                 __nanosleep(1024);
             return;
         }
@@ -797,8 +881,10 @@ __global__ void k_end(BfsArgs a, cudaGraphConditionalHandle wh) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     BfsCtl c = *a.ctl;
     const int k = (c.level + 1) % 3;
-    if (a.trace && c.level < c.trace_cap)
+    if (a.trace && c.level < c.trace_cap) {
         a.trace[c.level].bytes = level_bytes(c, c.dir, c.acc_n[k], c.acc_bytes[k]);
+        write_stats(a.trace[c.level], c, k);
+    }
     c.launches += 2 + (c.branch == 1 ? 4 : 3);  // decide, end, steps
     roll(c, c.dir, c.acc_n[k], c.acc_mo[k], c.acc_mi[k], c.acc_full[k]);
     if (c.level < c.trace_cap) c.trace_len = c.level;
@@ -819,7 +905,14 @@ __global__ void k_scatter(BfsArgs a, int32_t *level, int32_t *parent) {
 
 // ------------------------------------------------------ persistent kernel
 
-__device__ bool grid_sync(BfsCtl *ctl, unsigned nblocks) {
+// Grid barrier of the persistent kernel. Its wait is bounded by
+// a.barrier_ns: on expiry it records ALB_ERR_TIMEOUT and every block leaves.
+// (withhold_level: a test hook under which one block skips its arrival at
+// level L's barriers and leaves.)
+__device__ bool grid_sync(const BfsArgs &a, unsigned nblocks, int L) {
+    BfsCtl *ctl = a.ctl;
+    if (a.withhold_level >= 0 && L == a.withhold_level && (int)blockIdx.x == a.withhold_block)
+        return false;
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned *gen = &ctl->bar_gen;
@@ -833,7 +926,7 @@ __device__ bool grid_sync(BfsCtl *ctl, unsigned nblocks) {
         } else {
             const uint64_t t0 = globaltimer_ns();
             while (*gen == g0) {
-                if (globaltimer_ns() - t0 > kBarrierTimeoutNs) {
+                if (globaltimer_ns() - t0 > a.barrier_ns) {
                     atomicExch(&ctl->err, ALB_ERR_TIMEOUT);
                     break;
                 }
@@ -866,6 +959,7 @@ __global__ void __launch_bounds__(256) k_persistent(BfsArgs a) {
                     a.ctl->acc_mi[k] = 0;
                     a.ctl->acc_full[k] = 0;
                     a.ctl->acc_bytes[k] = 0;
+                    for (int i = 0; i < kStatN; i++) a.ctl->acc_stat[k][i] = 0;
                     a.ctl->nbig[k] = 0;
                     a.ctl->work[k] = 0;
                     a.ctl->qn[k] = 0;
@@ -879,53 +973,55 @@ __global__ void __launch_bounds__(256) k_persistent(BfsArgs a) {
         if (dir == ALB_DIR_TOPDOWN) {
             if (!c.q_valid || c.n_dirty) {
                 prep_phase<true>(a, L, !c.q_valid, c.n_dirty != 0, r);
-                ok = grid_sync(a.ctl, nb);
+                ok = grid_sync(a, nb, L);
             }
             if (ok) {
                 td_phase<true>(a, L, r);
-                ok = grid_sync(a.ctl, nb);
+                ok = grid_sync(a, nb, L);
             }
             if (ok && *(volatile unsigned long long *)&a.ctl->nbig[L % 3]) {
                 td_big_phase<true>(a, L, r);
-                ok = grid_sync(a.ctl, nb);
+                ok = grid_sync(a, nb, L);
             }
             if (ok) {
                 td_finish_phase<true>(a, L, r);
-                ok = grid_sync(a.ctl, nb);
+                ok = grid_sync(a, nb, L);
             }
         } else if (dir == ALB_DIR_BOTTOMUP) {
             if (a.nlong) {
                 bu_long_phase<true, true>(a, L, r);
-                ok = grid_sync(a.ctl, nb);
+                ok = grid_sync(a, nb, L);
                 if (ok && *(volatile unsigned long long *)&a.ctl->nbig[L % 3]) {
                     bu_long_tail_phase<true, true>(a, L, r);
-                    ok = grid_sync(a.ctl, nb);
+                    ok = grid_sync(a, nb, L);
                 }
             }
             if (ok) {
                 bu_phase<true, true, true>(a, L, r);
-                ok = grid_sync(a.ctl, nb);
+                ok = grid_sync(a, nb, L);
             }
         } else {
             if (a.nlong) {
                 bu_long_phase<true, false>(a, L, r);
-                ok = grid_sync(a.ctl, nb);
+                ok = grid_sync(a, nb, L);
                 if (ok && *(volatile unsigned long long *)&a.ctl->nbig[L % 3]) {
                     bu_long_tail_phase<true, false>(a, L, r);
-                    ok = grid_sync(a.ctl, nb);
+                    ok = grid_sync(a, nb, L);
                 }
             }
             if (ok) {
                 bu_phase<true, false, false>(a, L, r);
-                ok = grid_sync(a.ctl, nb);
+                ok = grid_sync(a, nb, L);
             }
         }
         if (!ok) break;
         if (threadIdx.x == 0) {
             const int k = (L + 1) % 3;
             volatile BfsCtl *g = a.ctl;
-            if (blockIdx.x == 0 && a.trace && L < c.trace_cap)
+            if (blockIdx.x == 0 && a.trace && L < c.trace_cap) {
                 a.trace[L].bytes = level_bytes(c, dir, g->acc_n[k], g->acc_bytes[k]);
+                write_stats(a.trace[L], *g, k);
+            }
             roll(c, dir, g->acc_n[k], g->acc_mo[k], g->acc_mi[k], g->acc_full[k]);
             c.dir = dir;
         }
@@ -961,6 +1057,8 @@ __global__ void __launch_bounds__(256) k_persistent(BfsArgs a) {
 
 struct alb::CachedLoop {
     int block = 0;
+    uint64_t bulk_ns = 0;  // the wait settings baked into the kernel nodes
+    int32_t short_bulk = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
@@ -1087,6 +1185,12 @@ BfsArgs make_args(alb_graph *g) {
     a.ctl = b.ctl;
     a.trace = b.trace;
     a.mlp = selector_device_params(0);
+    const DeviceWaits dw = device_waits(kBarrierTimeoutNs, kBulkWaitNs);
+    a.barrier_ns = dw.barrier_ns;
+    a.bulk_ns = dw.bulk_ns;
+    a.withhold_level = dw.withhold_level;
+    a.withhold_block = dw.withhold_block;
+    a.short_bulk = dw.short_bulk;
     return a;
 }
 
@@ -1169,6 +1273,8 @@ alb_status build_loop_graph(alb_graph *g, int block) {
     g->loop = cl;
     cl->block = block;
     BfsArgs a = make_args(g);
+    cl->bulk_ns = a.bulk_ns;
+    cl->short_bulk = a.short_bulk;
     const Launch wide = level_launch(g, block);
     const Launch one{1, 32, g->num_sms};
     const BuSlices bu2 = bu_slices<true, true>(a, wide), bu3 = bu_slices<false, false>(a, wide);
@@ -1367,7 +1473,9 @@ alb_status bfs_impl(alb_graph *g, int32_t root, const alb_bfs_opts &o, int32_t *
     } else if (o.loop == ALB_LOOP_PERSISTENT) {
         lrc = run_persistent(g, a);
     } else {
-        if (!g->loop || g->loop->block != o.block) lrc = build_loop_graph(g, o.block);
+        if (!g->loop || g->loop->block != o.block || g->loop->bulk_ns != a.bulk_ns ||
+            g->loop->short_bulk != a.short_bulk)
+            lrc = build_loop_graph(g, o.block);
         if (lrc == ALB_OK && cudaGraphLaunch(g->loop->exec, stream) != cudaSuccess)
             lrc = fail(ALB_ERR_CUDA, "cudaGraphLaunch: %s", cudaGetErrorString(cudaGetLastError()));
     }

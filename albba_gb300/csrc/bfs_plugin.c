@@ -8,6 +8,7 @@
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
+#include <string.h>
 
 #include "albba.h"
 
@@ -28,6 +29,52 @@ static int *g_parents = NULL;
 
 const int *bfs_gb300_last_levels(void) { return g_levels; }
 const int *bfs_gb300_last_parents(void) { return g_parents; }
+
+/* Directory of the bypass records: the reference writes them to
+ * ../bfs/data/ (bfs/src/bfs_SELLCSv2.c:774); ALB_BYPASS_DIR overrides it. */
+static const char *bypass_dir(void)
+{
+    const char *d = getenv("ALB_BYPASS_DIR");
+    return (d && *d) ? d : "../bfs/data";
+}
+
+/* One CSV line per run in the reference's bypass record format
+ * (bfs/src/bfs_SELLCSv2.c:773-818): name, rows, columns, entries, levels, the
+ * unit count, then one count per level. The slice record counts 32-row words
+ * skipped because every row was visited (the reference's slices); the column
+ * record counts 4-column groups a row left unread because it stopped at its
+ * first frontier source, against the total of such groups per lane. */
+static void write_bypass(const SparseMatrixCSR *m, alb_graph *g, const alb_level_rec *tr, int cnt)
+{
+    const char *name = m->name ? m->name : "matrix";
+    const char *slash = strrchr(name, '/');
+    if (slash) name = slash + 1;
+    int64_t nslices = 0, nwords = 0;
+    alb_sell_export(g, &nslices, NULL, NULL, NULL, NULL);
+    int64_t *off = (int64_t *)malloc(sizeof(int64_t) * (size_t)(nslices + 1));
+    int64_t ngroups = 0;
+    if (off && alb_sell_export(g, NULL, NULL, NULL, off, NULL) == ALB_OK)
+        ngroups = off[nslices] / (4 * 32);
+    free(off);
+    nwords = (m->nrows + 31) / 32;
+    const char *files[2] = {bypass_record == 2 ? "spmv-slice-bypass.csv" : "bfs-slice-bypass.csv",
+                            "bfs-column-bypass.csv"};
+    for (int f = 0; f < (bypass_record == 2 ? 1 : 2); f++) {
+        char path[4096];
+        snprintf(path, sizeof(path), "%s/%s", bypass_dir(), files[f]);
+        FILE *out = fopen(path, "a");
+        if (!out) { /* the reference crashes here (unchecked fopen) */
+            fprintf(stderr, "bfs_gb300: cannot append to %s\n", path);
+            continue;
+        }
+        fprintf(out, "%s,%i,%i,%i,%i,%lld", name, m->nrows, m->ncolumns, m->nnz, cnt,
+                (long long)(f == 0 ? nwords : ngroups));
+        for (int l = 0; l < cnt; l++)
+            fprintf(out, ",%lld", (long long)(f == 0 ? tr[l].words_bypassed : tr[l].groups_bypassed));
+        fprintf(out, "\n");
+        fclose(out);
+    }
+}
 
 static void report_failure(const char *what, int *num_iter, double *bfs_time)
 {
@@ -94,6 +141,7 @@ void run_custom_bfs_test(const SparseMatrixCSR *m, elem_t *bfs_x, int *colidx_x,
             if (verify && frontier) frontier[l] = (int)tr[l].nf; /* bfs_SELLCSv2.c:444-447 */
             if (perf_analysis && iter_times) iter_times[l] = tr[l].step_us / 1000.0;
         }
+        if (bypass_record == 1 || bypass_record == 2) write_bypass(m, g, tr, cnt);
     }
     free(tr);
     *num_iter = st.num_levels;

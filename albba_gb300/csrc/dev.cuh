@@ -20,6 +20,36 @@ constexpr int64_t kLongChunk = 1024;
 // SELL build: rows with more raw entries than this are copied in chunks.
 constexpr int64_t kFillChunk = 2048;
 
+// ------------------------------------------------------- checked build
+// Built with -DALB_CHECKED (libalbba_gb300_checked.so), every vertex id a
+// traversal kernel loads from the matrix or a queue is checked against its
+// array before it is used as an index: an id outside [0, limit) records
+// ALB_ERR_DEVICE in the control block's error word (no trap) and is replaced
+// by `safe`, a value the kernel treats as padding or "no entry". The normal
+// build compiles the checks away.
+#ifdef ALB_CHECKED
+__device__ __forceinline__ int32_t checked_id(int32_t c, int64_t limit, int32_t safe,
+                                              int32_t *err) {
+    if (c >= 0 && (int64_t)c < limit) return c;
+    atomicExch(err, ALB_ERR_DEVICE);
+    return safe;
+}
+#define ALB_CHECK_ID(c, limit, safe, err) ((c) = ::alb::checked_id((c), (limit), (safe), (err)))
+#define ALB_CHECK_ID4(c4, limit, safe, err)    \
+    do {                                       \
+        ALB_CHECK_ID((c4).x, limit, safe, err); \
+        ALB_CHECK_ID((c4).y, limit, safe, err); \
+        ALB_CHECK_ID((c4).z, limit, safe, err); \
+        ALB_CHECK_ID((c4).w, limit, safe, err); \
+    } while (0)
+#define ALB_CHECK_POS(pos, limit, err) ((pos) >= 0 && (int64_t)(pos) < (int64_t)(limit) \
+                                        ? true : (atomicExch((err), ALB_ERR_DEVICE), false))
+#else
+#define ALB_CHECK_ID(c, limit, safe, err) ((void)0)
+#define ALB_CHECK_ID4(c4, limit, safe, err) ((void)0)
+#define ALB_CHECK_POS(pos, limit, err) true
+#endif
+
 // ---------------------------------------------------------------- loads
 // Column and structure arrays are read-only for a whole traversal: read them
 // through the non-coherent path. Bitmaps and queues are rewritten between
@@ -179,12 +209,23 @@ struct BfsCtl {
     unsigned long long acc_n[3], acc_mo[3], acc_mi[3], acc_full[3], qn[3], acc_bytes[3];
     unsigned long long nbig[3];  // rows too long for one warp, per level slot
     unsigned long long work[3];  // bottom-up word counter (grab_words), per level slot
+    unsigned long long acc_stat[3][5];  // bypass statistics per level slot (kSt*)
     unsigned int bar_count, bar_gen;  // persistent-kernel grid barrier
     int32_t trace_cap, trace_len;
     int32_t level_cap;       // safety bound on the number of levels
     int32_t branch;          // loop-graph switch branch taken this level
     int64_t launches;        // kernel launches of the level loop
     float feat_mean_deg, feat_skew;  // static selector features
+};
+
+// Bypass statistics accumulated per level (alb_level_rec).
+enum LevelStat : int {
+    kStWordsBypassed = 0,
+    kStRowsScanned = 1,
+    kStGroupsRead = 2,
+    kStGroupsTotal = 3,
+    kStEdgesBypassed = 4,
+    kStatN = 5,
 };
 
 // Per-traversal device arguments (passed by value to every kernel).
@@ -215,6 +256,9 @@ struct BfsArgs {
     BfsCtl *ctl;
     alb_level_rec *trace;
     const float *mlp;          // selector parameters or null
+    // bounded waits (DeviceWaits): limits and test hooks
+    uint64_t barrier_ns, bulk_ns;
+    int32_t withhold_level, withhold_block, short_bulk;
 };
 
 // Shared by host and device: pick the direction for the current level.

@@ -16,6 +16,9 @@
 //   k/4 of a C=32 slice issues one fully coalesced 512-byte int4 load.
 //   Self-loops are dropped, so the padding value doubles as an end marker.
 #include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -103,6 +106,29 @@ void dfree(void *p) {
     cudaStreamSynchronize(0);
 }
 
+static double now_ms() {
+    return std::chrono::duration<double, std::milli>(
+               std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
+
+PhaseLog::PhaseLog(const char *c) : call(c) {
+    static const bool enabled = [] {
+        const char *e = std::getenv("ALB_TRACE_PHASES");
+        return e && *e && *e != '0';
+    }();
+    on = enabled;
+    if (on) t = now_ms();
+}
+
+void PhaseLog::mark(const char *phase, cudaStream_t st) {
+    if (!on) return;
+    cudaStreamSynchronize(st);
+    const double t1 = now_ms();
+    std::fprintf(stderr, "alb phase %s/%s %.3f ms\n", call, phase, t1 - t);
+    t = t1;
+}
+
 int resident_blocks(const void *func, int block) {
     static std::mutex mu;
     static std::map<std::pair<const void *, int>, int> cache;
@@ -178,7 +204,9 @@ alb_status finish_device_csr(alb_graph *g, int64_t *d_rp, int32_t *d_col, int64_
     g->col_in = g->col_out = d_col;
     g->nnz_in = g->nnz_out = nnz;
     bool sorted = true;
-    ALB_TRY(csr_check(g->n, d_rp, d_col, nnz, g->stream, &sorted));
+    // ALB_CSR_SORTED: the caller vouches for the order, only ranges are checked
+    ALB_TRY(csr_check(g->n, d_rp, d_col, nnz, g->stream,
+                      (flags & ALB_CSR_SORTED) ? nullptr : &sorted));
     if (!sorted) ALB_TRY(sort_rows(g->n, d_rp, d_col, nnz, g->stream));
     if (flags & ALB_CSR_SYMMETRIC) {
         g->symmetric = true;
@@ -209,13 +237,17 @@ alb_status create_impl(int64_t n, const int64_t *rowptr, const int32_t *col, uin
                        alb_graph **out) {
     if (rowptr[0] != 0 || rowptr[n] < 0)
         return fail(ALB_ERR_INVALID, "row offsets must start at 0 and end at nnz >= 0");
+    PhaseLog ph("graph_create");
     alb_graph *g = nullptr;
     ALB_TRY(graph_shell(n, &g));
+    ph.mark("setup", g->stream);
     int64_t *d_rp = nullptr;
     int32_t *d_col = nullptr;
     alb_status st = upload(n, rowptr, col, &d_rp, &d_col, g->stream);
+    ph.mark("upload", g->stream);
     if (st == ALB_OK) {
         st = finish_device_csr(g, d_rp, d_col, rowptr[n], flags);
+        ph.mark("check_sort_transpose", g->stream);
     } else {
         dfree(d_rp);
         dfree(d_col);
@@ -234,9 +266,11 @@ alb_status create_impl(int64_t n, const int64_t *rowptr, const int32_t *col, uin
 
 // --------------------------------------------------------- device kernels
 
-// Row lengths without self-loops, for both sides.
+// Row lengths without self-loops, for both sides; optionally (sl_off != 0)
+// each row's self-loop run: its offset in the row and its length.
 __global__ void k_row_lengths(int64_t n, const int64_t *rp, const int32_t *col, int32_t *len,
-                              int32_t *max_len) {
+                              int32_t *max_len, int32_t *sl_off = nullptr,
+                              int32_t *sl_num = nullptr) {
     int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     int32_t l = 0;
     if (v < n) {
@@ -257,6 +291,10 @@ __global__ void k_row_lengths(int64_t n, const int64_t *rp, const int32_t *col, 
         }
         l = (int32_t)((e - b) - (lo2 - lo));
         len[v] = l;
+        if (sl_off) {
+            sl_off[v] = (int32_t)(lo - b);
+            sl_num[v] = (int32_t)(lo2 - lo);
+        }
     }
     l = __reduce_max_sync(kFull, l);
     if ((threadIdx.x & 31) == 0 && l > 0) atomicMax(max_len, l);
@@ -350,15 +388,38 @@ __global__ void k_identity(int64_t n, int32_t *perm) {
     if (p < n) perm[p] = (int32_t)p;
 }
 
-// inv, and per-position degrees.
+alb_status window_order_impl(int64_t n, int32_t sigma, const int32_t *d_len, int32_t *d_perm,
+                             cudaStream_t st) {
+    if (sigma <= 1) {
+        k_identity<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, d_perm);
+    } else {
+        int tpb = std::min(1024, std::max(32, ((sigma / 16 + 31) / 32) * 32));
+        int items = (sigma + tpb - 1) / tpb;
+        size_t sm = sizeof(int32_t) * sigma + sizeof(int32_t) * 16 * tpb +
+                    2 * sizeof(uint16_t) * sigma;
+        ALB_CK(cudaFuncSetAttribute(k_window_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)sm));
+        unsigned nwin = (unsigned)((n + sigma - 1) / sigma);
+        k_window_sort<<<nwin, tpb, sm, st>>>(n, sigma, items, d_len, d_perm);
+    }
+    ALB_CK(cudaGetLastError());
+    return ALB_OK;
+}
+
+// inv, and per-position degrees; for the flat fill, each position's raw
+// pull-row start and self-loop run.
 __global__ void k_positions(int64_t n, const int32_t *perm, const int32_t *ilen,
-                            const int32_t *olen, int32_t *inv, int32_t *ideg, int32_t *odeg) {
+                            const int32_t *olen, int32_t *inv, int32_t *ideg, int32_t *odeg,
+                            const int64_t *rp, const int32_t *sl_off, const int32_t *sl_num,
+                            int64_t *rstart, int2 *sl) {
     int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (p >= n) return;
     int32_t v = perm[p];
     inv[v] = (int32_t)p;
     ideg[p] = ilen[v];
     odeg[p] = olen[v];
+    rstart[p] = rp[v];
+    sl[p] = make_int2(sl_off[v], sl_num[v]);
 }
 
 __device__ __forceinline__ bool is_long(int32_t d, int32_t long_row) {
@@ -379,69 +440,82 @@ __global__ void k_widths(int64_t n, int64_t nslices, int32_t C, int32_t long_row
     ssize[s] = (int64_t)C * ((w + 3) & ~3);
 }
 
-// Fill the 4-interleaved SELL columns, one thread per (padded) row, so that
-// a warp keeps 32 rows' loads in flight instead of one row's: each thread
-// reads its CSR row four entries at a time (the four column loads, then the
-// four inv gathers, each group independent of the next), drops self-loops,
-// and writes every group of four kept entries as one int4; the C rows of a
-// slice write group g as C contiguous int4 (coalesced). The slice is padded
-// with the row's own position up to its width. The CSR columns are read once
-// (L2 evict-first) and the slices written with streaming stores, so that inv,
-// gathered at random, keeps its lines in L2.
-__global__ void k_fill_sell(int64_t n, int64_t npad, int32_t C, int32_t log2C, int32_t long_row,
-                            const int32_t *perm, const int32_t *inv, const int32_t *ideg,
-                            const int32_t *width, const int64_t *slice_off, const int64_t *rp,
-                            const int32_t *col, int32_t *scol) {
-    const int64_t str = (int64_t)gridDim.x * blockDim.x;
+// Largest slice s in [lo, hi] whose first int4 slot is <= q (empty slices
+// share their successor's offset and are passed over).
+__device__ __forceinline__ int64_t slice_of(const int64_t *slice_off, int64_t q, int64_t lo,
+                                            int64_t hi) {
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) >> 1;
+        if ((slice_off[mid] >> 2) <= q) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Flat fill of the 4-interleaved SELL: one thread per int4 slot (four entries
+// of one row), 32 consecutive slots per warp, so every thread does the same
+// small amount of work (four column loads, four inv gathers, one coalesced
+// 16-byte store) however long its row is, and a warp's store is 512
+// contiguous bytes. A slot's slice is found by binary search inside the
+// range the warp's first and last slots span. kPush (symmetric graphs, where
+// a position's push row is its SELL row): the same entries are written to the
+// push CSR too, so the CSR is read and gathered once for both. Long rows stay
+// padding here (their lists are filled by k_fill_chunks).
+template <bool kPush>
+__global__ void __launch_bounds__(256) k_fill_flat(
+    int64_t n, int64_t nslices, int64_t nslots, int32_t C, int32_t log2C, int32_t long_row,
+    const int64_t *slice_off, const int32_t *ideg, const int64_t *rstart, const int2 *sl,
+    const int32_t *col, const int32_t *inv, int32_t *scol, const int64_t *prow, int32_t *pcol) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const uint64_t pstream = l2_evict_first();
-    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npad; p += str) {
-        const int64_t s = p >> log2C;
-        const int32_t r = (int32_t)(p & (C - 1));
-        const int32_t ng = (width[s] + 3) >> 2;
-        // slice_off is a multiple of 4 (every slice holds C * w4 entries)
-        int4 *base = reinterpret_cast<int4 *>(scol + slice_off[s]) + r;
+    int4 *scol4 = reinterpret_cast<int4 *>(scol);
+    for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w * 32 < nslots;
+         w += nw) {
+        const int64_t q0 = w * 32, q = q0 + lane;
+        const int64_t qlast = min(q0 + 31, nslots - 1);
+        int64_t s_lo = 0, s_hi = 0;
+        if (lane == 0) s_lo = slice_of(slice_off, q0, 0, nslices - 1);
+        if (lane == 31) s_hi = slice_of(slice_off, qlast, 0, nslices - 1);
+        s_lo = __shfl_sync(kFull, s_lo, 0);
+        s_hi = __shfl_sync(kFull, s_hi, 31);
+        if (q >= nslots) continue;
+        const int64_t sc = slice_of(slice_off, q, s_lo, s_hi);
+        const int64_t k4 = q - (slice_off[sc] >> 2);
+        const int32_t g = (int32_t)(k4 >> log2C);
+        const int64_t p = sc * C + (k4 & (C - 1));
         const int32_t pad = p < n ? (int32_t)p : 0;
-        int32_t g = 0, nb = 0;
-        int4 cur = make_int4(pad, pad, pad, pad);
-        auto put = [&](int32_t x) {
-            if (nb == 0) cur.x = x;
-            else if (nb == 1) cur.y = x;
-            else if (nb == 2) cur.z = x;
-            else cur.w = x;
-            if (++nb == 4) {
-                __stcs(base + (int64_t)g * C, cur);
-                g++;
-                nb = 0;
-                cur = make_int4(pad, pad, pad, pad);
+        int32_t v[4] = {pad, pad, pad, pad};
+        const int32_t d = p < n ? __ldg(ideg + p) : 0;
+        const int32_t k0 = 4 * g;
+        if (p < n && !is_long(d, long_row) && k0 < d) {
+            const int64_t b = __ldg(rstart + p);
+            const int2 run = __ldg(sl + p);
+            int32_t c[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int32_t kk = k0 + k;
+                const int32_t raw = kk < run.x ? kk : kk + run.y;
+                c[k] = kk < d ? ld_hint(col + b + raw, pstream) : -1;
             }
-        };
-        if (p < n && !is_long(ideg[p], long_row)) {
-            const int32_t v = perm[p];
-            const int64_t b = rp[v], e = rp[v + 1];
-            for (int64_t i = b; i < e; i += 4) {
-                int32_t c[4], q[4];
 #pragma unroll
-                for (int k = 0; k < 4; k++) c[k] = i + k < e ? ld_hint(col + i + k, pstream) : v;
-#pragma unroll
-                for (int k = 0; k < 4; k++) q[k] = c[k] != v ? __ldg(inv + c[k]) : 0;
+            for (int k = 0; k < 4; k++)
+                if (c[k] >= 0) v[k] = __ldg(inv + c[k]);
+            if (kPush) {
+                const int64_t at = __ldg(prow + p) + k0;
 #pragma unroll
                 for (int k = 0; k < 4; k++)
-                    if (c[k] != v) put(q[k]);
+                    if (k0 + k < d) __stcs(pcol + at + k, v[k]);
             }
         }
-        if (nb > 0) {  // the last partial group, padded
-            __stcs(base + (int64_t)g * C, cur);
-            g++;
-        }
-        const int4 pads = make_int4(pad, pad, pad, pad);
-        for (; g < ng; g++) __stcs(base + (int64_t)g * C, pads);
+        __stcs(scol4 + q, make_int4(v[0], v[1], v[2], v[3]));
     }
 }
 
-// Push-side CSR in position space, one thread per row (as k_fill_sell: four
-// column loads, then four inv gathers, per step, with the same L2
-// policies). Rows with more than
-// kFillChunk raw entries are left to k_fill_chunks.
+// Push-side CSR in position space for graphs whose push side differs from
+// the pull side, one thread per row: four column loads, then four inv
+// gathers, per step (columns read evict-first, outputs streamed). Rows with
+// more than kFillChunk raw entries are left to k_fill_chunks.
 __global__ void k_fill_push(int64_t n, const int32_t *perm, const int32_t *inv,
                             const int64_t *prow, const int64_t *rp, const int32_t *col,
                             int32_t *pcol) {
@@ -540,7 +614,7 @@ __global__ void k_fill_chunks(int64_t nchunks, const int32_t *crow, const int32_
                               const int64_t *cb, const int64_t *slo, const int64_t *shi,
                               const int32_t *perm, const int32_t *inv, const int64_t *rp,
                               const int32_t *col, const int64_t *obase, int by_pos,
-                              int32_t *out) {
+                              int32_t *out, const int64_t *obase2, int32_t *out2) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
     const uint64_t pstream = l2_evict_first();
@@ -554,9 +628,15 @@ __global__ void k_fill_chunks(int64_t nchunks, const int32_t *crow, const int32_
         const int64_t s1 = min(e, s0 + kFillChunk);
         const int64_t lo = slo[i], hi = shi[i];
         const int64_t o = by_pos ? obase[p] : obase[i];
+        const int64_t o2 = out2 ? obase2[p] : 0;
         for (int64_t j = s0 + lane; j < s1; j += 32) {
             const int32_t c = ld_hint(col + j, pstream);
-            if (c != v) __stcs(out + o + (j - b) - (min(max(j, lo), hi) - lo), __ldg(inv + c));
+            if (c != v) {
+                const int64_t at = (j - b) - (min(max(j, lo), hi) - lo);
+                const int32_t q = __ldg(inv + c);
+                __stcs(out + o + at, q);
+                if (out2) __stcs(out2 + o2 + at, q);
+            }
         }
     }
 }
@@ -565,28 +645,22 @@ __global__ void k_fill_chunks(int64_t nchunks, const int32_t *crow, const int32_
 // be discovered by a pull, so they start visited (their level stays -1).
 __global__ void k_vinit(int64_t n, int64_t nwords, const int32_t *ideg, uint32_t *vinit,
                         unsigned long long *counters) {
-    int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (w >= nwords) return;
-    uint32_t m = 0;
-    int32_t z = 0;
-    unsigned long long sum = 0;
-    for (int b = 0; b < 32; b++) {
-        int64_t p = w * 32 + b;
-        if (p >= n) {
-            m |= 1u << b;
-        } else {
-            int32_t d = ideg[p];
-            sum += (unsigned long long)d;
-            if (d == 0) {
-                m |= 1u << b;
-                z++;
-            }
-        }
+    // thread per position (coalesced degree loads), one ballot per word
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int64_t w = p >> 5;
+    if (w >= nwords) return;  // whole warps leave together (nwords * 32 positions)
+    const int32_t d = p < n ? ideg[p] : 0;
+    const bool pre = p >= n || d == 0;
+    const uint32_t m = __ballot_sync(kFull, pre);
+    const unsigned z = __popc(__ballot_sync(kFull, p < n && d == 0));
+    const unsigned long long sum = warp_sum((unsigned long long)d);
+    if (lane == 0) {
+        vinit[w] = m;
+        if (m != kFull) atomicAdd(&counters[0], 1ull);  // active words
+        if (z) atomicAdd(&counters[1], (unsigned long long)z);  // rows without sources
+        if (sum) atomicAdd(&counters[2], sum);  // pull-side entries
     }
-    vinit[w] = m;
-    if (m != kFull) atomicAdd(&counters[0], 1ull);  // active words
-    if (z) atomicAdd(&counters[1], (unsigned long long)z);  // rows without sources
-    if (sum) atomicAdd(&counters[2], sum);  // pull-side entries
 }
 
 inline unsigned grid_for(int64_t count, int tpb) { return (unsigned)((count + tpb - 1) / tpb); }
@@ -617,7 +691,8 @@ alb_status chunk_list(const int32_t *cnt, int64_t nr, int64_t **cb, int32_t **cr
 alb_status fill_rows_chunked(const int32_t *rows, int64_t nr, const int32_t *perm,
                              const int32_t *inv, const int64_t *rp, const int32_t *col,
                              const int64_t *obase, bool by_pos, int32_t *out, unsigned grid,
-                             cudaStream_t st) {
+                             cudaStream_t st, const int64_t *obase2 = nullptr,
+                             int32_t *out2 = nullptr) {
     if (nr == 0) return ALB_OK;
     int32_t *cnt = nullptr, *crow = nullptr;
     int64_t *slo = nullptr, *shi = nullptr, *cb = nullptr;
@@ -639,7 +714,7 @@ alb_status fill_rows_chunked(const int32_t *rows, int64_t nr, const int32_t *per
         ALB_TRY(chunk_list(cnt, nr, &cb, &crow, &nchunks, st));
         if (nchunks)
             k_fill_chunks<<<grid, 256, 0, st>>>(nchunks, crow, rows, cb, slo, shi, perm, inv, rp,
-                                                col, obase, by_pos ? 1 : 0, out);
+                                                col, obase, by_pos ? 1 : 0, out, obase2, out2);
         ALB_CK(cudaGetLastError());
         // the temporaries are freed below: finish with them first
         ALB_CK(cudaStreamSynchronize(st));
@@ -664,8 +739,9 @@ alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma, int32_t long_
     s.nslices = (n + C - 1) / C;
     const int64_t npad = s.nslices * C;
     s.nwords = (npad + 31) / 32;
-    int32_t *ilen = nullptr, *olen = nullptr, *dmax = nullptr;
-    int64_t *ssize = nullptr;
+    int32_t *ilen = nullptr, *olen = nullptr, *dmax = nullptr, *sl_off = nullptr, *sl_num = nullptr;
+    int64_t *ssize = nullptr, *rstart = nullptr;
+    int2 *slrun = nullptr;
     unsigned long long *dcnt = nullptr;
     auto tmp_free = [&]() {
         dfree(ilen);
@@ -673,7 +749,12 @@ alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma, int32_t long_
         dfree(dmax);
         dfree(ssize);
         dfree(dcnt);
+        dfree(sl_off);
+        dfree(sl_num);
+        dfree(rstart);
+        dfree(slrun);
     };
+    PhaseLog ph("sell_build");
     alb_status rc = [&]() -> alb_status {
         ALB_TRY(dmalloc((void **)&ilen, sizeof(int32_t) * n, "row lengths"));
         ALB_TRY(dmalloc((void **)&olen, sizeof(int32_t) * n, "row lengths"));
@@ -688,29 +769,25 @@ alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma, int32_t long_
         ALB_TRY(dmalloc((void **)&ssize, sizeof(int64_t) * (s.nslices + 1), "slice sizes"));
         ALB_TRY(dmalloc((void **)&s.prow, sizeof(int64_t) * (n + 1), "push offsets"));
         ALB_TRY(dmalloc((void **)&s.vinit, sizeof(uint32_t) * s.nwords, "vinit"));
+        ALB_TRY(dmalloc((void **)&sl_off, sizeof(int32_t) * n, "self-loop runs"));
+        ALB_TRY(dmalloc((void **)&sl_num, sizeof(int32_t) * n, "self-loop runs"));
+        ALB_TRY(dmalloc((void **)&rstart, sizeof(int64_t) * n, "row starts"));
+        ALB_TRY(dmalloc((void **)&slrun, sizeof(int2) * n, "self-loop runs"));
         ALB_CK(cudaMemsetAsync(dmax, 0, sizeof(int32_t) * 2, st));
         ALB_CK(cudaMemsetAsync(dcnt, 0, sizeof(unsigned long long) * 3, st));
         const int T = 256;
-        k_row_lengths<<<grid_for(n, T), T, 0, st>>>(n, g->rp_in, g->col_in, ilen, dmax);
+        k_row_lengths<<<grid_for(n, T), T, 0, st>>>(n, g->rp_in, g->col_in, ilen, dmax, sl_off,
+                                                     sl_num);
         if (g->symmetric)
             ALB_CK(cudaMemcpyAsync(olen, ilen, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, st));
         else
             k_row_lengths<<<grid_for(n, T), T, 0, st>>>(n, g->rp_out, g->col_out, olen, dmax + 1);
         ALB_CK(cudaGetLastError());
-        if (sigma <= 1) {
-            k_identity<<<grid_for(n, T), T, 0, st>>>(n, s.perm);
-        } else {
-            int tpb = std::min(1024, std::max(32, ((sigma / 16 + 31) / 32) * 32));
-            int items = (sigma + tpb - 1) / tpb;
-            size_t sm = sizeof(int32_t) * sigma + sizeof(int32_t) * 16 * tpb +
-                        2 * sizeof(uint16_t) * sigma;
-            ALB_CK(cudaFuncSetAttribute(k_window_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)sm));
-            unsigned nwin = (unsigned)((n + sigma - 1) / sigma);
-            k_window_sort<<<nwin, tpb, sm, st>>>(n, sigma, items, ilen, s.perm);
-        }
-        ALB_CK(cudaGetLastError());
-        k_positions<<<grid_for(n, T), T, 0, st>>>(n, s.perm, ilen, olen, s.inv, s.ideg, s.odeg);
+        ph.mark("alloc_lengths", st);
+        ALB_TRY(window_order(n, sigma, ilen, s.perm, st));
+        ph.mark("sort", st);
+        k_positions<<<grid_for(n, T), T, 0, st>>>(n, s.perm, ilen, olen, s.inv, s.ideg, s.odeg,
+                                                   g->rp_in, sl_off, sl_num, rstart, slrun);
         k_widths<<<grid_for(s.nslices, T), T, 0, st>>>(n, s.nslices, C, long_row, s.ideg, s.width,
                                                         ssize);
         ALB_CK(cudaGetLastError());
@@ -730,14 +807,32 @@ alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma, int32_t long_
                         "SELL columns"));
         ALB_TRY(dmalloc((void **)&s.pcol, sizeof(int32_t) * (size_t)std::max<int64_t>(s.m_out, 1),
                         "push columns"));
+        ph.mark("positions_widths_scans", st);
         const unsigned fill_grid = (unsigned)(g->num_sms * 8);
-        k_fill_sell<<<fill_grid, T, 0, st>>>(n, npad, C, s.log2C, long_row, s.perm, s.inv, s.ideg,
-                                             s.width, s.slice_off, g->rp_in, g->col_in, s.col);
-        k_fill_push<<<fill_grid, T, 0, st>>>(n, s.perm, s.inv, s.prow, g->rp_out, g->col_out,
-                                             s.pcol);
+        // a symmetric graph's push row of a position is its pull row: one
+        // pass writes both (long rows' push rows come with their lists)
+        const bool fused = g->symmetric;
+        const int64_t nslots = s.ncol / 4;
+        if (nslots > 0) {
+            const unsigned flat_grid =
+                (unsigned)std::min<int64_t>((nslots + T - 1) / T, (int64_t)g->num_sms * 64);
+            if (fused)
+                k_fill_flat<true><<<flat_grid, T, 0, st>>>(n, s.nslices, nslots, C, s.log2C,
+                                                           long_row, s.slice_off, s.ideg, rstart,
+                                                           slrun, g->col_in, s.inv, s.col, s.prow,
+                                                           s.pcol);
+            else
+                k_fill_flat<false><<<flat_grid, T, 0, st>>>(n, s.nslices, nslots, C, s.log2C,
+                                                            long_row, s.slice_off, s.ideg, rstart,
+                                                            slrun, g->col_in, s.inv, s.col,
+                                                            s.prow, s.pcol);
+        }
+        if (!fused)
+            k_fill_push<<<fill_grid, T, 0, st>>>(n, s.perm, s.inv, s.prow, g->rp_out, g->col_out,
+                                                 s.pcol);
         ALB_CK(cudaGetLastError());
         // push rows too long for one warp: listed, then copied in chunks
-        {
+        if (!fused) {
             int32_t *flag = nullptr, *rows = nullptr;
             int64_t *idx = nullptr;
             struct Tmp {
@@ -764,6 +859,7 @@ alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma, int32_t long_
                                           true, s.pcol, fill_grid, st));
             }
         }
+        ph.mark("fill", st);
         // long rows: flags -> scan -> scatter -> offsets -> fill
         {
             int32_t *flag = nullptr, *llen = nullptr;
@@ -797,10 +893,13 @@ alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma, int32_t long_
             ALB_CK(cudaStreamSynchronize(st));
             ALB_TRY(dmalloc((void **)&s.lcol, sizeof(int32_t) * std::max<int64_t>(nent, 1),
                             "long-row sources"));
+            // (fused: the same entries are the long rows' push rows)
             ALB_TRY(fill_rows_chunked(s.lrow, s.nlong, s.perm, s.inv, g->rp_in, g->col_in, s.lptr,
-                                      false, s.lcol, fill_grid, st));
+                                      false, s.lcol, fill_grid, st, fused ? s.prow : nullptr,
+                                      fused ? s.pcol : nullptr));
         }
-        k_vinit<<<grid_for(s.nwords, T), T, 0, st>>>(n, s.nwords, s.ideg, s.vinit, dcnt);
+        ph.mark("long_rows", st);
+        k_vinit<<<grid_for(s.nwords * 32, T), T, 0, st>>>(n, s.nwords, s.ideg, s.vinit, dcnt);
         ALB_CK(cudaGetLastError());
         unsigned long long hc[3];
         ALB_CK(cudaMemcpyAsync(hc, dcnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
@@ -811,6 +910,7 @@ alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma, int32_t long_
         return ALB_OK;
     }();
     tmp_free();
+    ph.mark("vinit_free", st);
     if (rc != ALB_OK) {
         free_sell(g->sell);
         return rc;
@@ -820,6 +920,13 @@ alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma, int32_t long_
 }
 
 }  // namespace
+}  // namespace alb
+
+namespace alb {
+alb_status window_order(int64_t n, int32_t sigma, const int32_t *d_len, int32_t *d_perm,
+                        cudaStream_t st) {
+    return window_order_impl(n, sigma, d_len, d_perm, st);
+}
 }  // namespace alb
 
 using namespace alb;

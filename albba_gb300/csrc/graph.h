@@ -45,6 +45,17 @@ void launch_resident(void (*f)(P...), int block, int num_sms, cudaStream_t st, A
         if (s_ != ALB_OK) return s_;         \
     } while (0)
 
+// Phase timer for the host-visible entry points: with ALB_TRACE_PHASES set
+// in the environment, mark() waits for the stream and prints the wall time
+// of the phase that just ended to stderr; otherwise it does nothing.
+struct PhaseLog {
+    bool on = false;
+    const char *call = "";
+    double t = 0;
+    PhaseLog(const char *c);
+    void mark(const char *phase, cudaStream_t st);
+};
+
 struct CachedLoop;  // CUDA graph for the device-driven level loop (bfs.cu)
 
 struct Sell {
@@ -119,5 +130,10 @@ void bfs_scratch_free(alb_graph *g);
 void ms_scratch_free(alb_graph *g);
 float skew_of(const Sell &s, int64_t n);
 void loop_cache_free(alb_graph *g);
+// perm = positions -> rows, rows sorted by d_len descending (stable) inside
+// windows of sigma rows (sigma <= 1: identity); the reference's
+// get_order_by_row_size_radix (bfs/src/sorting_utils.c:232-253).
+alb_status window_order(int64_t n, int32_t sigma, const int32_t *d_len, int32_t *d_perm,
+                        cudaStream_t st);
 BfsArgs make_args(alb_graph *g);
 }  // namespace alb

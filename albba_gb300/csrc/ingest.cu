@@ -78,16 +78,17 @@ __device__ bool starts_row(int64_t n, const int64_t *rp, int64_t e) {
 }
 
 __global__ void k_check_columns(int64_t n, const int64_t *rp, const int32_t *col, int64_t nnz,
-                                int *flags) {
+                                int check_order, int *flags) {
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t nth = (int64_t)gridDim.x * blockDim.x;
-    int bits = 0;
+    int bits = check_order ? 0 : kUnsorted;  // (kUnsorted set: no order test)
     for (int64_t e = tid; e < nnz; e += nth) {
         const int32_t c = col[e];
         if (c < 0 || c >= n) bits |= kBadColumn;
         if (e > 0 && col[e - 1] > c && !(bits & kUnsorted) && !starts_row(n, rp, e))
             bits |= kUnsorted;
     }
+    if (!check_order) bits &= ~kUnsorted;
     bits = __reduce_or_sync(kFull, bits);
     if (bits && (threadIdx.x & 31) == 0) atomicOr(flags, bits);
 }
@@ -366,7 +367,8 @@ alb_status csr_check(int64_t n, const int64_t *d_rp, const int32_t *d_col, int64
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     // the column pass binary-searches the offsets: only run it on valid ones
     if (e == cudaSuccess && !(h & kBadOffsets) && nnz > 0) {
-        k_check_columns<<<grid_for(nnz, 256), 256, 0, st>>>(n, d_rp, d_col, nnz, d_flags);
+        k_check_columns<<<grid_for(nnz, 256), 256, 0, st>>>(n, d_rp, d_col, nnz,
+                                                             sorted ? 1 : 0, d_flags);
         e = cudaGetLastError();
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(&h, d_flags, sizeof(int), cudaMemcpyDeviceToHost, st);

@@ -10,7 +10,8 @@
 namespace alb {
 
 // Offsets start at 0, never decrease and end at nnz; columns in [0, n)
-// (ALB_ERR_INVALID otherwise). *sorted: every row ascending.
+// (ALB_ERR_INVALID otherwise). *sorted: every row ascending (sorted == NULL:
+// the order is not checked).
 alb_status csr_check(int64_t n, const int64_t *d_rp, const int32_t *d_col, int64_t nnz,
                      cudaStream_t st, bool *sorted);
 // Sorts every row ascending in place.

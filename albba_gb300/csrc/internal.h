@@ -17,6 +17,17 @@ alb_status fail(alb_status code, const char *fmt, ...);
 // Host fault injection for device allocations (alb_debug_fail_alloc_after).
 bool injected_alloc_failure();
 
+// Limits and test hooks of the bounded device-side waits
+// (alb_debug_device_waits): the given defaults unless a test shortened them.
+struct DeviceWaits {
+    uint64_t barrier_ns;     // grid barrier of the persistent kernels
+    uint64_t bulk_ns;        // bulk copy into shared memory
+    int32_t withhold_level;  // level at which one block skips its barrier arrival (-1: none)
+    int32_t withhold_block;
+    int32_t short_bulk;      // the staged pull expects 16 bytes its copy never delivers
+};
+DeviceWaits device_waits(uint64_t barrier_ns, uint64_t bulk_ns);
+
 // SplitMix64 finaliser (Steele, Lea, Flood 2014; Vigna's splitmix64.c):
 // a bijective 64-bit mix used for every counter-based random draw.
 inline uint64_t mix64(uint64_t z) {

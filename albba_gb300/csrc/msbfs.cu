@@ -373,6 +373,21 @@ __global__ void __launch_bounds__(kMsBuBlock, kWide ? 4 : 5) k_ms_bu(MsArgs a, i
     int32_t wd_c;
     int64_t so_c;
     geometry(w, d, vis_c, wd_c, so_c);
+    // a word's first column groups are requested while the previous word is
+    // processed (its geometry came in one word ahead), so a word starts with
+    // its columns at hand instead of one DRAM round trip behind
+    auto first_groups = [&](int64_t ww, uint32_t dd, uint64_t vv, int32_t wdv, int64_t sov,
+                            int4 &g0, int4 &g1) {
+        const int32_t pw = (int32_t)(ww * 32 + lane);
+        g0 = g1 = make_int4(pw, pw, pw, pw);
+        if (ww >= a.nwords || (kBypass && dd == kFull) || (vv | tm) == kAll) return;
+        const int32_t ngw = (wdv + 3) >> 2;
+        const int4 *cpw = a.col4 + (sov >> 2) + (pw & (a.C - 1));
+        if (ngw > 0) g0 = ld_stream(cpw, pol);
+        if (kWide && !kFilt && ngw > 1) g1 = ld_stream(cpw + a.C, pol);
+    };
+    int4 f0, f1;
+    first_groups(w, d, vis_c, wd_c, so_c, f0, f1);
     while (w < a.nwords) {
         uint64_t vis1;
         int32_t wd1;
@@ -396,9 +411,7 @@ __global__ void __launch_bounds__(kMsBuBlock, kWide ? 4 : 5) k_ms_bu(MsArgs a, i
             const int32_t pp = (int32_t)p;
             if (kWide && !kFilt) {
                 const int4 pad = make_int4(pp, pp, pp, pp);
-                int4 c0 = pad, c1 = pad;
-                if (active && ng > 0) c0 = ld_stream(cp, pol);
-                if (active && ng > 1) c1 = ld_stream(cp + a.C, pol);
+                int4 c0 = f0, c1 = f1;
                 for (int32_t g = 0;; g += 2) {
                     active = active && g < ng;
                     if (!__any_sync(kFull, active)) break;
@@ -406,6 +419,8 @@ __global__ void __launch_bounds__(kMsBuBlock, kWide ? 4 : 5) k_ms_bu(MsArgs a, i
                     int4 n0 = pad, n1 = pad;
                     if (g + 2 < ng) n0 = ld_stream(cp + (int64_t)(g + 2) * a.C, pol);
                     if (g + 3 < ng) n1 = ld_stream(cp + (int64_t)(g + 3) * a.C, pol);
+                    ALB_CHECK_ID4(c0, a.npad, pp, &a.ctl->err);
+                    ALB_CHECK_ID4(c1, a.npad, pp, &a.ctl->err);
                     // past the row's last group c1 is padding (p itself)
                     acc |= __ldg(F + c0.x) | __ldg(F + c0.y) | __ldg(F + c0.z) | __ldg(F + c0.w) |
                            __ldg(F + c1.x) | __ldg(F + c1.y) | __ldg(F + c1.z) | __ldg(F + c1.w);
@@ -416,8 +431,7 @@ __global__ void __launch_bounds__(kMsBuBlock, kWide ? 4 : 5) k_ms_bu(MsArgs a, i
                 }
                 ng = 0;  // the single-group loop below has nothing left
             }
-            int4 c = make_int4(pp, pp, pp, pp);
-            if (active && ng > 0) c = ld_stream(cp, pol);
+            int4 c = f0;
             for (int32_t g = 0;; g++) {
                 active = active && g < ng;
                 if (!__any_sync(kFull, active)) break;
@@ -426,6 +440,7 @@ __global__ void __launch_bounds__(kMsBuBlock, kWide ? 4 : 5) k_ms_bu(MsArgs a, i
                 if (g + 1 < ng) nx = ld_stream(cp + (int64_t)(g + 1) * a.C, pol);
                 // padding entries hold p itself: S[j][p] only has bits already in
                 // V[p], so OR-ing it changes nothing
+                ALB_CHECK_ID4(c, a.npad, pp, &a.ctl->err);
                 if (kFilt) {
                     const uint32_t z0 = __ldg(Az + (c.x >> 5)), z1 = __ldg(Az + (c.y >> 5)),
                                    z2 = __ldg(Az + (c.z >> 5)), z3 = __ldg(Az + (c.w >> 5));
@@ -471,6 +486,7 @@ __global__ void __launch_bounds__(kMsBuBlock, kWide ? 4 : 5) k_ms_bu(MsArgs a, i
                 cfull += (d != kFull && (d | dm) == kFull);
             }
         }
+        first_groups(w1, d1, vis1, wd1, so1, f0, f1);
         w = w1;
         d = d1;
         vis_c = vis1;
@@ -528,6 +544,7 @@ __device__ __forceinline__ uint64_t ms_long_scan(const MsArgs &a, const uint64_t
         for (int u = 0; u < 4; u++) {
             const int64_t e = e0 + 32 * u + lane;
             c[u] = e < en ? __ldg(a.lcol + e) : -1;
+            if (c[u] >= 0) ALB_CHECK_ID(c[u], a.n, -1, &a.ctl->err);
         }
         int fetched = 0;
 #pragma unroll
@@ -858,7 +875,8 @@ __global__ void k_ms_td(MsArgs a, int j) {
     const int64_t stride = nwarps * G;
     for (int64_t cb = (blockIdx.x * wpb + wib) * G; cb < qlen; cb += stride) {
         const int64_t i = cb + lane;
-        const int32_t u = (lane < G && i < qlen) ? Q[i] : -1;
+        int32_t u = (lane < G && i < qlen) ? Q[i] : -1;
+        if (u >= 0) ALB_CHECK_ID(u, a.n, -1, &a.ctl->err);
         int64_t st = 0, d = 0;
         uint64_t f = 0;
         if (u >= 0) {
@@ -895,6 +913,7 @@ __global__ void k_ms_td(MsArgs a, int j) {
                     for (int step = 16; step > 0; step >>= 1)
                         if (s_ex[wib][jj + step] <= e) jj += step;
                     v[k] = __ldg(a.pcol + s_st[wib][jj] + (e - s_ex[wib][jj]));
+                    ALB_CHECK_ID(v[k], a.n, -1, &a.ctl->err);
                     ff[k] = s_f[wib][jj];
                 }
             }
@@ -959,6 +978,7 @@ __global__ void k_ms_td_big(MsArgs a, int j) {
         for (int q = 0; q < 4; q++) {
             const int64_t e = c * kBigChunk + 32 * q + lane;
             v[q] = e < e1 ? __ldg(a.pcol + st + e) : -1;
+            if (v[q] >= 0) ALB_CHECK_ID(v[q], a.n, -1, &a.ctl->err);
             ff[q] = f;
         }
         ms_push4<kPush>(a, N, An, v, ff, cnt);
@@ -977,7 +997,9 @@ __global__ void k_ms_td_finish(MsArgs a, int j) {
     unsigned long long cn = 0, cbits = 0, cmo = 0, cmi = 0, cfull = 0, cedges = 0, cdone = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nqlen;
          i += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t v = NQ[i];
+        int32_t v = NQ[i];
+        ALB_CHECK_ID(v, a.n, -1, &a.ctl->err);
+        if (v < 0) continue;
         const uint64_t raw = N[v];
         const uint64_t old = a.V[v];  // only this thread writes V[v] in this kernel
         const uint64_t nb = raw & ~old;  // the pushes did not mask by V
@@ -1759,7 +1781,9 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
                       int32_t *d_levels, alb_stats *st, std::vector<alb_level_rec> *trace,
                       std::vector<alb_level_profile> *prof = nullptr) {
     MsScratch &m = ms_scratch(g);
+    PhaseLog ph("msbfs64_device");
     ALB_TRY(ms_alloc(g, m));
+    ph.mark("scratch", g->stream);
     MsArgs a = ms_args(g, m);
     a.mlp = selector_device_params(1);
     const Sell &s = g->sell;
@@ -2071,16 +2095,20 @@ alb_status alb_msbfs64(alb_graph *g, const int32_t *roots, int32_t nroots, const
                        int32_t *levels, alb_stats *st) {
     if (!g) return fail(ALB_ERR_INVALID, "alb_msbfs64: graph is NULL");
     ALB_CK(cudaSetDevice(g->device));
+    PhaseLog ph("msbfs64");
     MsScratch &m = ms_scratch(g);
     if (levels && !m.out) {
         ALB_TRY(dmalloc((void **)&m.out, sizeof(int32_t) * (size_t)g->n * 64, "msbfs levels"));
     }
+    ph.mark("out_alloc", g->stream);
     ALB_TRY(alb_msbfs64_device(g, roots, nroots, o, levels ? m.out : nullptr, st));
+    ph.mark("traversal", g->stream);
     if (levels) {
         ALB_CK(cudaMemcpyAsync(levels, m.out, sizeof(int32_t) * (size_t)g->n * 64,
                                cudaMemcpyDeviceToHost, g->stream));
         ALB_CK(cudaStreamSynchronize(g->stream));
     }
+    ph.mark("copy_out", g->stream);
     return ALB_OK;
 }
 

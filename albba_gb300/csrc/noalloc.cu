@@ -64,9 +64,14 @@ struct NaArgs {
     float alpha, beta;
     int32_t *level, *parent;
     unsigned char *scratch;  // device address of g_noalloc_scratch
+    uint64_t barrier_ns;     // bound of every barrier wait
+    int32_t withhold_level, withhold_block;  // test hook (DeviceWaits)
 };
 
-__device__ bool na_sync(NaCtl *c, unsigned nblocks) {
+__device__ bool na_sync(NaCtl *c, unsigned nblocks, const NaArgs &a, int L) {
+    // test hook: one block skips its arrival at level L's barriers and leaves
+    if (a.withhold_level >= 0 && L == a.withhold_level && (int)blockIdx.x == a.withhold_block)
+        return false;
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned *gen = &c->bar_gen;
@@ -79,7 +84,7 @@ __device__ bool na_sync(NaCtl *c, unsigned nblocks) {
         } else {
             const uint64_t t0 = globaltimer_ns();
             while (*gen == g0) {
-                if (globaltimer_ns() - t0 > kNoAllocTimeoutNs) {
+                if (globaltimer_ns() - t0 > a.barrier_ns) {
                     atomicExch(&c->err, ALB_ERR_TIMEOUT);
                     break;
                 }
@@ -125,7 +130,7 @@ __global__ void k_bfs_noalloc(NaArgs a) {
         c->nn = c->mo = c->mi = 0;
         c->err = 0;
     }
-    if (!na_sync(c, nb)) return;
+    if (!na_sync(c, nb, a, -1)) return;
     if (tid == 0) {
         const int32_t r = a.root;
         V[r >> 5] |= 1u << (r & 31);
@@ -134,7 +139,7 @@ __global__ void k_bfs_noalloc(NaArgs a) {
         a.level[r] = 0;
         a.parent[r] = r;
     }
-    if (!na_sync(c, nb)) return;
+    if (!na_sync(c, nb, a, -1)) return;
     int64_t nf = 1, prev_nf = 0;
     int64_t mf = a.rp[a.root + 1] - a.rp[a.root];
     int64_t mu = m - mf;
@@ -153,7 +158,7 @@ __global__ void k_bfs_noalloc(NaArgs a) {
         if (dir == 0) {
             if (dense) {  // frontier only in F: rebuild the queue from it
                 if (tid == 0) c->qn[L & 1] = 0;
-                if (!na_sync(c, nb)) return;
+                if (!na_sync(c, nb, a, L)) return;
                 for (int64_t w = tid; w < nwords; w += nth) {
                     uint32_t word = __ldcg(F + w);
                     while (word) {
@@ -162,7 +167,7 @@ __global__ void k_bfs_noalloc(NaArgs a) {
                         Qc[atomicAdd(&c->qn[L & 1], 1ull)] = (int32_t)(w * 32 + b);
                     }
                 }
-                if (!na_sync(c, nb)) return;
+                if (!na_sync(c, nb, a, L)) return;
             }
             const int64_t ql = (int64_t)*(volatile unsigned long long *)&c->qn[L & 1];
             unsigned long long cn = 0, cmo = 0;
@@ -186,7 +191,7 @@ __global__ void k_bfs_noalloc(NaArgs a) {
                 atomicAdd(&c->nn, cn);
                 atomicAdd(&c->mo, cmo);
             }
-            if (!na_sync(c, nb)) return;
+            if (!na_sync(c, nb, a, L)) return;
             // V |= N; F <- N; N <- 0 (dense over the bitmap words)
             for (int64_t w = tid; w < nwords; w += nth) {
                 const uint32_t x = __ldcg(N + w);
@@ -216,7 +221,7 @@ __global__ void k_bfs_noalloc(NaArgs a) {
                 atomicAdd(&c->nn, cn);
                 atomicAdd(&c->mo, cmo);
             }
-            if (!na_sync(c, nb)) return;
+            if (!na_sync(c, nb, a, L)) return;
             for (int64_t w = tid; w < nwords; w += nth) {
                 const uint32_t x = __ldcg(N + w);
                 V[w] |= x;
@@ -227,19 +232,19 @@ __global__ void k_bfs_noalloc(NaArgs a) {
         }
         (void)qlen;
         if (tid == 0) c->qn[L & 1] = 0;
-        if (!na_sync(c, nb)) return;
+        if (!na_sync(c, nb, a, L)) return;
         prev_nf = nf;
         nf = (int64_t)*(volatile unsigned long long *)&c->nn;
         mf = (int64_t)*(volatile unsigned long long *)&c->mo;
         mu -= mf;
         prev_dir = dir;
-        if (!na_sync(c, nb)) return;  // everyone has read the counters
+        if (!na_sync(c, nb, a, L)) return;  // everyone has read the counters
         if (tid == 0) {
             c->nn = 0;
             c->mo = 0;
             c->level = L + 1;
         }
-        if (!na_sync(c, nb)) return;
+        if (!na_sync(c, nb, a, L)) return;
     }
     if (tid == 0) c->done = 1;
 }
@@ -346,6 +351,10 @@ extern "C" alb_status alb_bfs_csr_noalloc(int64_t n, const int64_t *d_rowptr, co
     a.level = d_level;
     a.parent = d_parent;
     a.scratch = scratch;
+    const DeviceWaits dw = device_waits(kNoAllocTimeoutNs, kNoAllocTimeoutNs);
+    a.barrier_ns = dw.barrier_ns;
+    a.withhold_level = dw.withhold_level;
+    a.withhold_block = dw.withhold_block;
     int per_sm = 0, sms = 0;
     ALB_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bfs_noalloc, 256, 0));
     ALB_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));

@@ -1,0 +1,323 @@
+// fp64 SELL-C-sigma SpMV, y = A x.
+//
+// Reference: kernel_SELLCS_DFC (bfs/src/bfs_par_kernels.c:8-53) over the
+// matrix built by convert_csr_to_sellcs_dfc (bfs/src/sparse_matrix.c:
+// 523-623): rows sorted by length inside sigma windows, C = 256 lanes per
+// slice, one column op per entry index, and per lane a fused multiply-add
+// (_vel_vfmadd_vvvvl) of value * x[column] into an accumulator that starts at
+// 0; y[row] is that accumulator. Entry k of a row is handled by column op k,
+// so every row sums its entries in CSR order with one rounding per entry --
+// the result is fixed by the CSR alone, whatever C, sigma or the lanes are.
+//
+// GB300 layout: the same sigma-window order (the library's device sort), C =
+// 32 rows per slice so that one warp owns a slice and lane r its row r, and
+// the 4-interleaved layout of the BFS's SELL: group g of slice s holds entries
+// 4g..4g+3 of every row, lane r's four column ids at col[off + 128 g + 4 r]
+// (one int4 per lane, 512 contiguous bytes per warp) and its four values at
+// the same index of val (two double2 per lane, 1 KB per warp). Entries are
+// kept exactly as given (diagonal and repeated entries included); padding is
+// never read: a lane stops at its row's length, so the fma chain is the
+// reference's, bit for bit.
+#include <cstring>
+
+#include "graph.h"
+#include "ingest.h"
+#include "scan.cuh"
+
+struct alb_sellmat {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int64_t n = 0, nnz = 0, nslices = 0, stored = 0;
+    int32_t sigma = 0;
+    int32_t *perm = nullptr;       // position -> row
+    int32_t *deg = nullptr;        // row length by position
+    int64_t *slice_off = nullptr;  // first entry of each slice (multiple of 128)
+    int32_t *col = nullptr;        // 4-interleaved column ids
+    double *val = nullptr;         // values, same layout
+    double *dx = nullptr, *dy = nullptr;  // staging for host vectors
+};
+
+namespace alb {
+namespace {
+
+constexpr int kSpC = 32;
+
+unsigned blocks_for(int64_t work, int block) {
+    int64_t g = (work + block - 1) / block;
+    return (unsigned)(g < 1 ? 1 : g);
+}
+
+__global__ void k_lengths(int64_t n, const int64_t *rp, int32_t *len) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r < n) len[r] = (int32_t)(rp[r + 1] - rp[r]);
+}
+
+__global__ void k_sp_positions(int64_t n, const int32_t *perm, const int32_t *len, int32_t *deg) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p < n) deg[p] = len[perm[p]];
+}
+
+// Slice sizes: 32 rows x the longest row rounded up to 4.
+__global__ void k_sp_sizes(int64_t n, int64_t nslices, const int32_t *deg, int64_t *ssize) {
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= nslices) return;
+    int32_t w = 0;
+    for (int r = 0; r < kSpC; r++) {
+        const int64_t p = s * kSpC + r;
+        if (p < n) w = max(w, deg[p]);
+    }
+    ssize[s] = (int64_t)kSpC * ((w + 3) & ~3);
+}
+
+// One thread per position: copies its row's entries (CSR order) into the
+// interleaved slots; the slice's remaining groups of the row are padded with
+// column 0 and value 0 (never read).
+__global__ void k_sp_fill(int64_t n, int64_t npad, const int32_t *perm, const int32_t *deg,
+                          const int64_t *slice_off, const int64_t *rp, const int32_t *col,
+                          const double *val, int32_t *scol, double *sval) {
+    const int64_t str = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npad; p += str) {
+        const int64_t s = p / kSpC;
+        const int64_t base = slice_off[s] + 4 * (p % kSpC);
+        const int32_t ng = (int32_t)((slice_off[s + 1] - slice_off[s]) / (4 * kSpC));
+        const int32_t d = p < n ? deg[p] : 0;
+        const int64_t b = p < n ? rp[perm[p]] : 0;
+        for (int32_t g = 0; g < ng; g++) {
+            int32_t c4[4];
+            double v4[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int32_t e = 4 * g + k;
+                c4[k] = e < d ? col[b + e] : 0;
+                v4[k] = e < d ? val[b + e] : 0.0;
+            }
+            const int64_t at = base + (int64_t)g * 4 * kSpC;
+            *reinterpret_cast<int4 *>(scol + at) = make_int4(c4[0], c4[1], c4[2], c4[3]);
+            reinterpret_cast<double2 *>(sval + at)[0] = make_double2(v4[0], v4[1]);
+            reinterpret_cast<double2 *>(sval + at)[1] = make_double2(v4[2], v4[3]);
+        }
+    }
+}
+
+// Warp per slice, lane per row. The next group's columns and values are
+// requested before this group's x gathers are used, so each lane keeps the
+// stream and the gathers in flight together.
+__global__ void __launch_bounds__(256) k_spmv(int64_t n, int64_t nslices, const int32_t *perm,
+                                              const int32_t *deg, const int64_t *slice_off,
+                                              const int32_t *col, const double *val,
+                                              const double *x, double *y) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const uint64_t pol = l2_evict_first();
+    for (int64_t s = w0; s < nslices; s += nw) {
+        const int64_t p = s * kSpC + lane;
+        const int32_t d = p < n ? __ldg(deg + p) : 0;
+        const int32_t ng = (d + 3) >> 2;
+        const int64_t base = __ldg(slice_off + s) + 4 * lane;
+        const int4 *cp = reinterpret_cast<const int4 *>(col + base);
+        const double2 *vp = reinterpret_cast<const double2 *>(val + base);
+        double acc = 0.0;
+        int4 c = make_int4(0, 0, 0, 0);
+        double2 va = make_double2(0.0, 0.0), vb = va;
+        if (ng > 0) {
+            c = ld_stream(cp, pol);
+            va = __ldcs(vp);
+            vb = __ldcs(vp + 1);
+        }
+        for (int32_t g = 0; g < ng; g++) {
+            int4 cn = c;
+            double2 van = va, vbn = vb;
+            if (g + 1 < ng) {
+                cn = ld_stream(cp + (int64_t)(g + 1) * kSpC, pol);
+                van = __ldcs(vp + (int64_t)(g + 1) * 2 * kSpC);
+                vbn = __ldcs(vp + (int64_t)(g + 1) * 2 * kSpC + 1);
+            }
+            const int32_t left = d - 4 * g;
+            const double x0 = __ldg(x + c.x);
+            const double x1 = left > 1 ? __ldg(x + c.y) : 0.0;
+            const double x2 = left > 2 ? __ldg(x + c.z) : 0.0;
+            const double x3 = left > 3 ? __ldg(x + c.w) : 0.0;
+            acc = fma(va.x, x0, acc);
+            if (left > 1) acc = fma(va.y, x1, acc);
+            if (left > 2) acc = fma(vb.x, x2, acc);
+            if (left > 3) acc = fma(vb.y, x3, acc);
+            c = cn;
+            va = van;
+            vb = vbn;
+        }
+        if (p < n) y[__ldg(perm + p)] = acc;
+    }
+}
+
+alb_status build(alb_sellmat *m, const int64_t *rowptr, const int32_t *col, const double *val) {
+    const int64_t n = m->n, nnz = m->nnz;
+    cudaStream_t st = m->stream;
+    int64_t *d_rp = nullptr, *ssize = nullptr;
+    int32_t *d_col = nullptr, *len = nullptr;
+    double *d_val = nullptr;
+    auto tmp_free = [&]() {
+        dfree(d_rp);
+        dfree(d_col);
+        dfree(d_val);
+        dfree(len);
+        dfree(ssize);
+    };
+    alb_status rc = [&]() -> alb_status {
+        ALB_TRY(dmalloc((void **)&d_rp, sizeof(int64_t) * (size_t)(n + 1), "SpMV row offsets"));
+        ALB_TRY(dmalloc((void **)&d_col, sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1), "SpMV columns"));
+        ALB_TRY(dmalloc((void **)&d_val, sizeof(double) * (size_t)(nnz > 0 ? nnz : 1), "SpMV values"));
+        ALB_CK(cudaMemcpyAsync(d_rp, rowptr, sizeof(int64_t) * (size_t)(n + 1),
+                               cudaMemcpyHostToDevice, st));
+        if (nnz > 0) {
+            ALB_CK(cudaMemcpyAsync(d_col, col, sizeof(int32_t) * (size_t)nnz, cudaMemcpyHostToDevice, st));
+            ALB_CK(cudaMemcpyAsync(d_val, val, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, st));
+        }
+        bool sorted = true;
+        ALB_TRY(csr_check(n, d_rp, d_col, nnz, st, &sorted));
+        m->nslices = (n + kSpC - 1) / kSpC;
+        const int64_t npad = m->nslices * kSpC;
+        ALB_TRY(dmalloc((void **)&len, sizeof(int32_t) * (size_t)n, "SpMV lengths"));
+        ALB_TRY(dmalloc((void **)&m->perm, sizeof(int32_t) * (size_t)n, "SpMV order"));
+        ALB_TRY(dmalloc((void **)&m->deg, sizeof(int32_t) * (size_t)n, "SpMV degrees"));
+        ALB_TRY(dmalloc((void **)&ssize, sizeof(int64_t) * (size_t)(m->nslices + 1), "SpMV sizes"));
+        ALB_TRY(dmalloc((void **)&m->slice_off, sizeof(int64_t) * (size_t)(m->nslices + 1),
+                        "SpMV slice offsets"));
+        k_lengths<<<blocks_for(n, 256), 256, 0, st>>>(n, d_rp, len);
+        ALB_CK(cudaGetLastError());
+        ALB_TRY(window_order(n, m->sigma, len, m->perm, st));
+        k_sp_positions<<<blocks_for(n, 256), 256, 0, st>>>(n, m->perm, len, m->deg);
+        k_sp_sizes<<<blocks_for(m->nslices, 256), 256, 0, st>>>(n, m->nslices, m->deg, ssize);
+        ALB_CK(cudaGetLastError());
+        ALB_TRY(exclusive_scan(ssize, m->slice_off, m->nslices, st));
+        ALB_CK(cudaMemcpyAsync(&m->stored, m->slice_off + m->nslices, sizeof(int64_t),
+                               cudaMemcpyDeviceToHost, st));
+        ALB_CK(cudaStreamSynchronize(st));
+        ALB_TRY(dmalloc((void **)&m->col, sizeof(int32_t) * (size_t)(m->stored > 0 ? m->stored : 4),
+                        "SpMV SELL columns"));
+        ALB_TRY(dmalloc((void **)&m->val, sizeof(double) * (size_t)(m->stored > 0 ? m->stored : 4),
+                        "SpMV SELL values"));
+        k_sp_fill<<<blocks_for(npad, 256), 256, 0, st>>>(n, npad, m->perm, m->deg, m->slice_off,
+                                                          d_rp, d_col, d_val, m->col, m->val);
+        ALB_CK(cudaGetLastError());
+        ALB_CK(cudaStreamSynchronize(st));
+        return ALB_OK;
+    }();
+    tmp_free();
+    return rc;
+}
+
+void destroy(alb_sellmat *m) {
+    if (!m) return;
+    int prev = -1;
+    cudaGetDevice(&prev);
+    cudaSetDevice(m->device);
+    if (m->stream) cudaStreamSynchronize(m->stream);
+    dfree(m->perm);
+    dfree(m->deg);
+    dfree(m->slice_off);
+    dfree(m->col);
+    dfree(m->val);
+    dfree(m->dx);
+    dfree(m->dy);
+    if (m->ev0) cudaEventDestroy(m->ev0);
+    if (m->ev1) cudaEventDestroy(m->ev1);
+    if (m->stream) cudaStreamDestroy(m->stream);
+    cudaGetLastError();
+    if (prev >= 0) cudaSetDevice(prev);
+    delete m;
+}
+
+alb_status launch(alb_sellmat *m, const double *d_x, double *d_y, float *us) {
+    int per = 0, sms = 0;
+    ALB_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_spmv, 256, 0));
+    ALB_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device));
+    const int64_t want = (m->nslices + 7) / 8;
+    const int64_t cap = (int64_t)(per > 0 ? per : 4) * sms;
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min(want, cap));
+    if (us) ALB_CK(cudaEventRecord(m->ev0, m->stream));
+    k_spmv<<<grid, 256, 0, m->stream>>>(m->n, m->nslices, m->perm, m->deg, m->slice_off, m->col,
+                                         m->val, d_x, d_y);
+    ALB_CK(cudaGetLastError());
+    if (us) {
+        ALB_CK(cudaEventRecord(m->ev1, m->stream));
+        ALB_CK(cudaEventSynchronize(m->ev1));
+        float ms = 0;
+        ALB_CK(cudaEventElapsedTime(&ms, m->ev0, m->ev1));
+        *us = ms * 1000.0f;
+    }
+    return ALB_OK;
+}
+
+}  // namespace
+}  // namespace alb
+
+using namespace alb;
+
+extern "C" {
+
+alb_status alb_sellmat_create(int64_t n, const int64_t *rowptr, const int32_t *col,
+                              const double *values, int32_t sigma, alb_sellmat **out) {
+    if (!out) return fail(ALB_ERR_INVALID, "alb_sellmat_create: out is NULL");
+    *out = nullptr;
+    if (n <= 0 || n > INT32_MAX || !rowptr || rowptr[0] != 0 || rowptr[n] < 0 ||
+        (rowptr[n] > 0 && (!col || !values)))
+        return fail(ALB_ERR_INVALID, "alb_sellmat_create: bad arguments");
+    if (sigma < 1 || sigma > 16384)
+        return fail(ALB_ERR_UNSUPPORTED, "alb_sellmat_create: sigma %d outside 1..16384", sigma);
+    alb_sellmat *m = new alb_sellmat();
+    m->n = n;
+    m->nnz = rowptr[n];
+    m->sigma = sigma;
+    cudaError_t e = cudaGetDevice(&m->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&m->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&m->ev1);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        destroy(m);
+        return fail(ALB_ERR_CUDA, "alb_sellmat_create: %s", cudaGetErrorString(e));
+    }
+    alb_status rc = build(m, rowptr, col, values);
+    if (rc != ALB_OK) {
+        destroy(m);
+        return rc;
+    }
+    *out = m;
+    return ALB_OK;
+}
+
+void alb_sellmat_destroy(alb_sellmat *m) { destroy(m); }
+
+alb_status alb_sellmat_info(const alb_sellmat *m, int64_t *n, int64_t *nnz, int64_t *stored) {
+    if (!m) return fail(ALB_ERR_INVALID, "alb_sellmat_info: matrix is NULL");
+    if (n) *n = m->n;
+    if (nnz) *nnz = m->nnz;
+    if (stored) *stored = m->stored;
+    return ALB_OK;
+}
+
+alb_status alb_sellmat_spmv(alb_sellmat *m, const double *d_x, double *d_y, float *kernel_us) {
+    if (!m || !d_x || !d_y) return fail(ALB_ERR_INVALID, "alb_sellmat_spmv: bad arguments");
+    ALB_CK(cudaSetDevice(m->device));
+    ALB_TRY(launch(m, d_x, d_y, kernel_us));
+    ALB_CK(cudaStreamSynchronize(m->stream));
+    return ALB_OK;
+}
+
+alb_status alb_sellmat_spmv_host(alb_sellmat *m, const double *x, double *y) {
+    if (!m || !x || !y) return fail(ALB_ERR_INVALID, "alb_sellmat_spmv_host: bad arguments");
+    ALB_CK(cudaSetDevice(m->device));
+    if (!m->dx) ALB_TRY(dmalloc((void **)&m->dx, sizeof(double) * (size_t)m->n, "SpMV x"));
+    if (!m->dy) ALB_TRY(dmalloc((void **)&m->dy, sizeof(double) * (size_t)m->n, "SpMV y"));
+    ALB_CK(cudaMemcpyAsync(m->dx, x, sizeof(double) * (size_t)m->n, cudaMemcpyHostToDevice,
+                           m->stream));
+    ALB_TRY(launch(m, m->dx, m->dy, nullptr));
+    ALB_CK(cudaMemcpyAsync(y, m->dy, sizeof(double) * (size_t)m->n, cudaMemcpyDeviceToHost,
+                           m->stream));
+    ALB_CK(cudaStreamSynchronize(m->stream));
+    return ALB_OK;
+}
+
+}  // extern "C"

@@ -204,6 +204,21 @@ typedef struct {
     float step_us;         /* CUDA-event time of the step kernels (host loop
                               only; -1 otherwise) */
     int32_t pad_;
+    /* Bypass statistics of the single-root BFS, counted by the kernels (the
+     * reference records slice and column bypass per level,
+     * bfs/src/bfs_SELLCSv2.c:773-818, counted at bfs/src/bfs_par_kernels.c:
+     * 192 and 630; 0 for the 64-root batched BFS). Bottom-up levels: */
+    int64_t words_bypassed;  /* 32-row bitmap words skipped because every row
+                                in them was visited (slice bypass) */
+    int64_t rows_scanned;    /* unvisited rows whose SELL columns were read */
+    int64_t groups_read;     /* 4-column groups those rows read */
+    int64_t groups_bypassed; /* groups of those rows (up to the slice width)
+                                left unread because the row stopped at its
+                                first frontier source or its end (column
+                                bypass) */
+    /* Top-down levels: */
+    int64_t edges_bypassed;  /* pushed entries whose target was already
+                                visited (no parent/claim update issued) */
 } alb_level_rec;
 /* Algorithmic bytes (the elements the step reads or writes, counted by the
  * kernels themselves): bottom-up = 12*nwords (visited read and write, next
@@ -305,11 +320,47 @@ alb_status alb_selector_train(const float *x, const float *y, const float *mask,
                               int32_t steps, float lr, uint64_t seed, int32_t init,
                               float *params, float *loss);
 
+/* ----------------------------------------------- fp64 SELL-C-sigma SpMV */
+
+/* y = A x in fp64 over a SELL-C-sigma matrix on the device. Replaces the
+ * reference's kernel_SELLCS_DFC (bfs/src/bfs_par_kernels.c:8-53) and its
+ * matrix build convert_csr_to_sellcs_dfc (bfs/src/sparse_matrix.c:523-623):
+ * row r accumulates values[e] * x[col[e]] over its entries in CSR order with
+ * one fused multiply-add each, starting from 0 -- the reference's per-lane
+ * vfmadd chain -- so y is bit-identical to the reference's for the same CSR.
+ * Rows are ordered by length inside sigma windows (1..16384) as in the
+ * reference; slices hold 32 rows, entries 4-interleaved (int32 columns,
+ * fp64 values), diagonal and repeated entries kept as given. */
+typedef struct alb_sellmat alb_sellmat;
+alb_status alb_sellmat_create(int64_t n, const int64_t *rowptr, const int32_t *col,
+                              const double *values, int32_t sigma, alb_sellmat **out);
+void alb_sellmat_destroy(alb_sellmat *m);
+/* n, entries, and stored SELL slots (entries + padding). */
+alb_status alb_sellmat_info(const alb_sellmat *m, int64_t *n, int64_t *nnz, int64_t *stored);
+/* Device vectors x[n], y[n] (current device); kernel_us (may be NULL)
+ * receives the kernel's CUDA-event time in microseconds. */
+alb_status alb_sellmat_spmv(alb_sellmat *m, const double *d_x, double *d_y, float *kernel_us);
+/* Host vectors, copied in and out. */
+alb_status alb_sellmat_spmv_host(alb_sellmat *m, const double *x, double *y);
+
 /* ---------------------------------------------------------------- testing */
 
 /* Host-side fault injection: the k-th next device allocation made by the
  * library fails with ALB_ERR_OOM (k >= 1); k = 0 disarms. */
 void alb_debug_fail_alloc_after(int32_t k);
+
+/* Test hooks for the bounded device-side waits (the reference has no
+ * failure handling: bfs/src/utils.c:102-109 exits). timeout_us > 0 makes
+ * every such wait give up after timeout_us instead of seconds;
+ * withhold_level >= 0 makes block withhold_block skip its arrival at the grid
+ * barriers of that level (the persistent level loop and
+ * alb_bfs_csr_noalloc), so the other blocks' waits run out; short_bulk != 0
+ * makes the staged bottom-up pass expect 16 bytes more than its bulk copy
+ * delivers, so its wait runs out. The call that hits one returns
+ * ALB_ERR_TIMEOUT; nothing faults and the next call on the same graph runs
+ * normally. (-1, 0, 0, 0) turns everything off. */
+void alb_debug_device_waits(int32_t withhold_level, int32_t withhold_block, int32_t short_bulk,
+                            int64_t timeout_us);
 
 #ifdef __cplusplus
 }

@@ -62,6 +62,8 @@ def lib() -> C.CDLL:
         P = C.c_void_p
         L.orc_bfs.restype = C.c_int32
         L.orc_bfs.argtypes = [C.c_int64, P, P, P, P, C.c_int32, P, P]
+        L.orc_spmv.restype = None
+        L.orc_spmv.argtypes = [C.c_int64, P, P, P, P, P]
         L.orc_level_counts.restype = None
         L.orc_level_counts.argtypes = [C.c_int64, P, C.c_int32, P]
         L.orc_validate.restype = C.c_int32
@@ -110,6 +112,16 @@ def bfs(rowptr, col, root, in_rowptr=None, in_col=None):
     nl = lib().orc_bfs(n, rp.ctypes.data, cl.ctypes.data, irp.ctypes.data, icl.ctypes.data,
                        int(root), level.ctypes.data, parent.ctypes.data)
     return level, parent, nl
+
+
+def spmv(rowptr, col, val, x):
+    """y = A x in fp64, one fused multiply-add per entry in CSR order."""
+    rp, cl = _a(rowptr, np.int64), _a(col, np.int32)
+    v, xx = _a(val, np.float64), _a(x, np.float64)
+    n = rp.shape[0] - 1
+    y = np.empty(n, np.float64)
+    lib().orc_spmv(n, rp.ctypes.data, cl.ctypes.data, v.ctypes.data, xx.ctypes.data, y.ctypes.data)
+    return y
 
 
 def level_counts(level, num_levels):

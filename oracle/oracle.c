@@ -360,3 +360,18 @@ void orc_adam_step(float *params, const float *grad, float *m, float *v,
         params[i] -= lr * mh / (sqrtf(vh) + eps);
     }
 }
+
+/* kernel_SELLCS_DFC (bfs/src/bfs_par_kernels.c:8-53), row by row: entry k of
+ * row r sits in column op k of r's slice lane, so the lane's accumulator sees
+ * the row's entries in CSR order. */
+void orc_spmv(int64_t n, const int64_t *rowptr, const int32_t *col, const double *val,
+              const double *x, double *y)
+{
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t r = 0; r < n; r++) {
+        double acc = 0.0;
+        for (int64_t e = rowptr[r]; e < rowptr[r + 1]; e++)
+            acc = fma(val[e], x[col[e]], acc);
+        y[r] = acc;
+    }
+}

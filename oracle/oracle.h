@@ -90,6 +90,14 @@ int64_t orc_sell_long(int64_t n, const int64_t *rowptr, const int32_t *adj,
                       const int32_t *order, int32_t long_row, int32_t *lrow,
                       int64_t *lptr, int32_t *lcol);
 
+/* y = A x in fp64 as the reference's SELL-C-sigma SpMV computes it
+ * (kernel_SELLCS_DFC, bfs/src/bfs_par_kernels.c:8-53): row r accumulates
+ * values * x[col] over its entries in CSR order with one fused multiply-add
+ * each (_vel_vfmadd_vvvvl), starting from 0; the SELL layout only changes
+ * which lane does the row, not the order of its operations. */
+void orc_spmv(int64_t n, const int64_t *rowptr, const int32_t *col, const double *val,
+              const double *x, double *y);
+
 /* Timed CPU port of the reference's level loop (C = 256 SELL with active-lane
  * ("DFC") layout, pull kernel above 4% of n frontier, sparse-x kernel below),
  * for a symmetric graph. Root is relabelled by the caller-independent rule of

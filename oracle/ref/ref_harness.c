@@ -11,6 +11,8 @@
  *   get_order_by_row_size_radix  bfs/src/sorting_utils.c:232-253
  *   convert_csr_to_sellcs        bfs/src/sparse_matrix.c:435-521
  *   convert_csr_to_sellcs_dfc    bfs/src/sparse_matrix.c:523-623
+ *   kernel_SELLCS_DFC            bfs/src/bfs_par_kernels.c:8-53 (fp64 SpMV, through
+ *                                the scalar restatement in ve_scalar.c)
  *   run_custom_bfs_test          bfs/src/bfs_SELLCSv2.c:126-820 (root row 0)
  *   mmio_info, mmio_data         bfs/src/mmio_highlevel.h:11-263 (.mtx -> CSR)
  *   the undirected conversion    bfs/src/main.c:127-163 (CSR merged with its
@@ -150,6 +152,39 @@ int refh_sell_dfc(int n, const int *rowptr, const int *col, int sigma,
     free(rows_size);
     free_csr(&m);
     return nops;
+}
+
+/* y = A x through the reference's fp64 SELL-C-sigma SpMV: the DFC matrix
+ * (C = 256) built by convert_csr_to_sellcs_dfc from a CSR with the given
+ * values, then kernel_SELLCS_DFC over all slices. */
+void refh_spmv_dfc(int n, const int *rowptr, const int *col, const double *values, int sigma,
+                   const double *x, double *y)
+{
+    SparseMatrixCSR m;
+    make_csr(&m, n, rowptr, col);
+    for (int i = 0; i < rowptr[n]; i++)
+        m.values[i] = values[i];
+    int padded = 0;
+    int *rows_size = get_rows_size(m.row_pointers, n, &padded);
+    int *row_order = get_order_by_row_size_radix(rows_size, n, sigma);
+    SparseMatrixSELLCS s;
+    memset(&s, 0, sizeof(s));
+    s.C = 256;
+    s.sigma = sigma;
+    convert_csr_to_sellcs_dfc(&m, &s, rows_size, row_order, 0);
+    s.row_order = row_order;
+    kernel_SELLCS_DFC(&s, x, y, 0, s.nslices);
+    free(s.slice_widths);
+    free(s.vop_pointers);
+    free(s.vop_lengths);
+    free(s.slice_pointers);
+    free(s.max_index);
+    free(s.min_index);
+    free(s.column_indices);
+    free(s.values);
+    free(row_order);
+    free(rows_size);
+    free_csr(&m);
 }
 
 /* The reference's own level loop from row 0 (verify on, so frontier sizes

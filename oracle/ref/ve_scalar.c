@@ -20,6 +20,8 @@
  * and equal switch thresholds (bfs_SELLCSv2.c:283-284, main.c:189); they
  * only record that they were called.
  */
+#include <math.h>
+
 #include "bfs_par_kernels.h"
 
 int ve_scalar_dead_calls = 0;
@@ -54,8 +56,8 @@ void kernel_SELLCS_DFC(const SparseMatrixSELLCS *restrict m, const elem_t *restr
         int op = m->vop_pointers[s];
         for (int i = 0; i < m->slice_widths[s]; i++) {
             int act = (int)m->vop_lengths[op++] + 1;
-            for (int l = 0; l < act; l++)
-                acc[l] += m->values[at + l] * x[m->column_indices[at + l]];
+            for (int l = 0; l < act; l++) /* _vel_vfmadd_vvvvl: one rounding */
+                acc[l] = fma(x[m->column_indices[at + l]], m->values[at + l], acc[l]);
             at += act;
         }
         for (int l = 0; l < lanes; l++)

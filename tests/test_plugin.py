@@ -108,3 +108,27 @@ def test_plugin_matches_run_bfs_ref_counts(perf):
         got = np.ctypeslib.as_array(lib.bfs_gb300_last_levels(), shape=(g.n,))
         gotp = np.ctypeslib.as_array(lib.bfs_gb300_last_parents(), shape=(g.n,))
         assert np.array_equal(got, lv) and np.array_equal(gotp, pa)
+
+
+@pytest.mark.gpu
+def test_plugin_writes_bypass_records(tmp_path, monkeypatch):
+    """bypass_record = 1: one line per run in the reference's slice- and
+    column-bypass CSV files (bfs/src/bfs_SELLCSv2.c:773-818), its counts the
+    kernels' per-level bypass statistics."""
+    lib = plugin()
+    g = ab.gen_rmat(14, 16, seed=31)
+    monkeypatch.setenv("ALB_BYPASS_DIR", str(tmp_path))
+    C.c_int.in_dll(lib, "bypass_record").value = 1
+    try:
+        out = call(lib, g, 0, verify=1)
+    finally:
+        C.c_int.in_dll(lib, "bypass_record").value = 0
+    for fname in ("bfs-slice-bypass.csv", "bfs-column-bypass.csv"):
+        line = (tmp_path / fname).read_text().strip().split(",")
+        assert line[0] == "graph" and int(line[1]) == g.n and int(line[3]) == g.nnz
+        assert int(line[4]) == out["num_iter"]
+        counts = [int(x) for x in line[6:]]
+        assert len(counts) == out["num_iter"] and all(c >= 0 for c in counts)
+    slices = [int(x) for x in (tmp_path / "bfs-slice-bypass.csv").read_text().split(",")[6:]]
+    # the levels after the largest pull skip fully visited words
+    assert sum(slices) > 0
