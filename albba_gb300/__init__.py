@@ -20,9 +20,11 @@ import numpy as np
 
 _PKG = Path(__file__).resolve().parent
 # ALB_LIBRARY=checked loads the bounds-checked build (tests of the kernels'
-# index discipline); the default is the production library
-LIB_PATH = _PKG / ("libalbba_gb300_checked.so" if os.environ.get("ALB_LIBRARY") == "checked"
-                   else "libalbba_gb300.so")
+# index discipline), ALB_LIBRARY=<path to a .so> another build of the same
+# ABI; the default is the production library
+_sel = os.environ.get("ALB_LIBRARY", "")
+LIB_PATH = (_PKG / "libalbba_gb300_checked.so" if _sel == "checked"
+            else Path(_sel) if _sel.endswith(".so") else _PKG / "libalbba_gb300.so")
 
 if not LIB_PATH.exists():
     raise ImportError(
@@ -168,6 +170,7 @@ _sigs = {
     "alb_worklist_run_device": (C.c_int32, [_P, C.c_int32, _P, C.POINTER(Stats)]),
     "alb_selector_load": (C.c_int32, [C.c_int32, _P]),
     "alb_selector_clear": (C.c_int32, [C.c_int32]),
+    "alb_spmspv_merge": (C.c_int32, [_P, _P, C.c_int64, _P, _P, _i64p]),
     "alb_sellmat_create": (C.c_int32, [C.c_int64, _P, _P, _P, C.c_int32, C.POINTER(_P)]),
     "alb_sellmat_destroy": (None, [_P]),
     "alb_sellmat_info": (C.c_int32, [_P, _i64p, _i64p, _i64p]),
@@ -393,6 +396,17 @@ class Graph:
         col = np.empty(max(int(rp[-1]), 1), np.int32)
         check(_lib.alb_graph_export_csr(self._h, side, None, col.ctypes.data))
         return Csr(rp, col[: int(rp[-1])])
+
+    def spmspv_merge(self, frontier, visited_bits) -> np.ndarray:
+        """Ascending distinct unvisited out-neighbours of the frontier
+        (alb_spmspv_merge); visited_bits: uint32 bitmap over original ids."""
+        x = np.ascontiguousarray(frontier, dtype=np.int32)
+        vb = np.ascontiguousarray(visited_bits, dtype=np.uint32)
+        y = np.empty(self.n, np.int32)
+        ny = C.c_int64()
+        check(_lib.alb_spmspv_merge(self._h, x.ctypes.data, x.shape[0], vb.ctypes.data,
+                                    y.ctypes.data, C.byref(ny)))
+        return y[: ny.value]
 
     @property
     def symmetric(self) -> bool:

@@ -136,16 +136,18 @@ __device__ __forceinline__ void add_stat(const BfsArgs &a, int L, int which, uns
 }
 
 // Pushed edges u -> v (u's original id ou): the smallest source wins the
-// parent, and v's bit goes into the next-frontier bitmap N (the next queue,
-// levels and counters are made from N by td_finish_phase, so no counter is
-// shared by every claim).
+// parent, and v's bit goes into the next-frontier bitmap N. The next queue,
+// levels and counters are made from N by td_finish_phase (no counter shared
+// by every claim) -- or, in append mode (a small frontier, where scanning all
+// of N would cost more than the level), the claimer of v (the push whose
+// atomicOr set v's bit) records v for the next queue.
 // Four edges per lane (v[k] < 0: none): the visited words of all four are
 // requested together, then the parent and bitmap words of the unvisited
 // targets together, then the atomics, so one lane keeps four loads in
 // flight where one edge at a time kept one.
 __device__ __forceinline__ void push_edges4(const BfsArgs &a, uint32_t *N, const int32_t (&v)[4],
                                             const uint32_t (&ou)[4], bool persist,
-                                            unsigned &bypassed) {
+                                            unsigned &bypassed, bool append, unsigned &claimed) {
     bool live[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
@@ -174,9 +176,42 @@ __device__ __forceinline__ void push_edges4(const BfsArgs &a, uint32_t *N, const
         if (!live[k]) continue;
         const uint32_t bit = 1u << (v[k] & 31);
         if (ou[k] < cur_parent[k]) atomicMin(a.parent_pos + v[k], ou[k]);
-        if (!(cur_n[k] & bit)) atomicOr(N + (v[k] >> 5), bit);
+        if (!(cur_n[k] & bit)) {
+            const uint32_t old = atomicOr(N + (v[k] >> 5), bit);
+            if (append && !(old & bit)) claimed |= 1u << k;
+        }
     }
 }
+
+// Appends the warp's claimed targets (bit k of claimed: v[k], one lane's
+// four edges of push_edges4) to the next queue, one atomicAdd per warp. Call
+// from all lanes of a warp.
+__device__ __forceinline__ void flush_claims(const BfsArgs &a, int32_t *NQ,
+                                             unsigned long long *nq_slot, const int32_t (&v)[4],
+                                             unsigned &claimed) {
+    const int lane = threadIdx.x & 31;
+    const int cnt = __popc(claimed);
+    const int inc = warp_inclusive_scan(cnt);
+    const int tot = __shfl_sync(kFull, inc, 31);
+    if (tot) {
+        unsigned long long base = 0;
+        if (lane == 31) base = atomicAdd(nq_slot, (unsigned long long)tot);
+        base = __shfl_sync(kFull, base, 31);
+        int64_t pos = (int64_t)base + inc - cnt;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (!((claimed >> k) & 1u)) continue;
+            if (ALB_CHECK_POS(pos, a.n, &a.ctl->err)) NQ[pos] = v[k];
+            pos++;
+        }
+    }
+    claimed = 0;
+}
+
+// Append mode for a top-down level: the frontier's push edges are no more
+// than the bitmap's words, so the next queue is built by the claims rather
+// than by scanning the whole next-frontier bitmap.
+__device__ __forceinline__ bool td_append(const BfsArgs &a, int64_t mf) { return mf <= a.nwords; }
 
 // Rows per warp for the short-row pass: as many frontier rows as keep every
 // warp busy (1 when the frontier is small, up to 32 when it is large).
@@ -193,8 +228,11 @@ constexpr int kBigShift = 38;
 constexpr unsigned long long kBigMask = (1ull << kBigShift) - 1;
 
 template <bool kPersist>
-__device__ void td_phase(const BfsArgs &a, int L, Range r) {
+__device__ void td_phase(const BfsArgs &a, int L, Range r, bool append) {
     const int32_t *Q = (L & 1) ? a.q1 : a.q0;
+    int32_t *NQ = (L & 1) ? a.q0 : a.q1;
+    unsigned long long *nq_slot = &a.ctl->qn[(L + 1) % 3];
+    unsigned claimed = 0;
     uint32_t *N = (L & 1) ? a.bm0 : a.bm1;
     const int64_t qlen = (int64_t)ld_state<kPersist>(&a.ctl->qn[L % 3]);
     unsigned long long *big_slot = &a.ctl->nbig[L % 3];
@@ -233,7 +271,10 @@ __device__ void td_phase(const BfsArgs &a, int L, Range r) {
         s_st[wib][lane] = st;
         s_ou[wib][lane] = ou;
         __syncwarp();
-        for (int64_t e0 = lane; e0 < T; e0 += 128) {
+        // the loop bound is warp-uniform (lanes past T carry no edge) so that
+        // append mode can flush its claims with warp collectives
+        for (int64_t eb = 0; eb < T; eb += 128) {
+            const int64_t e0 = eb + lane;
             int32_t v[4];
             uint32_t ou4[4];
 #pragma unroll
@@ -251,7 +292,8 @@ __device__ void td_phase(const BfsArgs &a, int L, Range r) {
                     ou4[k] = (uint32_t)s_ou[wib][j];
                 }
             }
-            push_edges4(a, N, v, ou4, kPersist, bypassed);
+            push_edges4(a, N, v, ou4, kPersist, bypassed, append, claimed);
+            if (append) flush_claims(a, NQ, nq_slot, v, claimed);
         }
         __syncwarp();
     }
@@ -263,7 +305,7 @@ __device__ void td_phase(const BfsArgs &a, int L, Range r) {
 // first chunk by binary search over the chunk bases (monotone in the list
 // index) and walks forward from there.
 template <bool kPersist>
-__device__ void td_big_phase(const BfsArgs &a, int L, Range r) {
+__device__ void td_big_phase(const BfsArgs &a, int L, Range r, bool append) {
     const unsigned long long ctr = ld_state<kPersist>(&a.ctl->nbig[L % 3]);
     if (ctr == 0) return;
     const int64_t nbig = (int64_t)(ctr >> kBigShift);
@@ -276,6 +318,9 @@ __device__ void td_big_phase(const BfsArgs &a, int L, Range r) {
     const int64_t per = (total + nwarps - 1) / nwarps;
     const int64_t k0 = gw * per, k1 = min(total, k0 + per);
     unsigned bypassed = 0;
+    int32_t *NQ = (L & 1) ? a.q0 : a.q1;
+    unsigned long long *nq_slot = &a.ctl->qn[(L + 1) % 3];
+    unsigned claimed = 0;
     if (k0 >= k1) {
         add_stat(a, L, kStEdgesBypassed, bypassed);  // keeps every lane at the shuffle
         return;
@@ -313,7 +358,8 @@ __device__ void td_big_phase(const BfsArgs &a, int L, Range r) {
             if (v[q] >= 0) ALB_CHECK_ID(v[q], a.n, -1, &a.ctl->err);
             ou4[q] = ou;
         }
-        push_edges4(a, N, v, ou4, kPersist, bypassed);
+        push_edges4(a, N, v, ou4, kPersist, bypassed, append, claimed);
+        if (append) flush_claims(a, NQ, nq_slot, v, claimed);
     }
     add_stat(a, L, kStEdgesBypassed, bypassed);
 }
@@ -323,7 +369,7 @@ __device__ void td_big_phase(const BfsArgs &a, int L, Range r) {
 // the warp, one atomic per warp), recording levels and counters and marking
 // the new vertices visited (each word by the one thread that owns it).
 template <bool kPersist>
-__device__ void td_finish_phase(const BfsArgs &a, int L, Range r) {
+__device__ void td_finish_phase(const BfsArgs &a, int L, Range r, bool append) {
     const int32_t *Q = (L & 1) ? a.q1 : a.q0;
     int32_t *NQ = (L & 1) ? a.q0 : a.q1;
     uint32_t *F = (L & 1) ? a.bm1 : a.bm0;
@@ -337,8 +383,21 @@ __device__ void td_finish_phase(const BfsArgs &a, int L, Range r) {
     const int32_t lvl = L + 1;
     unsigned cn = 0, full = 0;
     unsigned long long cmo = 0, cmi = 0;
+    if (append) {  // the claims built the next queue: walk it
+        const int64_t nq = (int64_t)ld_state<kPersist>(nq_slot);
+        for (int64_t i = tid; i < nq; i += nth) {
+            const int32_t v = ld_state<kPersist>(NQ + i);
+            const uint32_t bit = 1u << (v & 31);
+            const uint32_t old = atomicOr(a.vis + (v >> 5), bit);
+            full += (old != kFull && (old | bit) == kFull);
+            a.level_pos[v] = lvl;
+            cn++;
+            cmo += (unsigned long long)__ldg(a.odeg + v);
+            cmi += (unsigned long long)__ldg(a.ideg + v);
+        }
+    }
     // the loop bound is warp-uniform so that every lane reaches the shuffles
-    for (int64_t w0 = tid & ~31ll; w0 < a.nwords; w0 += nth) {
+    for (int64_t w0 = append ? a.nwords : (tid & ~31ll); w0 < a.nwords; w0 += nth) {
         const int64_t w = w0 + lane;
         uint32_t m = w < a.nwords ? ld_bits<kPersist>(N + w) : 0u;
         const int cnt = __popc(m);
@@ -395,6 +454,10 @@ __device__ __forceinline__ uint32_t ld_front(const uint32_t *F, int32_t w) {
 // kEarly: stop each row at its first frontier source or its padding.
 // Fs: where the frontier words are read (the global bitmap, or its copy in
 // shared memory when kSmemF).
+// Words per run of the bottom-up pull (a warp's unit of work from the
+// level's counter): one visited word per lane.
+constexpr int64_t kBuRun = 32;
+
 template <bool kPersist, bool kBypass, bool kEarly, bool kSmemF = false>
 __device__ void bu_phase(const BfsArgs &a, int L, Range r, const uint32_t *Fs = nullptr) {
     const uint32_t *F = kSmemF ? Fs : ((L & 1) ? a.bm1 : a.bm0);
@@ -407,71 +470,107 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r, const uint32_t *Fs = 
     unsigned long long cmo = 0, cmi = 0, bytes = 0;
     unsigned n_wbyp = 0, n_rows = 0, n_grp = 0, n_gtot = 0;
     const uint64_t pol = l2_evict_first();
-    // words come in runs from the level's counter; the next word's visited
-    // mask is requested one iteration ahead (only the warp that takes a word
-    // writes it during the level), and a word's slice geometry is requested
-    // without waiting for its mask
+    // Words come in runs of kBuRun from the level's counter. Lane l holds the
+    // visited mask of word l of the run (one coalesced load, the next run's
+    // requested one run ahead; only the warp that takes a word writes its
+    // mask during the level). With kBypass the run's fully visited words are
+    // skipped together: their next-frontier words are cleared by one store
+    // per lane and only the other words are walked, one at a time.
     unsigned long long *ctr = &a.ctl->work[L % 3];
-    WordRuns runs;
-    int64_t w = runs.first(ctr, a.nwords);
-    // A word's visited mask and slice geometry are requested one word ahead,
-    // and its first column group as soon as they are in, while the word
-    // before it is processed: a word starts with its columns at hand rather
-    // than three dependent round trips behind. (Only the warp that takes a
-    // word writes its visited mask during the level.)
-    auto geometry = [&](int64_t ww, uint32_t &vv, int32_t &wdv, int64_t &sov) {
-        vv = kFull;
-        wdv = 0;
-        sov = 0;
-        if (ww < a.nwords) {
-            vv = ld_bits<kPersist>(a.vis + ww);
-            const int32_t pw = (int32_t)(ww * 32 + lane);
-            // rows past n are preset visited; clamp their slice index
-            const int64_t sw = (int64_t)(pw < a.n ? pw : a.n - 1) >> log2C;
-            wdv = __ldg(a.width + sw);
-            sov = __ldg(a.slice_off + sw);
-        }
+    auto grab = [&]() {
+        unsigned long long v = 0;
+        if (lane == 0) v = atomicAdd(ctr, (unsigned long long)kBuRun);
+        return (int64_t)__shfl_sync(kFull, v, 0);
     };
-    auto first_group = [&](int64_t ww, uint32_t vv, int32_t wdv, int64_t sov) {
-        const int32_t pw = (int32_t)(ww * 32 + lane);
-        int4 g0 = make_int4(pw, pw, pw, pw);
-        if (ww < a.nwords && !(kBypass && vv == kFull) && !((vv >> lane) & 1u) && wdv > 0)
-            g0 = ld_stream(a.col4 + (sov >> 2) + (pw & (C - 1)), pol);
-        return g0;
+    auto run_vis = [&](int64_t rw) {
+        return rw + lane < a.nwords ? ld_bits<kPersist>(a.vis + rw + lane) : kFull;
     };
-    uint32_t vis_c;
-    int32_t wd_c;
-    int64_t so_c;
-    geometry(w, vis_c, wd_c, so_c);
-    int4 f0 = first_group(w, vis_c, wd_c, so_c);
-    for (int64_t wn; w < a.nwords; w = wn) {
-        wn = runs.after(w, ctr, a.nwords);
-        uint32_t vis_n;
-        int32_t wd_n;
-        int64_t so_n;
-        geometry(wn, vis_n, wd_n, so_n);
-        const uint32_t vis = vis_c;
-        if (kBypass && vis == kFull) {
-            if (lane == 0) {
-                N[w] = 0;
-                n_wbyp++;
-            }
-            f0 = first_group(wn, vis_n, wd_n, so_n);
-            vis_c = vis_n;
-            wd_c = wd_n;
-            so_c = so_n;
-            continue;
+    int64_t cur = grab(), nxt = grab();
+    uint32_t vcur = run_vis(cur), vnxt = run_vis(nxt);
+    while (cur < a.nwords) {
+        unsigned todo;
+        if (kBypass) {
+            const bool valid = cur + lane < a.nwords;
+            const bool full_w = valid && vcur == kFull;
+            if (full_w) N[cur + lane] = 0;
+            n_wbyp += full_w;
+            todo = __ballot_sync(kFull, valid && !full_w);
+        } else {
+            todo = __ballot_sync(kFull, cur + lane < a.nwords);
         }
+        const int64_t base_w = cur;
+        const uint32_t vrun = vcur;
+        cur = nxt;
+        vcur = vnxt;
+        if (cur < a.nwords) {
+            nxt = grab();
+            vnxt = run_vis(nxt);
+        }
+        // Slices of C >= 32 rows: a word lies inside one slice, so lane l
+        // loads the geometry (width, offset) of word l of the run, and a
+        // word's first column group can be requested as soon as the word
+        // before it starts -- its columns then arrive while that word waits
+        // on its frontier gathers. (C < 32: each row's slice is loaded per
+        // word, no lookahead.)
+        const bool run_geom = log2C >= 5;
+        int32_t wd_l = 0;
+        int64_t so_l = 0;
+        if (run_geom && base_w + lane < a.nwords) {
+            const int64_t sl = (base_w + lane) >> (log2C - 5);
+            wd_l = __ldg(a.width + sl);
+            so_l = __ldg(a.slice_off + sl);
+        }
+        // first column group of word q of the run (rows' own position when
+        // the row is visited or empty)
+        auto first_group = [&](int q, uint32_t vq) {
+            const int32_t pq = (int32_t)((base_w + q) * 32 + lane);
+            int4 g0 = make_int4(pq, pq, pq, pq);
+            const int32_t wdq = __shfl_sync(kFull, wd_l, q);
+            const int64_t soq = __shfl_sync(kFull, so_l, q);
+            if (!((vq >> lane) & 1u) && wdq > 0)
+                g0 = ld_stream(a.col4 + (soq >> 2) + (pq & (C - 1)), pol);
+            return g0;
+        };
+        int4 c_next = make_int4(0, 0, 0, 0);
+        if (run_geom && todo) {
+            const int q0 = __ffs(todo) - 1;
+            c_next = first_group(q0, __shfl_sync(kFull, vrun, q0));
+        }
+      while (todo) {
+        const int q = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const int64_t w = base_w + q;
+        const uint32_t vis = __shfl_sync(kFull, vrun, q);
         const int32_t p = (int32_t)(w * 32 + lane);
+        int32_t wd;
+        int64_t so;
+        if (run_geom) {
+            wd = __shfl_sync(kFull, wd_l, q);
+            so = __shfl_sync(kFull, so_l, q);
+        } else {
+            // rows past n are preset visited; clamp their slice index
+            const int64_t s = (int64_t)(p < a.n ? p : a.n - 1) >> log2C;
+            wd = __ldg(a.width + s);
+            so = __ldg(a.slice_off + s);
+        }
         bool active = !((vis >> lane) & 1u);
-        const int32_t ng = active ? (wd_c + 3) >> 2 : 0;
+        const int32_t ng = active ? (wd + 3) >> 2 : 0;
         n_rows += ng > 0;
         n_gtot += ng;
-        const int4 *cp = a.col4 + (so_c >> 2) + (p & (C - 1));
+        const int4 *cp = a.col4 + (so >> 2) + (p & (C - 1));
         int32_t found = -1;
         // group j+1 is requested before group j's frontier tests, so each lane
         // keeps one column load in flight while it waits on the bitmap
-        int4 c = f0;
+        int4 c = make_int4(p, p, p, p);
+        if (run_geom) {
+            c = c_next;  // requested when the previous word started
+            if (todo) {
+                const int q2 = __ffs(todo) - 1;
+                c_next = first_group(q2, __shfl_sync(kFull, vrun, q2));
+            }
+        } else if (active && ng > 0) {
+            c = ld_stream(cp, pol);
+        }
         // an unvisited row whose first entry is padding is a long row (rows
         // without sources start visited): the long-row pass has run already
         const bool long_cand = active && c.x == p;
@@ -522,10 +621,7 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r, const uint32_t *Fs = 
             cmo += (unsigned long long)__ldg(a.odeg + p);
             cmi += (unsigned long long)__ldg(a.ideg + p);
         }
-        f0 = first_group(wn, vis_n, wd_n, so_n);
-        vis_c = vis_n;
-        wd_c = wd_n;
-        so_c = so_n;
+      }
     }
     add_stat(a, L, kStWordsBypassed, n_wbyp);
     add_stat(a, L, kStRowsScanned, n_rows);
@@ -809,15 +905,18 @@ __global__ void k_prep(BfsArgs a) {
 }
 
 __global__ void k_td(BfsArgs a) {
-    td_phase<false>(a, a.ctl->level, Range{(int)blockIdx.x, (int)gridDim.x});
+    td_phase<false>(a, a.ctl->level, Range{(int)blockIdx.x, (int)gridDim.x},
+                    td_append(a, a.ctl->mf));
 }
 
 __global__ void k_td_big(BfsArgs a) {
-    td_big_phase<false>(a, a.ctl->level, Range{(int)blockIdx.x, (int)gridDim.x});
+    td_big_phase<false>(a, a.ctl->level, Range{(int)blockIdx.x, (int)gridDim.x},
+                        td_append(a, a.ctl->mf));
 }
 
 __global__ void k_td_finish(BfsArgs a) {
-    td_finish_phase<false>(a, a.ctl->level, Range{(int)blockIdx.x, (int)gridDim.x});
+    td_finish_phase<false>(a, a.ctl->level, Range{(int)blockIdx.x, (int)gridDim.x},
+                           td_append(a, a.ctl->mf));
 }
 
 // The slice pass runs with kBuBlock threads whatever the loop's block size:
@@ -939,7 +1038,7 @@ __device__ bool grid_sync(const BfsArgs &a, unsigned nblocks, int L) {
     return *(volatile int32_t *)&ctl->err == 0;
 }
 
-__global__ void __launch_bounds__(256) k_persistent(BfsArgs a) {
+__global__ void __launch_bounds__(256, 3) k_persistent(BfsArgs a) {
     __shared__ BfsCtl c;
     __shared__ int s_dir;
     const unsigned nb = gridDim.x;
@@ -975,16 +1074,17 @@ __global__ void __launch_bounds__(256) k_persistent(BfsArgs a) {
                 prep_phase<true>(a, L, !c.q_valid, c.n_dirty != 0, r);
                 ok = grid_sync(a, nb, L);
             }
+            const bool app = td_append(a, c.mf);
             if (ok) {
-                td_phase<true>(a, L, r);
+                td_phase<true>(a, L, r, app);
                 ok = grid_sync(a, nb, L);
             }
             if (ok && *(volatile unsigned long long *)&a.ctl->nbig[L % 3]) {
-                td_big_phase<true>(a, L, r);
+                td_big_phase<true>(a, L, r, app);
                 ok = grid_sync(a, nb, L);
             }
             if (ok) {
-                td_finish_phase<true>(a, L, r);
+                td_finish_phase<true>(a, L, r, app);
                 ok = grid_sync(a, nb, L);
             }
         } else if (dir == ALB_DIR_BOTTOMUP) {

@@ -373,21 +373,6 @@ __global__ void __launch_bounds__(kMsBuBlock, kWide ? 4 : 5) k_ms_bu(MsArgs a, i
     int32_t wd_c;
     int64_t so_c;
     geometry(w, d, vis_c, wd_c, so_c);
-    // a word's first column groups are requested while the previous word is
-    // processed (its geometry came in one word ahead), so a word starts with
-    // its columns at hand instead of one DRAM round trip behind
-    auto first_groups = [&](int64_t ww, uint32_t dd, uint64_t vv, int32_t wdv, int64_t sov,
-                            int4 &g0, int4 &g1) {
-        const int32_t pw = (int32_t)(ww * 32 + lane);
-        g0 = g1 = make_int4(pw, pw, pw, pw);
-        if (ww >= a.nwords || (kBypass && dd == kFull) || (vv | tm) == kAll) return;
-        const int32_t ngw = (wdv + 3) >> 2;
-        const int4 *cpw = a.col4 + (sov >> 2) + (pw & (a.C - 1));
-        if (ngw > 0) g0 = ld_stream(cpw, pol);
-        if (kWide && !kFilt && ngw > 1) g1 = ld_stream(cpw + a.C, pol);
-    };
-    int4 f0, f1;
-    first_groups(w, d, vis_c, wd_c, so_c, f0, f1);
     while (w < a.nwords) {
         uint64_t vis1;
         int32_t wd1;
@@ -411,7 +396,9 @@ __global__ void __launch_bounds__(kMsBuBlock, kWide ? 4 : 5) k_ms_bu(MsArgs a, i
             const int32_t pp = (int32_t)p;
             if (kWide && !kFilt) {
                 const int4 pad = make_int4(pp, pp, pp, pp);
-                int4 c0 = f0, c1 = f1;
+                int4 c0 = pad, c1 = pad;
+                if (active && ng > 0) c0 = ld_stream(cp, pol);
+                if (active && ng > 1) c1 = ld_stream(cp + a.C, pol);
                 for (int32_t g = 0;; g += 2) {
                     active = active && g < ng;
                     if (!__any_sync(kFull, active)) break;
@@ -431,7 +418,8 @@ __global__ void __launch_bounds__(kMsBuBlock, kWide ? 4 : 5) k_ms_bu(MsArgs a, i
                 }
                 ng = 0;  // the single-group loop below has nothing left
             }
-            int4 c = f0;
+            int4 c = make_int4(pp, pp, pp, pp);
+            if (active && ng > 0) c = ld_stream(cp, pol);
             for (int32_t g = 0;; g++) {
                 active = active && g < ng;
                 if (!__any_sync(kFull, active)) break;
@@ -486,7 +474,6 @@ __global__ void __launch_bounds__(kMsBuBlock, kWide ? 4 : 5) k_ms_bu(MsArgs a, i
                 cfull += (d != kFull && (d | dm) == kFull);
             }
         }
-        first_groups(w1, d1, vis1, wd1, so1, f0, f1);
         w = w1;
         d = d1;
         vis_c = vis1;

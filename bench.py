@@ -299,6 +299,7 @@ def run_ours(args, rank: int, world: int, dist) -> None:
     roof = None if args.no_roofline else roofline(dg, roots, d_ms, policy)
     roof_plain = None if args.no_roofline else roofline_plain(dg, roots[:8])
     heldout = selector_heldout(dg, g, roots, loaded)
+    spmv = None if args.no_roofline else spmv_roofline(g)
     e2e = None if args.no_e2e else e2e_batched(args, g, roots, ab, torch, bopts)
     cpu = cpu_baseline(g, roots, args.cpu_roots) if rank == 0 and args.cpu_roots > 0 else None
     if rank != 0:
@@ -322,7 +323,7 @@ def run_ours(args, rank: int, world: int, dist) -> None:
                                                  for f, m in meta.items()}},
             "sell_build_ms": build_ms, "graph_gen_s": gen_s,
             "gpu_launches": launches, "clocks": clk.summary(), "roofline": roof,
-            "roofline_plain": roof_plain,
+            "roofline_plain": roof_plain, "spmv": spmv,
             "e2e": e2e, "cpu_baseline": cpu}
     emit(line, args)
 
@@ -388,6 +389,35 @@ def selector_heldout(dg, g, roots, loaded, plain_roots: int = 4) -> dict:
                      "mlp": selector.regret(us, selector.mlp_choices(w, feat)),
                      "beamer": selector.regret(us, selector.beamer_choices(state, group, best))}
     return out
+
+
+def spmv_roofline(g, reps: int = 20) -> dict:
+    """The fp64 SELL-C-sigma SpMV (alb_sellmat_spmv, the reference's
+    kernel_SELLCS_DFC) on this run's graph with seeded values: algorithmic
+    bytes per launch = 12 per stored entry (int32 column + fp64 value) +
+    24 per row (x read once, y written, row order and length read) over the
+    kernel's CUDA-event time, against the measured HBM copy bandwidth."""
+    import torch
+
+    import albba_gb300 as ab
+    peak, kind = peaks()
+    rng = np.random.default_rng(5)
+    val = rng.uniform(-1.0, 1.0, g.nnz)
+    with ab.SellMatrix(g.rowptr, g.col, val, 1024) as m:
+        dx = torch.from_numpy(rng.standard_normal(g.n)).cuda()
+        dy = torch.empty(g.n, dtype=torch.float64, device="cuda")
+        for _ in range(3):
+            m.spmv_device(dx, dy)
+        us = sorted(m.spmv_device(dx, dy) for _ in range(reps))
+        stored = m.stored
+    t = statistics.median(us)
+    byts = 12 * g.nnz + 24 * g.n
+    gbs = byts / t / 1e3
+    return {"kernel": "k_spmv (fp64 SELL-32-sigma SpMV, y = A x)", "bound": "hbm",
+            "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+            "peak_kind": f"{kind} HBM copy bandwidth (burst)", "bytes_per_launch": byts,
+            "us_per_launch": t, "stored_slots": stored, "entries": g.nnz,
+            "gflops": 2 * g.nnz / t / 1e3}
 
 
 def roofline_plain(dg, roots) -> dict:
@@ -459,18 +489,19 @@ def e2e_batched(args, g, roots, ab, torch, opts, steps: int = 5) -> dict:
                                           ab.C.byref(ab.Stats())))
         return 0
 
-    step()
+    # two untimed steps first: the host<->device link and the memory pool
+    # reach their steady state (the first copies after the host has been
+    # busy run several times slower)
+    for _ in range(2):
+        step()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
         step()
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
-    deg = g.degrees()
-    edges = 0
-    for i in range(len(roots)):
-        edges += int(deg[levels[:, i] >= 0].sum()) // 2
-    # phase split of one more step (wall clock, a synchronize after each call)
+    # phase split of one more step, right away (wall clock, a synchronize
+    # after each call)
     ph = {}
     t = time.perf_counter()
     dg = ab.Graph(hg, flags=flags)
@@ -489,6 +520,10 @@ def e2e_batched(args, g, roots, ab, torch, opts, steps: int = 5) -> dict:
     dg.close()
     torch.cuda.synchronize()
     ph["graph_destroy_ms"] = (time.perf_counter() - t) * 1e3
+    deg = g.degrees()
+    edges = 0
+    for i in range(len(roots)):
+        edges += int(deg[levels[:, i] >= 0].sum()) // 2
     fl = copy_floor(torch)
     floor_ms = h2d / fl["h2d_gbs"] / 1e6 + d2h / fl["d2h_gbs"] / 1e6
     return {"value": steps * edges / dt / 1e9, "unit": "GTEPS", "h2d_bytes_per_step": h2d,

@@ -320,6 +320,20 @@ alb_status alb_selector_train(const float *x, const float *y, const float *mask,
                               int32_t steps, float lr, uint64_t seed, int32_t init,
                               float *params, float *loss);
 
+/* ------------------------------------------- sparse frontier expansion */
+
+/* The reference's push-merge kernel csc_spmspv_merge
+ * (bfs/src/bfs_par_kernels.c:350-416, with the task merge of
+ * bfs/src/bfs_SELLCSv2.c:530-575): the next frontier of the frontier x[nx]
+ * (original ids) as the ascending, duplicate-free list of the out-neighbours
+ * of x whose bit in visited (host bitmap over original ids, n bits, bit
+ * v & 31 of word v >> 5) is clear. *ny receives the list's length; y (host,
+ * may be NULL) must hold up to n entries. Computed by marking a bitmap on
+ * the device and compacting it in id order, which gives the reference's
+ * sorted merge result without merging. */
+alb_status alb_spmspv_merge(alb_graph *g, const int32_t *x, int64_t nx, const uint32_t *visited,
+                            int32_t *y, int64_t *ny);
+
 /* ----------------------------------------------- fp64 SELL-C-sigma SpMV */
 
 /* y = A x in fp64 over a SELL-C-sigma matrix on the device. Replaces the

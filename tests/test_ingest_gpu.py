@@ -175,3 +175,40 @@ def test_undirected_merge_at_scale_matches_host_restatement():
         lv, pa, _ = dg.bfs(3)
     olv, opa, _ = oracle.bfs(want_rp, want_col, 3)
     assert np.array_equal(lv, olv) and np.array_equal(pa, opa)
+
+
+def _visited_bits(n, visited):
+    bits = np.zeros((n + 31) // 32, np.uint32)
+    ids = np.flatnonzero(visited)
+    np.bitwise_or.at(bits, ids >> 5, (np.uint32(1) << (ids & 31).astype(np.uint32)))
+    return bits
+
+
+@pytest.mark.parametrize("directed_graph", [False, True])
+def test_spmspv_merge_is_the_sorted_unvisited_union(directed_graph):
+    """alb_spmspv_merge against the reference's push-merge semantics
+    (csc_spmspv_merge, bfs/src/bfs_par_kernels.c:350-416, and the task merge
+    of bfs/src/bfs_SELLCSv2.c:530-575): the ascending, duplicate-free list of
+    the frontier's out-neighbours that are not visited."""
+    rng = np.random.default_rng(3)
+    if directed_graph:
+        n = 1 << 14
+        u, v = directed(n, 120_000, seed=8, hubs=((5, 6000),))
+        rp, col = sorted_csr(n, u, v)
+        dg = ab.Graph(ab.Csr(rp, col), flags=ab.CSR_OUT)
+    else:
+        g = ab.gen_rmat(16, 16, seed=2024)
+        n, rp, col = g.n, g.rowptr, g.col
+        dg = ab.Graph(g)
+    with dg:
+        for nx, pv in ((1, 0.0), (37, 0.3), (2000, 0.5), (n // 2, 0.1), (0, 0.0)):
+            x = rng.choice(n, nx, replace=False).astype(np.int32)
+            visited = rng.random(n) < pv
+            got = dg.spmspv_merge(x, _visited_bits(n, visited))
+            nbrs = np.concatenate([col[rp[u]:rp[u + 1]] for u in x]) if nx else np.zeros(0, np.int32)
+            want = np.unique(nbrs)
+            want = want[~visited[want]]
+            assert np.array_equal(got, want), nx
+        with pytest.raises(ab.AlbError) as ei:
+            dg.spmspv_merge(np.array([n], np.int32), _visited_bits(n, np.zeros(n, bool)))
+        assert ei.value.code == ab.ERR_INVALID
