@@ -506,53 +506,16 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r, const uint32_t *Fs = 
             nxt = grab();
             vnxt = run_vis(nxt);
         }
-        // Slices of C >= 32 rows: a word lies inside one slice, so lane l
-        // loads the geometry (width, offset) of word l of the run, and a
-        // word's first column group can be requested as soon as the word
-        // before it starts -- its columns then arrive while that word waits
-        // on its frontier gathers. (C < 32: each row's slice is loaded per
-        // word, no lookahead.)
-        const bool run_geom = log2C >= 5;
-        int32_t wd_l = 0;
-        int64_t so_l = 0;
-        if (run_geom && base_w + lane < a.nwords) {
-            const int64_t sl = (base_w + lane) >> (log2C - 5);
-            wd_l = __ldg(a.width + sl);
-            so_l = __ldg(a.slice_off + sl);
-        }
-        // first column group of word q of the run (rows' own position when
-        // the row is visited or empty)
-        auto first_group = [&](int q, uint32_t vq) {
-            const int32_t pq = (int32_t)((base_w + q) * 32 + lane);
-            int4 g0 = make_int4(pq, pq, pq, pq);
-            const int32_t wdq = __shfl_sync(kFull, wd_l, q);
-            const int64_t soq = __shfl_sync(kFull, so_l, q);
-            if (!((vq >> lane) & 1u) && wdq > 0)
-                g0 = ld_stream(a.col4 + (soq >> 2) + (pq & (C - 1)), pol);
-            return g0;
-        };
-        int4 c_next = make_int4(0, 0, 0, 0);
-        if (run_geom && todo) {
-            const int q0 = __ffs(todo) - 1;
-            c_next = first_group(q0, __shfl_sync(kFull, vrun, q0));
-        }
       while (todo) {
         const int q = __ffs(todo) - 1;
         todo &= todo - 1;
         const int64_t w = base_w + q;
         const uint32_t vis = __shfl_sync(kFull, vrun, q);
         const int32_t p = (int32_t)(w * 32 + lane);
-        int32_t wd;
-        int64_t so;
-        if (run_geom) {
-            wd = __shfl_sync(kFull, wd_l, q);
-            so = __shfl_sync(kFull, so_l, q);
-        } else {
-            // rows past n are preset visited; clamp their slice index
-            const int64_t s = (int64_t)(p < a.n ? p : a.n - 1) >> log2C;
-            wd = __ldg(a.width + s);
-            so = __ldg(a.slice_off + s);
-        }
+        // rows past n are preset visited; clamp their slice index
+        const int64_t s = (int64_t)(p < a.n ? p : a.n - 1) >> log2C;
+        const int32_t wd = __ldg(a.width + s);
+        const int64_t so = __ldg(a.slice_off + s);
         bool active = !((vis >> lane) & 1u);
         const int32_t ng = active ? (wd + 3) >> 2 : 0;
         n_rows += ng > 0;
@@ -562,15 +525,7 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r, const uint32_t *Fs = 
         // group j+1 is requested before group j's frontier tests, so each lane
         // keeps one column load in flight while it waits on the bitmap
         int4 c = make_int4(p, p, p, p);
-        if (run_geom) {
-            c = c_next;  // requested when the previous word started
-            if (todo) {
-                const int q2 = __ffs(todo) - 1;
-                c_next = first_group(q2, __shfl_sync(kFull, vrun, q2));
-            }
-        } else if (active && ng > 0) {
-            c = ld_stream(cp, pol);
-        }
+        if (active && ng > 0) c = ld_stream(cp, pol);
         // an unvisited row whose first entry is padding is a long row (rows
         // without sources start visited): the long-row pass has run already
         const bool long_cand = active && c.x == p;
