@@ -205,9 +205,29 @@ def cmd_selector(a):
         del g
 
 
+def cmd_spmv(a):
+    """fp64 SELL-32-sigma SpMV (alb_sellmat_*) on RMAT graphs with seeded
+    values: kernel microseconds and GB/s of 12 bytes per entry + 24 per row."""
+    import numpy as np
+    import torch
+    for sc in a.scales:
+        g = ab.gen_rmat(sc, 16, seed=24)
+        rng = np.random.default_rng(5)
+        with ab.SellMatrix(g.rowptr, g.col, rng.uniform(-1.0, 1.0, g.nnz), 1024) as m:
+            dx = torch.from_numpy(rng.standard_normal(g.n)).cuda()
+            dy = torch.empty(g.n, dtype=torch.float64, device="cuda")
+            for _ in range(3):
+                m.spmv_device(dx, dy)
+            us = statistics.median(m.spmv_device(dx, dy) for _ in range(20))
+            emit({"config": "spmv", "scale": sc, "n": g.n, "entries": g.nnz,
+                  "stored_slots": m.stored, "us": us,
+                  "gbs": (12 * g.nnz + 24 * g.n) / us / 1e3, "gflops": 2 * g.nnz / us / 1e3})
+        del g
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["scales", "loops", "batched", "worklist", "selector"])
+    ap.add_argument("what", choices=["scales", "loops", "batched", "worklist", "selector", "spmv"])
     ap.add_argument("--scales", type=int, nargs="*", default=[20, 22, 24])
     ap.add_argument("--roots", type=int, default=64)
     ap.add_argument("--graphs", type=int, default=256)
@@ -220,7 +240,7 @@ def main(argv=None):
         from albba_gb300 import tune
         tune.CACHE = Path(a.cache)
     {"scales": cmd_scales, "loops": cmd_loops, "batched": cmd_batched,
-     "worklist": cmd_worklist, "selector": cmd_selector}[a.what](a)
+     "worklist": cmd_worklist, "selector": cmd_selector, "spmv": cmd_spmv}[a.what](a)
 
 
 if __name__ == "__main__":

@@ -34,6 +34,7 @@ namespace alb {
 
 constexpr int kMaxBlock = 1024;
 constexpr uint64_t kBarrierTimeoutNs = 4ull * 1000 * 1000 * 1000;
+constexpr unsigned kBarFailed = 0x80000000u;  // grid barrier gave up (bar_gen bit 31)
 
 // Loads of bitmaps/queues: .nc is safe in standalone kernels (the data was
 // written by an earlier launch); the persistent kernel needs ordinary loads.
@@ -183,6 +184,35 @@ __device__ __forceinline__ void push_edges4(const BfsArgs &a, uint32_t *N, const
     }
 }
 
+// Lazy push (persistent loop, small frontiers): a target counts as visited
+// when its level was set before this level (level_pos <= L), and the push
+// that claims an unvisited target is the one whose atomicCAS moves its level
+// from -1 to L + 1. Parents still meet by atomicMin over every source one
+// level up. Neither the visited nor the frontier bitmaps are touched: a level
+// that needs them rebuilds them from the levels first (materialize_phase),
+// so a run of such levels costs one grid barrier each.
+__device__ __forceinline__ void push_edges4_lazy(const BfsArgs &a, int L, const int32_t (&v)[4],
+                                                 const uint32_t (&ou)[4], unsigned &bypassed,
+                                                 unsigned &claimed) {
+    int32_t lp[4];
+    bool live[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) lp[k] = v[k] >= 0 ? __ldcg(a.level_pos + v[k]) : 0;
+    uint32_t cur_parent[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        live[k] = v[k] >= 0 && (lp[k] == -1 || lp[k] == L + 1);
+        bypassed += v[k] >= 0 && !live[k];
+        cur_parent[k] = live[k] ? __ldcg(a.parent_pos + v[k]) : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        if (!live[k]) continue;
+        if (ou[k] < cur_parent[k]) atomicMin(a.parent_pos + v[k], ou[k]);
+        if (lp[k] == -1 && atomicCAS(a.level_pos + v[k], -1, L + 1) == -1) claimed |= 1u << k;
+    }
+}
+
 // Appends the warp's claimed targets (bit k of claimed: v[k], one lane's
 // four edges of push_edges4) to the next queue, one atomicAdd per warp. Call
 // from all lanes of a warp.
@@ -208,6 +238,31 @@ __device__ __forceinline__ void flush_claims(const BfsArgs &a, int32_t *NQ,
     claimed = 0;
 }
 
+// Counters of a lazy level, kept by the claimers (no finish pass counts them).
+struct LazyCounts {
+    unsigned n = 0;
+    unsigned long long mo = 0, mi = 0;
+    __device__ __forceinline__ void add(const BfsArgs &a, const int32_t (&v)[4], unsigned claimed) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (!((claimed >> k) & 1u)) continue;
+            n++;
+            mo += (unsigned long long)__ldg(a.odeg + v[k]);
+            mi += (unsigned long long)__ldg(a.ideg + v[k]);
+        }
+    }
+    __device__ __forceinline__ void flush(const BfsArgs &a, int L) {
+        const unsigned cn = warp_sum(n);
+        const unsigned long long cmo = warp_sum(mo), cmi = warp_sum(mi);
+        if ((threadIdx.x & 31) == 0 && cn) {
+            const int k = (L + 1) % 3;
+            atomicAdd(&a.ctl->acc_n[k], (unsigned long long)cn);
+            atomicAdd(&a.ctl->acc_mo[k], cmo);
+            atomicAdd(&a.ctl->acc_mi[k], cmi);
+        }
+    }
+};
+
 // Append mode for a top-down level: the frontier's push edges are no more
 // than the bitmap's words, so the next queue is built by the claims rather
 // than by scanning the whole next-frontier bitmap.
@@ -228,7 +283,8 @@ constexpr int kBigShift = 38;
 constexpr unsigned long long kBigMask = (1ull << kBigShift) - 1;
 
 template <bool kPersist>
-__device__ void td_phase(const BfsArgs &a, int L, Range r, bool append) {
+__device__ void td_phase(const BfsArgs &a, int L, Range r, bool append, bool lazy = false) {
+    LazyCounts lc;
     const int32_t *Q = (L & 1) ? a.q1 : a.q0;
     int32_t *NQ = (L & 1) ? a.q0 : a.q1;
     unsigned long long *nq_slot = &a.ctl->qn[(L + 1) % 3];
@@ -292,11 +348,17 @@ __device__ void td_phase(const BfsArgs &a, int L, Range r, bool append) {
                     ou4[k] = (uint32_t)s_ou[wib][j];
                 }
             }
-            push_edges4(a, N, v, ou4, kPersist, bypassed, append, claimed);
-            if (append) flush_claims(a, NQ, nq_slot, v, claimed);
+            if (lazy) {
+                push_edges4_lazy(a, L, v, ou4, bypassed, claimed);
+                lc.add(a, v, claimed);
+            } else {
+                push_edges4(a, N, v, ou4, kPersist, bypassed, append, claimed);
+            }
+            if (append || lazy) flush_claims(a, NQ, nq_slot, v, claimed);
         }
         __syncwarp();
     }
+    if (lazy) lc.flush(a, L);
     add_stat(a, L, kStEdgesBypassed, bypassed);
 }
 
@@ -305,7 +367,7 @@ __device__ void td_phase(const BfsArgs &a, int L, Range r, bool append) {
 // first chunk by binary search over the chunk bases (monotone in the list
 // index) and walks forward from there.
 template <bool kPersist>
-__device__ void td_big_phase(const BfsArgs &a, int L, Range r, bool append) {
+__device__ void td_big_phase(const BfsArgs &a, int L, Range r, bool append, bool lazy = false) {
     const unsigned long long ctr = ld_state<kPersist>(&a.ctl->nbig[L % 3]);
     if (ctr == 0) return;
     const int64_t nbig = (int64_t)(ctr >> kBigShift);
@@ -321,6 +383,7 @@ __device__ void td_big_phase(const BfsArgs &a, int L, Range r, bool append) {
     int32_t *NQ = (L & 1) ? a.q0 : a.q1;
     unsigned long long *nq_slot = &a.ctl->qn[(L + 1) % 3];
     unsigned claimed = 0;
+    LazyCounts lc;
     if (k0 >= k1) {
         add_stat(a, L, kStEdgesBypassed, bypassed);  // keeps every lane at the shuffle
         return;
@@ -358,9 +421,15 @@ __device__ void td_big_phase(const BfsArgs &a, int L, Range r, bool append) {
             if (v[q] >= 0) ALB_CHECK_ID(v[q], a.n, -1, &a.ctl->err);
             ou4[q] = ou;
         }
-        push_edges4(a, N, v, ou4, kPersist, bypassed, append, claimed);
-        if (append) flush_claims(a, NQ, nq_slot, v, claimed);
+        if (lazy) {
+            push_edges4_lazy(a, L, v, ou4, bypassed, claimed);
+            lc.add(a, v, claimed);
+        } else {
+            push_edges4(a, N, v, ou4, kPersist, bypassed, append, claimed);
+        }
+        if (append || lazy) flush_claims(a, NQ, nq_slot, v, claimed);
     }
+    if (lazy) lc.flush(a, L);
     add_stat(a, L, kStEdgesBypassed, bypassed);
 }
 
@@ -438,6 +507,38 @@ __device__ void td_finish_phase(const BfsArgs &a, int L, Range r, bool append) {
         }
         if (full) atomicAdd(&a.ctl->acc_full[k], (unsigned long long)full);
     }
+}
+
+// Rebuilds the bitmaps after a run of lazy levels (see push_edges4_lazy):
+// visited = the initial mask | every position with a level, frontier (of
+// level L) = the positions at level L, next frontier cleared; the words with
+// an unvisited row are counted into acc_active[L % 3]. One thread per
+// position, one ballot per word.
+__device__ void materialize_phase(const BfsArgs &a, int L, Range r) {
+    uint32_t *F = (L & 1) ? a.bm1 : a.bm0;
+    uint32_t *N = (L & 1) ? a.bm0 : a.bm1;
+    const int lane = threadIdx.x & 31;
+    const int64_t tid = (int64_t)r.bid * blockDim.x + threadIdx.x;
+    const int64_t nth = (int64_t)r.nblk * blockDim.x;
+    const int64_t npos = a.nwords * 32;
+    unsigned active = 0;
+    // the loop bound is warp-uniform so that every lane reaches the ballots
+    for (int64_t p0 = tid & ~31ll; p0 < npos; p0 += nth) {
+        const int64_t p = p0 + lane;
+        const int32_t lp = p < a.n ? __ldcg(a.level_pos + p) : -1;
+        const uint32_t vb = __ballot_sync(kFull, lp >= 0);
+        const uint32_t fb = __ballot_sync(kFull, lp == L);
+        if (lane == 0) {
+            const int64_t w = p0 >> 5;
+            const uint32_t vis = __ldg(a.vinit + w) | vb;
+            a.vis[w] = vis;
+            F[w] = fb;
+            N[w] = 0;
+            active += vis != kFull;
+        }
+    }
+    active = warp_sum(active);
+    if (lane == 0 && active) atomicAdd(&a.ctl->acc_active[L % 3], (unsigned long long)active);
 }
 
 // Frontier word read by the bottom-up pull: from the staged shared-memory
@@ -840,6 +941,7 @@ __global__ void k_decide(BfsArgs a, int forced, cudaGraphConditionalHandle sw) {
         a.ctl->acc_full[k] = 0;
         a.ctl->acc_bytes[k] = 0;
         for (int i = 0; i < kStatN; i++) a.ctl->acc_stat[k][i] = 0;
+        a.ctl->acc_active[k] = 0;
         a.ctl->nbig[k] = 0;
         a.ctl->work[k] = 0;
         a.ctl->qn[k] = 0;
@@ -967,33 +1069,49 @@ __device__ bool grid_sync(const BfsArgs &a, unsigned nblocks, int L) {
     BfsCtl *ctl = a.ctl;
     if (a.withhold_level >= 0 && L == a.withhold_level && (int)blockIdx.x == a.withhold_block)
         return false;
+    __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
+        // the generation word counts barriers in its low 31 bits; bit 31 is
+        // set by a block whose wait ran out, so that every waiter sees a
+        // change and leaves (and the status needs no second load)
         volatile unsigned *gen = &ctl->bar_gen;
         const unsigned g0 = *gen;
-        __threadfence();
-        const unsigned arrived = atomicAdd(&ctl->bar_count, 1u);
-        if (arrived == nblocks - 1) {
-            atomicExch(&ctl->bar_count, 0u);
+        bool ok = !(g0 & kBarFailed);
+        if (ok) {
             __threadfence();
-            atomicAdd(&ctl->bar_gen, 1u);
-        } else {
-            const uint64_t t0 = globaltimer_ns();
-            while (*gen == g0) {
-                if (globaltimer_ns() - t0 > a.barrier_ns) {
-                    atomicExch(&ctl->err, ALB_ERR_TIMEOUT);
-                    break;
+            const unsigned arrived = atomicAdd(&ctl->bar_count, 1u);
+            if (arrived == nblocks - 1) {
+                atomicExch(&ctl->bar_count, 0u);
+                __threadfence();
+                atomicAdd(&ctl->bar_gen, 1u);
+            } else {
+                const uint64_t t0 = globaltimer_ns();
+                unsigned gv;
+                while ((gv = *gen) == g0) {
+                    if (globaltimer_ns() - t0 > a.barrier_ns) {
+                        atomicExch(&ctl->err, ALB_ERR_TIMEOUT);
+                        atomicOr(&ctl->bar_gen, kBarFailed);
+                        gv = kBarFailed;
+                        break;
+                    }
+                    __nanosleep(64);
                 }
-                __nanosleep(64);
+                ok = !(gv & kBarFailed);
             }
+            __threadfence();
         }
-        __threadfence();
+        s_ok = ok ? 1 : 0;
     }
     __syncthreads();
-    return *(volatile int32_t *)&ctl->err == 0;
+    return s_ok != 0;
 }
 
-__global__ void __launch_bounds__(256, 3) k_persistent(BfsArgs a) {
+// One block of kPersistBlock threads per SM: a grid barrier then waits for
+// as few arrivals as the SM count.
+constexpr unsigned kPersistBlock = 768;
+
+__global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(BfsArgs a) {
     __shared__ BfsCtl c;
     __shared__ int s_dir;
     const unsigned nb = gridDim.x;
@@ -1014,6 +1132,7 @@ __global__ void __launch_bounds__(256, 3) k_persistent(BfsArgs a) {
                     a.ctl->acc_full[k] = 0;
                     a.ctl->acc_bytes[k] = 0;
                     for (int i = 0; i < kStatN; i++) a.ctl->acc_stat[k][i] = 0;
+                    a.ctl->acc_active[k] = 0;
                     a.ctl->nbig[k] = 0;
                     a.ctl->work[k] = 0;
                     a.ctl->qn[k] = 0;
@@ -1024,21 +1143,37 @@ __global__ void __launch_bounds__(256, 3) k_persistent(BfsArgs a) {
         const int dir = s_dir;
         const int L = c.level;
         bool ok = true;
-        if (dir == ALB_DIR_TOPDOWN) {
+        // small top-down levels run lazily: one barrier per level, the
+        // bitmaps rebuilt when a level that reads them comes (materialize)
+        const bool lazy = dir == ALB_DIR_TOPDOWN && td_append(a, c.mf);
+        if (c.lazy && !lazy) {
+            materialize_phase(a, L, r);
+            ok = grid_sync(a, nb, L);
+            if (threadIdx.x == 0) {
+                c.active_words = (int64_t) * (volatile unsigned long long *)&a.ctl->acc_active[L % 3];
+                c.lazy = 0;
+                c.q_valid = 1;  // the lazy levels' claims built the queue
+                c.n_dirty = 0;
+            }
+            __syncthreads();
+        }
+        if (!ok) {
+            // a barrier gave up: every block leaves below
+        } else if (dir == ALB_DIR_TOPDOWN) {
             if (!c.q_valid || c.n_dirty) {
                 prep_phase<true>(a, L, !c.q_valid, c.n_dirty != 0, r);
                 ok = grid_sync(a, nb, L);
             }
             const bool app = td_append(a, c.mf);
             if (ok) {
-                td_phase<true>(a, L, r, app);
+                td_phase<true>(a, L, r, app, lazy);
                 ok = grid_sync(a, nb, L);
             }
             if (ok && *(volatile unsigned long long *)&a.ctl->nbig[L % 3]) {
-                td_big_phase<true>(a, L, r, app);
+                td_big_phase<true>(a, L, r, app, lazy);
                 ok = grid_sync(a, nb, L);
             }
-            if (ok) {
+            if (ok && !lazy) {
                 td_finish_phase<true>(a, L, r, app);
                 ok = grid_sync(a, nb, L);
             }
@@ -1079,6 +1214,7 @@ __global__ void __launch_bounds__(256, 3) k_persistent(BfsArgs a) {
             }
             roll(c, dir, g->acc_n[k], g->acc_mo[k], g->acc_mi[k], g->acc_full[k]);
             c.dir = dir;
+            if (lazy) c.lazy = 1;
         }
         __syncthreads();
         if (c.done) break;
@@ -1478,13 +1614,13 @@ alb_status run_host_loop(alb_graph *g, const BfsArgs &a, const alb_bfs_opts &o,
 
 alb_status run_persistent(alb_graph *g, const BfsArgs &a) {
     int per_sm = 0;
-    ALB_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persistent, 256, 0));
+    ALB_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persistent, kPersistBlock, 0));
     if (per_sm < 1) return fail(ALB_ERR_CUDA, "persistent kernel does not fit on an SM");
     const unsigned grid = (unsigned)(per_sm * g->num_sms);
     BfsArgs args = a;
     void *kargs[] = {&args};
-    ALB_CK(cudaLaunchCooperativeKernel((void *)k_persistent, dim3(grid), dim3(256), kargs, 0,
-                                       g->stream));
+    ALB_CK(cudaLaunchCooperativeKernel((void *)k_persistent, dim3(grid), dim3(kPersistBlock), kargs,
+                                       0, g->stream));
     return ALB_OK;
 }
 

@@ -214,6 +214,10 @@ struct BfsCtl {
     int32_t trace_cap, trace_len;
     int32_t level_cap;       // safety bound on the number of levels
     int32_t branch;          // loop-graph switch branch taken this level
+    int32_t lazy;            // persistent loop: visited / frontier bitmaps stale,
+                             // level_pos authoritative (materialize before use)
+    unsigned long long acc_active[3];  // words with an unvisited row, counted
+                                       // when the bitmaps are rebuilt
     int64_t launches;        // kernel launches of the level loop
     float feat_mean_deg, feat_skew;  // static selector features
 };

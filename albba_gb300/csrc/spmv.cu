@@ -18,7 +18,19 @@
 // kept exactly as given (diagonal and repeated entries included); padding is
 // never read: a lane stops at its row's length, so the fma chain is the
 // reference's, bit for bit.
+//
+// Rows longer than kSpLong entries (the hubs of a power-law graph) keep an
+// empty SELL row: one lane walking a hub of 10^5 entries one group at a time
+// would hold its warp -- and the whole launch -- for tens of milliseconds.
+// They are copied in CSR order to a separate list and each is summed by one
+// warp: the lanes fetch the next 32 values and x gathers together (the batch
+// after it already requested) and stage them in shared memory, and every
+// lane then runs the row's fma chain over them in order. The chain itself
+// stays sequential -- its order is what makes y bit-identical -- so a hub
+// costs one dependent fma per entry, but no memory latency per entry.
+#include <algorithm>
 #include <cstring>
+#include <vector>
 
 #include "graph.h"
 #include "ingest.h"
@@ -36,12 +48,19 @@ struct alb_sellmat {
     int32_t *col = nullptr;        // 4-interleaved column ids
     double *val = nullptr;         // values, same layout
     double *dx = nullptr, *dy = nullptr;  // staging for host vectors
+    int64_t nlong = 0;             // rows longer than kSpLong, summed by a warp each
+    int32_t *lrow = nullptr;       // their row ids, longest first
+    int64_t *lptr = nullptr;       // nlong + 1 offsets into lcol / lval
+    int32_t *lcol = nullptr;       // their entries in CSR order
+    double *lval = nullptr;
+    unsigned long long *ctr = nullptr;  // k_spmv_long's row counter
 };
 
 namespace alb {
 namespace {
 
 constexpr int kSpC = 32;
+constexpr int32_t kSpLong = 512;  // longer rows are summed by a warp each
 
 unsigned blocks_for(int64_t work, int block) {
     int64_t g = (work + block - 1) / block;
@@ -65,7 +84,7 @@ __global__ void k_sp_sizes(int64_t n, int64_t nslices, const int32_t *deg, int64
     int32_t w = 0;
     for (int r = 0; r < kSpC; r++) {
         const int64_t p = s * kSpC + r;
-        if (p < n) w = max(w, deg[p]);
+        if (p < n && deg[p] <= kSpLong) w = max(w, deg[p]);
     }
     ssize[s] = (int64_t)kSpC * ((w + 3) & ~3);
 }
@@ -81,7 +100,7 @@ __global__ void k_sp_fill(int64_t n, int64_t npad, const int32_t *perm, const in
         const int64_t s = p / kSpC;
         const int64_t base = slice_off[s] + 4 * (p % kSpC);
         const int32_t ng = (int32_t)((slice_off[s + 1] - slice_off[s]) / (4 * kSpC));
-        const int32_t d = p < n ? deg[p] : 0;
+        const int32_t d = p < n && deg[p] <= kSpLong ? deg[p] : 0;
         const int64_t b = p < n ? rp[perm[p]] : 0;
         for (int32_t g = 0; g < ng; g++) {
             int32_t c4[4];
@@ -113,7 +132,9 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, int64_t nslices, const 
     const uint64_t pol = l2_evict_first();
     for (int64_t s = w0; s < nslices; s += nw) {
         const int64_t p = s * kSpC + lane;
-        const int32_t d = p < n ? __ldg(deg + p) : 0;
+        const int32_t dr = p < n ? __ldg(deg + p) : 0;
+        const bool mine = p < n && dr <= kSpLong;  // long rows: k_spmv_long
+        const int32_t d = mine ? dr : 0;
         const int32_t ng = (d + 3) >> 2;
         const int64_t base = __ldg(slice_off + s) + 4 * lane;
         const int4 *cp = reinterpret_cast<const int4 *>(col + base);
@@ -147,7 +168,78 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, int64_t nslices, const 
             va = van;
             vb = vbn;
         }
-        if (p < n) y[__ldg(perm + p)] = acc;
+        if (mine) y[__ldg(perm + p)] = acc;
+    }
+}
+
+// One warp per long row (the list is longest first, handed out from a
+// counter): batches of 32 entries, lane l fetching entry l of a batch -- its
+// value and x[column] -- one batch ahead; the batch goes to shared memory and
+// every lane then applies its 32 fmas in order, so all lanes carry the same
+// accumulator and lane 0 writes it.
+constexpr int kSpLongBlock = 128;
+
+__global__ void __launch_bounds__(kSpLongBlock) k_spmv_long(
+    int64_t nlong, const int32_t *lrow, const int64_t *lptr, const int32_t *lcol,
+    const double *lval, const double *x, double *y, unsigned long long *ctr) {
+    __shared__ double s_v[kSpLongBlock / 32][32], s_x[kSpLongBlock / 32][32];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    for (;;) {
+        unsigned long long i = 0;
+        if (lane == 0) i = atomicAdd(ctr, 1ull);
+        i = __shfl_sync(kFull, i, 0);
+        if ((int64_t)i >= nlong) break;
+        const int64_t b = lptr[i], e = lptr[i + 1];
+        double acc = 0.0;
+        // batch k holds entries b + 32k .. b + 32k + 31
+        double v = 0.0, xv = 0.0;
+        if (b + lane < e) {
+            v = __ldcs(lval + b + lane);
+            xv = __ldg(x + __ldcs(lcol + b + lane));
+        }
+        for (int64_t t = b; t < e; t += 32) {
+            double vn = 0.0, xn = 0.0;
+            if (t + 32 + lane < e) {
+                vn = __ldcs(lval + t + 32 + lane);
+                xn = __ldg(x + __ldcs(lcol + t + 32 + lane));
+            }
+            __syncwarp();
+            s_v[wib][lane] = v;
+            s_x[wib][lane] = xv;
+            __syncwarp();
+            const int cnt = (int)min((int64_t)32, e - t);
+            for (int k = 0; k < cnt; k++) acc = fma(s_v[wib][k], s_x[wib][k], acc);
+            v = vn;
+            xv = xn;
+        }
+        if (lane == 0) y[lrow[i]] = acc;
+    }
+}
+
+__global__ void k_sp_long_flags(int64_t n, const int32_t *len, int32_t *flag) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r < n) flag[r] = len[r] > kSpLong ? 1 : 0;
+}
+
+__global__ void k_sp_long_scatter(int64_t n, const int32_t *flag, const int64_t *idx,
+                                  int32_t *lrow) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r < n && flag[r]) lrow[idx[r]] = (int32_t)r;
+}
+
+// One warp per long row: its entries copied in CSR order.
+__global__ void k_sp_long_fill(int64_t nlong, const int32_t *lrow, const int64_t *lptr,
+                               const int64_t *rp, const int32_t *col, const double *val,
+                               int32_t *lcol, double *lval) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = w0; i < nlong; i += nw) {
+        const int64_t src = rp[lrow[i]], dst = lptr[i], len = lptr[i + 1] - dst;
+        for (int64_t k = lane; k < len; k += 32) {
+            lcol[dst + k] = col[src + k];
+            lval[dst + k] = val[src + k];
+        }
     }
 }
 
@@ -201,6 +293,59 @@ alb_status build(alb_sellmat *m, const int64_t *rowptr, const int32_t *col, cons
         k_sp_fill<<<blocks_for(npad, 256), 256, 0, st>>>(n, npad, m->perm, m->deg, m->slice_off,
                                                           d_rp, d_col, d_val, m->col, m->val);
         ALB_CK(cudaGetLastError());
+        // long rows: list (longest first, ordered on the host: a few
+        // thousand ids), offsets, entries
+        int64_t *idx = nullptr;
+        ALB_TRY(dmalloc((void **)&idx, sizeof(int64_t) * (size_t)(n + 1), "SpMV long index"));
+        struct Free {
+            int64_t *p;
+            ~Free() { dfree(p); }
+        } free_idx{idx};
+        ALB_TRY(dmalloc((void **)&m->ctr, sizeof(unsigned long long), "SpMV counter"));
+        int32_t *flags = nullptr;
+        ALB_TRY(dmalloc((void **)&flags, sizeof(int32_t) * (size_t)n, "SpMV long flags"));
+        struct Free32 {
+            int32_t *p;
+            ~Free32() { dfree(p); }
+        } free_flags{flags};
+        k_sp_long_flags<<<blocks_for(n, 256), 256, 0, st>>>(n, len, flags);
+        ALB_CK(cudaGetLastError());
+        ALB_TRY(exclusive_scan(flags, idx, n, st));
+        ALB_CK(cudaMemcpyAsync(&m->nlong, idx + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        ALB_CK(cudaStreamSynchronize(st));
+        if (m->nlong > 0) {
+            const int64_t nl = m->nlong;
+            ALB_TRY(dmalloc((void **)&m->lrow, sizeof(int32_t) * (size_t)nl, "SpMV long rows"));
+            ALB_TRY(dmalloc((void **)&m->lptr, sizeof(int64_t) * (size_t)(nl + 1), "SpMV long offsets"));
+            k_sp_long_scatter<<<blocks_for(n, 256), 256, 0, st>>>(n, flags, idx, m->lrow);
+            ALB_CK(cudaGetLastError());
+            std::vector<int32_t> hrow((size_t)nl);
+            ALB_CK(cudaMemcpyAsync(hrow.data(), m->lrow, sizeof(int32_t) * (size_t)nl,
+                                   cudaMemcpyDeviceToHost, st));
+            ALB_CK(cudaStreamSynchronize(st));
+            std::vector<int64_t> hlen((size_t)nl);
+            for (int64_t i = 0; i < nl; i++) hlen[(size_t)i] = rowptr[hrow[(size_t)i] + 1] - rowptr[hrow[(size_t)i]];
+            std::vector<int64_t> order((size_t)nl);
+            for (int64_t i = 0; i < nl; i++) order[(size_t)i] = i;
+            std::stable_sort(order.begin(), order.end(),
+                             [&](int64_t x, int64_t y) { return hlen[(size_t)x] > hlen[(size_t)y]; });
+            std::vector<int32_t> srow((size_t)nl);
+            std::vector<int64_t> sptr((size_t)nl + 1, 0);
+            for (int64_t i = 0; i < nl; i++) {
+                srow[(size_t)i] = hrow[(size_t)order[(size_t)i]];
+                sptr[(size_t)i + 1] = sptr[(size_t)i] + hlen[(size_t)order[(size_t)i]];
+            }
+            ALB_CK(cudaMemcpyAsync(m->lrow, srow.data(), sizeof(int32_t) * (size_t)nl,
+                                   cudaMemcpyHostToDevice, st));
+            ALB_CK(cudaMemcpyAsync(m->lptr, sptr.data(), sizeof(int64_t) * (size_t)(nl + 1),
+                                   cudaMemcpyHostToDevice, st));
+            const int64_t nent = sptr[(size_t)nl];
+            ALB_TRY(dmalloc((void **)&m->lcol, sizeof(int32_t) * (size_t)nent, "SpMV long columns"));
+            ALB_TRY(dmalloc((void **)&m->lval, sizeof(double) * (size_t)nent, "SpMV long values"));
+            k_sp_long_fill<<<blocks_for(nl * 32, 256), 256, 0, st>>>(nl, m->lrow, m->lptr, d_rp,
+                                                                    d_col, d_val, m->lcol, m->lval);
+            ALB_CK(cudaGetLastError());
+        }
         ALB_CK(cudaStreamSynchronize(st));
         return ALB_OK;
     }();
@@ -221,6 +366,11 @@ void destroy(alb_sellmat *m) {
     dfree(m->val);
     dfree(m->dx);
     dfree(m->dy);
+    dfree(m->lrow);
+    dfree(m->lptr);
+    dfree(m->lcol);
+    dfree(m->lval);
+    dfree(m->ctr);
     if (m->ev0) cudaEventDestroy(m->ev0);
     if (m->ev1) cudaEventDestroy(m->ev1);
     if (m->stream) cudaStreamDestroy(m->stream);
@@ -239,6 +389,12 @@ alb_status launch(alb_sellmat *m, const double *d_x, double *d_y, float *us) {
     if (us) ALB_CK(cudaEventRecord(m->ev0, m->stream));
     k_spmv<<<grid, 256, 0, m->stream>>>(m->n, m->nslices, m->perm, m->deg, m->slice_off, m->col,
                                          m->val, d_x, d_y);
+    if (m->nlong > 0) {
+        ALB_CK(cudaMemsetAsync(m->ctr, 0, sizeof(unsigned long long), m->stream));
+        const int64_t warps = std::min<int64_t>(m->nlong, (int64_t)sms * 16);
+        k_spmv_long<<<(unsigned)((warps + 3) / 4), kSpLongBlock, 0, m->stream>>>(
+            m->nlong, m->lrow, m->lptr, m->lcol, m->lval, d_x, d_y, m->ctr);
+    }
     ALB_CK(cudaGetLastError());
     if (us) {
         ALB_CK(cudaEventRecord(m->ev1, m->stream));

@@ -259,3 +259,26 @@ def test_frontier_staged_and_global_slice_passes(scale, staged):
                 for loop in ("graph", "host"):
                     lv, pa, _ = dg.bfs(int(r), ab.bfs_opts(policy, loop))
                     assert np.array_equal(lv, olv) and np.array_equal(pa, opa), (policy, loop)
+
+
+@pytest.mark.parametrize("policy", ["beamer", "topdown", "bottomup", "ref004"])
+def test_persistent_lazy_levels_on_a_grid(policy):
+    """The persistent loop runs small top-down levels lazily (one grid
+    barrier per level, targets claimed on their level word, the bitmaps left
+    stale) and rebuilds the visited and frontier bitmaps when a level that
+    reads them follows (a large top-down level or a bottom-up one). A grid
+    with shortcuts has long runs of small levels and frontiers that grow past
+    the lazy limit: every switch is taken, and the levels, parents and
+    per-level counters match the oracle and the other loop drivers."""
+    g = ab.gen_grid(300, 300, 0.1, 2e-4, seed=21)
+    with ab.Graph(g) as dg:
+        dg.sell_build(32, 1)
+        for r in g.pick_roots(4, seed=5):
+            olv, opa, nl = oracle.bfs(g.rowptr, g.col, int(r))
+            lv, pa, st = dg.bfs(int(r), ab.bfs_opts(policy, "persistent", trace=True))
+            assert np.array_equal(lv, olv) and np.array_equal(pa, opa), (policy, int(r))
+            assert st.num_levels == nl
+            pers = [(t.dir, t.nf, t.mf, t.nu, t.mu, t.bytes) for t in dg.level_trace()]
+            lv2, pa2, _ = dg.bfs(int(r), ab.bfs_opts(policy, "host", trace=True))
+            host = [(t.dir, t.nf, t.mf, t.nu, t.mu, t.bytes) for t in dg.level_trace()]
+            assert pers == host

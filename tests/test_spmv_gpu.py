@@ -62,3 +62,24 @@ def test_gpu_spmv_rejects_bad_input():
     with pytest.raises(ab.AlbError) as ei:
         ab.SellMatrix(rp, np.array([0, 1], np.int32), np.ones(2), sigma=0)
     assert ei.value.code == ab.ERR_UNSUPPORTED
+
+
+def test_gpu_spmv_long_rows_keep_csr_order():
+    """Rows at and past the warp-per-row threshold (511, 512, 513, 1000 and a
+    40000-entry hub with repeated columns, so that order matters) next to
+    short rows: every y bit equals the oracle's in-order chain."""
+    rng = np.random.default_rng(7)
+    n = 4096
+    lens = rng.integers(0, 24, n)
+    lens[[3, 100, 101, 2000, 4095]] = [511, 512, 513, 1000, 40000]
+    rp = np.zeros(n + 1, np.int64)
+    rp[1:] = np.cumsum(lens)
+    col = rng.integers(0, n, int(rp[-1])).astype(np.int32)
+    col[rp[4095]:rp[4095] + 64] = 17  # one column repeated inside the hub
+    val = rng.uniform(-1.0, 1.0, int(rp[-1])) * np.exp2(rng.integers(-30, 30, int(rp[-1])))
+    x = rng.standard_normal(n) * np.exp2(rng.integers(-10, 10, n))
+    want = oracle.spmv(rp, col, val, x)
+    for sigma in (1, 4096):
+        with ab.SellMatrix(rp, col, val, sigma) as m:
+            got = m.spmv(x)
+        assert np.array_equal(got.view(np.uint64), want.view(np.uint64)), sigma
