@@ -267,37 +267,51 @@ alb_status create_impl(int64_t n, const int64_t *rowptr, const int32_t *col, uin
 // --------------------------------------------------------- device kernels
 
 // Row lengths without self-loops, for both sides; optionally (sl_off != 0)
-// each row's self-loop run: its offset in the row and its length.
+// each row's self-loop run: its offset in the row and its length. Grid-stride
+// rows; the longest length is combined in the block and posted with one
+// atomic only when it beats the current maximum.
 __global__ void k_row_lengths(int64_t n, const int64_t *rp, const int32_t *col, int32_t *len,
                               int32_t *max_len, int32_t *sl_off = nullptr,
                               int32_t *sl_num = nullptr) {
-    int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    __shared__ int32_t s_max[32];
     int32_t l = 0;
-    if (v < n) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n;
+         v += (int64_t)gridDim.x * blockDim.x) {
         // rows are sorted: the self-loops are one run, found by two binary
-        // searches (a hub row costs log(deg), not deg)
+        // searches (a hub row costs log(deg), not deg); a row whose first
+        // entry is above v or last below it has none
         const int64_t b = rp[v], e = rp[v + 1];
         int64_t lo = b, hi = e;
-        while (lo < hi) {  // first entry >= v
-            const int64_t mid = (lo + hi) >> 1;
-            if (col[mid] < (int32_t)v) lo = mid + 1;
-            else hi = mid;
+        if (b < e && (col[b] > (int32_t)v || col[e - 1] < (int32_t)v)) {
+            lo = hi = col[b] > (int32_t)v ? b : e;
+        } else {
+            while (lo < hi) {  // first entry >= v
+                const int64_t mid = (lo + hi) >> 1;
+                if (col[mid] < (int32_t)v) lo = mid + 1;
+                else hi = mid;
+            }
         }
-        int64_t lo2 = lo, hi2 = e;
+        int64_t lo2 = lo, hi2 = lo < e && col[lo] == (int32_t)v ? e : lo;
         while (lo2 < hi2) {  // first entry > v
             const int64_t mid = (lo2 + hi2) >> 1;
             if (col[mid] <= (int32_t)v) lo2 = mid + 1;
             else hi2 = mid;
         }
-        l = (int32_t)((e - b) - (lo2 - lo));
-        len[v] = l;
+        const int32_t lv = (int32_t)((e - b) - (lo2 - lo));
+        len[v] = lv;
+        l = max(l, lv);
         if (sl_off) {
             sl_off[v] = (int32_t)(lo - b);
             sl_num[v] = (int32_t)(lo2 - lo);
         }
     }
     l = __reduce_max_sync(kFull, l);
-    if ((threadIdx.x & 31) == 0 && l > 0) atomicMax(max_len, l);
+    if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = l;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < (int)(blockDim.x >> 5); k++) l = max(l, s_max[k]);
+        if (l > 0 && l > __ldcg(max_len)) atomicMax(max_len, l);
+    }
 }
 
 // Stable descending sort of row lengths inside one sigma window per CTA:
@@ -452,33 +466,43 @@ __device__ __forceinline__ int64_t slice_of(const int64_t *slice_off, int64_t q,
     return lo;
 }
 
+// The slice holding the first int4 slot of every 32-slot chunk (one thread
+// per chunk, all lanes searching at once), so that k_fill_flat's warps start
+// from a narrow slice range instead of searching the whole offset table on
+// one lane.
+__global__ void k_chunk_slice(int64_t nslices, int64_t nchunks, const int64_t *slice_off,
+                              int32_t *cslice) {
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c < nchunks) cslice[c] = (int32_t)slice_of(slice_off, c * 32, 0, nslices - 1);
+}
+
 // Flat fill of the 4-interleaved SELL: one thread per int4 slot (four entries
 // of one row), 32 consecutive slots per warp, so every thread does the same
 // small amount of work (four column loads, four inv gathers, one coalesced
 // 16-byte store) however long its row is, and a warp's store is 512
 // contiguous bytes. A slot's slice is found by binary search inside the
-// range the warp's first and last slots span. kPush (symmetric graphs, where
+// range from its chunk's first slice to the next chunk's. kPush (symmetric graphs, where
 // a position's push row is its SELL row): the same entries are written to the
 // push CSR too, so the CSR is read and gathered once for both. Long rows stay
 // padding here (their lists are filled by k_fill_chunks).
 template <bool kPush>
 __global__ void __launch_bounds__(256) k_fill_flat(
     int64_t n, int64_t nslices, int64_t nslots, int32_t C, int32_t log2C, int32_t long_row,
-    const int64_t *slice_off, const int32_t *ideg, const int64_t *rstart, const int2 *sl,
-    const int32_t *col, const int32_t *inv, int32_t *scol, const int64_t *prow, int32_t *pcol) {
+    const int64_t *slice_off, const int32_t *cslice, const int32_t *ideg, const int64_t *rstart,
+    const int2 *sl, const int32_t *col, const int32_t *inv, int32_t *scol, const int64_t *prow,
+    int32_t *pcol) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t nchunks = (nslots + 31) >> 5;
     const uint64_t pstream = l2_evict_first();
     int4 *scol4 = reinterpret_cast<int4 *>(scol);
-    for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w * 32 < nslots;
+    for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w < nchunks;
          w += nw) {
-        const int64_t q0 = w * 32, q = q0 + lane;
-        const int64_t qlast = min(q0 + 31, nslots - 1);
-        int64_t s_lo = 0, s_hi = 0;
-        if (lane == 0) s_lo = slice_of(slice_off, q0, 0, nslices - 1);
-        if (lane == 31) s_hi = slice_of(slice_off, qlast, 0, nslices - 1);
-        s_lo = __shfl_sync(kFull, s_lo, 0);
-        s_hi = __shfl_sync(kFull, s_hi, 31);
+        const int64_t q = w * 32 + lane;
+        // slots of this chunk lie in [slice of its first slot, slice of the
+        // next chunk's first slot]
+        const int64_t s_lo = __ldg(cslice + w);
+        const int64_t s_hi = w + 1 < nchunks ? __ldg(cslice + w + 1) : nslices - 1;
         if (q >= nslots) continue;
         const int64_t sc = slice_of(slice_off, q, s_lo, s_hi);
         const int64_t k4 = q - (slice_off[sc] >> 2);
@@ -645,21 +669,34 @@ __global__ void k_fill_chunks(int64_t nchunks, const int32_t *crow, const int32_
 // be discovered by a pull, so they start visited (their level stays -1).
 __global__ void k_vinit(int64_t n, int64_t nwords, const int32_t *ideg, uint32_t *vinit,
                         unsigned long long *counters) {
-    // thread per position (coalesced degree loads), one ballot per word
-    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31;
-    const int64_t w = p >> 5;
-    if (w >= nwords) return;  // whole warps leave together (nwords * 32 positions)
-    const int32_t d = p < n ? ideg[p] : 0;
-    const bool pre = p >= n || d == 0;
-    const uint32_t m = __ballot_sync(kFull, pre);
-    const unsigned z = __popc(__ballot_sync(kFull, p < n && d == 0));
-    const unsigned long long sum = warp_sum((unsigned long long)d);
+    // warp per word, grid-stride (coalesced degree loads, one ballot per
+    // word); the three counts are combined in the block, then one atomic each
+    __shared__ unsigned long long s_c[3][32];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    unsigned long long act = 0, zero = 0, sum = 0;
+    for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w < nwords; w += nw) {
+        const int64_t p = w * 32 + lane;
+        const int32_t d = p < n ? ideg[p] : 0;
+        const uint32_t m = __ballot_sync(kFull, p >= n || d == 0);
+        if (lane == 0) vinit[w] = m;
+        act += lane == 0 && m != kFull;                 // active words
+        zero += p < n && d == 0;                        // rows without sources
+        sum += (unsigned long long)d;                   // pull-side entries
+    }
+    act = warp_sum(act);
+    zero = warp_sum(zero);
+    sum = warp_sum(sum);
     if (lane == 0) {
-        vinit[w] = m;
-        if (m != kFull) atomicAdd(&counters[0], 1ull);  // active words
-        if (z) atomicAdd(&counters[1], (unsigned long long)z);  // rows without sources
-        if (sum) atomicAdd(&counters[2], sum);  // pull-side entries
+        s_c[0][wib] = act;
+        s_c[1][wib] = zero;
+        s_c[2][wib] = sum;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        unsigned long long t = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) t += s_c[threadIdx.x][k];
+        if (t) atomicAdd(&counters[threadIdx.x], t);
     }
 }
 
@@ -776,12 +813,15 @@ alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma, int32_t long_
         ALB_CK(cudaMemsetAsync(dmax, 0, sizeof(int32_t) * 2, st));
         ALB_CK(cudaMemsetAsync(dcnt, 0, sizeof(unsigned long long) * 3, st));
         const int T = 256;
-        k_row_lengths<<<grid_for(n, T), T, 0, st>>>(n, g->rp_in, g->col_in, ilen, dmax, sl_off,
+        // grid-stride kernels that end in a block-combined atomic
+        const unsigned red_grid =
+            (unsigned)std::min<int64_t>(grid_for(n, T), (int64_t)g->num_sms * 16);
+        k_row_lengths<<<red_grid, T, 0, st>>>(n, g->rp_in, g->col_in, ilen, dmax, sl_off,
                                                      sl_num);
         if (g->symmetric)
             ALB_CK(cudaMemcpyAsync(olen, ilen, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, st));
         else
-            k_row_lengths<<<grid_for(n, T), T, 0, st>>>(n, g->rp_out, g->col_out, olen, dmax + 1);
+            k_row_lengths<<<red_grid, T, 0, st>>>(n, g->rp_out, g->col_out, olen, dmax + 1);
         ALB_CK(cudaGetLastError());
         ph.mark("alloc_lengths", st);
         ALB_TRY(window_order(n, sigma, ilen, s.perm, st));
@@ -814,18 +854,28 @@ alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma, int32_t long_
         const bool fused = g->symmetric;
         const int64_t nslots = s.ncol / 4;
         if (nslots > 0) {
+            const int64_t nchunks = (nslots + 31) / 32;
+            int32_t *cslice = nullptr;
+            struct Tmp {
+                int32_t *&a;
+                ~Tmp() { dfree(a); }
+            } tmp{cslice};
+            ALB_TRY(dmalloc((void **)&cslice, sizeof(int32_t) * nchunks, "chunk slices"));
+            k_chunk_slice<<<grid_for(nchunks, T), T, 0, st>>>(s.nslices, nchunks, s.slice_off,
+                                                               cslice);
             const unsigned flat_grid =
                 (unsigned)std::min<int64_t>((nslots + T - 1) / T, (int64_t)g->num_sms * 64);
             if (fused)
                 k_fill_flat<true><<<flat_grid, T, 0, st>>>(n, s.nslices, nslots, C, s.log2C,
-                                                           long_row, s.slice_off, s.ideg, rstart,
-                                                           slrun, g->col_in, s.inv, s.col, s.prow,
-                                                           s.pcol);
+                                                           long_row, s.slice_off, cslice, s.ideg,
+                                                           rstart, slrun, g->col_in, s.inv, s.col,
+                                                           s.prow, s.pcol);
             else
                 k_fill_flat<false><<<flat_grid, T, 0, st>>>(n, s.nslices, nslots, C, s.log2C,
-                                                            long_row, s.slice_off, s.ideg, rstart,
-                                                            slrun, g->col_in, s.inv, s.col,
-                                                            s.prow, s.pcol);
+                                                            long_row, s.slice_off, cslice, s.ideg,
+                                                            rstart, slrun, g->col_in, s.inv,
+                                                            s.col, s.prow, s.pcol);
+            ALB_CK(cudaGetLastError());
         }
         if (!fused)
             k_fill_push<<<fill_grid, T, 0, st>>>(n, s.perm, s.inv, s.prow, g->rp_out, g->col_out,
@@ -899,7 +949,8 @@ alb_status sell_build_impl(alb_graph *g, int32_t C, int32_t sigma, int32_t long_
                                       fused ? s.pcol : nullptr));
         }
         ph.mark("long_rows", st);
-        k_vinit<<<grid_for(s.nwords * 32, T), T, 0, st>>>(n, s.nwords, s.ideg, s.vinit, dcnt);
+        k_vinit<<<(unsigned)std::min<int64_t>(grid_for(s.nwords * 32, T), (int64_t)g->num_sms * 16),
+                  T, 0, st>>>(n, s.nwords, s.ideg, s.vinit, dcnt);
         ALB_CK(cudaGetLastError());
         unsigned long long hc[3];
         ALB_CK(cudaMemcpyAsync(hc, dcnt, sizeof(hc), cudaMemcpyDeviceToHost, st));

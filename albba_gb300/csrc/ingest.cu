@@ -56,41 +56,72 @@ unsigned grid_for(int64_t work, int block, int64_t cap = 152 * 32) {
     return (unsigned)g;
 }
 
-__global__ void k_check_offsets(int64_t n, const int64_t *rp, int64_t nnz, int *flags) {
+// Counters of the CSR check, one device word each.
+struct CheckWords {
+    int flags;
+    int pad;
+    unsigned long long descents;      // entries e > 0 with col[e - 1] > col[e]
+    unsigned long long start_desc;    // ... of them at the first entry of a row
+};
+
+// Offsets: rp[0] == 0, rp[n] == nnz, never decreasing. With check_order,
+// also counts the descents at row starts: every non-empty row r with
+// rp[r] > 0 compares its first entry with the entry before it (the bounds
+// are tested locally, so the loads stay inside col even when some other
+// offset is bad).
+__global__ void k_check_offsets(int64_t n, const int64_t *rp, const int32_t *col, int64_t nnz,
+                                int check_order, CheckWords *cw) {
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t nth = (int64_t)gridDim.x * blockDim.x;
     int bad = 0;
+    unsigned cnt = 0;
     if (tid == 0 && (rp[0] != 0 || rp[n] != nnz)) bad = 1;
-    for (int64_t r = tid; r < n; r += nth)
-        if (rp[r + 1] < rp[r]) bad = 1;
-    if (__any_sync(kFull, bad) && (threadIdx.x & 31) == 0) atomicOr(flags, kBadOffsets);
-}
-
-// Entry e starts a row when some row r has rp[r] == e (empty rows share it).
-__device__ bool starts_row(int64_t n, const int64_t *rp, int64_t e) {
-    int64_t lo = 0, hi = n;  // last r with rp[r] <= e
-    while (lo < hi) {
-        const int64_t mid = (lo + hi + 1) >> 1;
-        if (rp[mid] <= e) lo = mid;
-        else hi = mid - 1;
+    for (int64_t r = tid; r < n; r += nth) {
+        const int64_t a = rp[r], b = rp[r + 1];
+        if (b < a) bad = 1;
+        if (check_order && a > 0 && a < b && b <= nnz && col[a - 1] > col[a]) cnt++;
     }
-    return rp[lo] == e;
+    if (__any_sync(kFull, bad) && (threadIdx.x & 31) == 0) atomicOr(&cw->flags, kBadOffsets);
+    cnt = __reduce_add_sync(kFull, cnt);
+    if (cnt && (threadIdx.x & 31) == 0) atomicAdd(&cw->start_desc, (unsigned long long)cnt);
 }
 
-__global__ void k_check_columns(int64_t n, const int64_t *rp, const int32_t *col, int64_t nnz,
-                                int check_order, int *flags) {
+// Columns: inside [0, n); with check_order, the number of descents (entry
+// smaller than the one before it). Rows are sorted exactly when every
+// descent sits at a row start, i.e. when this count equals k_check_offsets'.
+// Four entries per thread and step (one 16-byte load; the entry before them
+// is the previous thread's, read through L1).
+__global__ void k_check_columns(int64_t n, const int32_t *col, int64_t nnz, int check_order,
+                                CheckWords *cw) {
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t nth = (int64_t)gridDim.x * blockDim.x;
-    int bits = check_order ? 0 : kUnsorted;  // (kUnsorted set: no order test)
-    for (int64_t e = tid; e < nnz; e += nth) {
-        const int32_t c = col[e];
-        if (c < 0 || c >= n) bits |= kBadColumn;
-        if (e > 0 && col[e - 1] > c && !(bits & kUnsorted) && !starts_row(n, rp, e))
-            bits |= kUnsorted;
+    const int64_t ng = nnz >> 2;
+    const int4 *c4 = reinterpret_cast<const int4 *>(col);
+    int bits = 0;
+    unsigned cnt = 0;
+    for (int64_t i = tid; i <= ng; i += nth) {
+        int32_t c[4];
+        int m = 4;
+        if (i < ng) {
+            const int4 v = c4[i];
+            c[0] = v.x, c[1] = v.y, c[2] = v.z, c[3] = v.w;
+        } else {  // the last nnz % 4 entries
+            m = (int)(nnz & 3);
+            for (int k = 0; k < m; k++) c[k] = col[4 * i + k];
+        }
+        int32_t prev = i > 0 && m > 0 ? __ldg(col + 4 * i - 1) : INT32_MIN;
+        for (int k = 0; k < m; k++) {
+            if (c[k] < 0 || c[k] >= n) bits |= kBadColumn;
+            if (prev > c[k]) cnt++;
+            prev = c[k];
+        }
     }
-    if (!check_order) bits &= ~kUnsorted;
     bits = __reduce_or_sync(kFull, bits);
-    if (bits && (threadIdx.x & 31) == 0) atomicOr(flags, bits);
+    if (bits && (threadIdx.x & 31) == 0) atomicOr(&cw->flags, bits);
+    if (check_order) {
+        cnt = __reduce_add_sync(kFull, cnt);
+        if (cnt && (threadIdx.x & 31) == 0) atomicAdd(&cw->descents, (unsigned long long)cnt);
+    }
 }
 
 // ------------------------------------------------------------- row sort
@@ -355,34 +386,30 @@ int key_bits(int64_t n) {
 
 alb_status csr_check(int64_t n, const int64_t *d_rp, const int32_t *d_col, int64_t nnz,
                      cudaStream_t st, bool *sorted) {
-    int *d_flags = nullptr;
-    ALB_TRY(dmalloc((void **)&d_flags, sizeof(int), "ingest flags"));
-    int h = 0;
-    cudaError_t e = cudaMemsetAsync(d_flags, 0, sizeof(int), st);
+    CheckWords *d_cw = nullptr;
+    ALB_TRY(dmalloc((void **)&d_cw, sizeof(CheckWords), "ingest flags"));
+    CheckWords h{};
+    const int order = sorted ? 1 : 0;
+    cudaError_t e = cudaMemsetAsync(d_cw, 0, sizeof(CheckWords), st);
     if (e == cudaSuccess) {
-        k_check_offsets<<<grid_for(n, 256), 256, 0, st>>>(n, d_rp, nnz, d_flags);
+        k_check_offsets<<<grid_for(n, 256), 256, 0, st>>>(n, d_rp, d_col, nnz, order, d_cw);
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d_flags, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && nnz > 0) {
+        k_check_columns<<<grid_for((nnz + 3) / 4, 256), 256, 0, st>>>(n, d_col, nnz, order, d_cw);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d_cw, sizeof(h), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    // the column pass binary-searches the offsets: only run it on valid ones
-    if (e == cudaSuccess && !(h & kBadOffsets) && nnz > 0) {
-        k_check_columns<<<grid_for(nnz, 256), 256, 0, st>>>(n, d_rp, d_col, nnz,
-                                                             sorted ? 1 : 0, d_flags);
-        e = cudaGetLastError();
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(&h, d_flags, sizeof(int), cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    }
-    dfree(d_flags);
+    dfree(d_cw);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return fail(ALB_ERR_CUDA, "CSR check: %s", cudaGetErrorString(e));
     }
-    if (h & kBadOffsets)
+    if (h.flags & kBadOffsets)
         return fail(ALB_ERR_INVALID, "row offsets must start at 0, never decrease and end at nnz");
-    if (h & kBadColumn) return fail(ALB_ERR_INVALID, "column index outside [0, n)");
-    if (sorted) *sorted = !(h & kUnsorted);
+    if (h.flags & kBadColumn) return fail(ALB_ERR_INVALID, "column index outside [0, n)");
+    if (sorted) *sorted = h.descents == h.start_desc;
     return ALB_OK;
 }
 

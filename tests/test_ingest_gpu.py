@@ -212,3 +212,37 @@ def test_spmspv_merge_is_the_sorted_unvisited_union(directed_graph):
         with pytest.raises(ab.AlbError) as ei:
             dg.spmspv_merge(np.array([n], np.int32), _visited_bits(n, np.zeros(n, bool)))
         assert ei.value.code == ab.ERR_INVALID
+
+
+@pytest.mark.parametrize("at", [1, 2, 3, 4, 5, 127, 128, 1023, -1])
+def test_one_descent_inside_one_row_is_found(at):
+    """Rows sorted everywhere but one descent inside a row, at entry `at` of
+    the column array (every offset of a 16-byte group, the last entry, or the
+    next entry when `at` starts a row); around it, empty rows and rows
+    starting below their predecessor's last entry (descents at row starts,
+    which are allowed). The graph must come back with every row sorted."""
+    rng = np.random.default_rng(at + 10)
+    n = 600
+    lens = rng.integers(0, 8, n)
+    lens[::7] = 0
+    lens[-1] = 5
+    rp = np.zeros(n + 1, np.int64)
+    rp[1:] = np.cumsum(lens)
+    nnz = int(rp[-1])
+    assert nnz > 1024
+    col = np.empty(nnz, np.int32)
+    for r in range(n):
+        col[rp[r]:rp[r + 1]] = np.sort(rng.choice(n, rp[r + 1] - rp[r], replace=False))
+    e = at % nnz
+    while e in set(rp.tolist()):  # a row start: take the next entry
+        e += 1
+    col[e - 1], col[e] = col[e], col[e - 1]
+    starts = set(rp[:-1][rp[:-1] < rp[1:]].tolist())
+    inner = [int(d) for d in np.nonzero(col[1:] < col[:-1])[0] + 1 if int(d) not in starts]
+    assert inner == [e]
+    with ab.Graph(ab.Csr(rp, col), flags=ab.CSR_IN) as dg:
+        back = dg.export_csr(0)  # the given side
+    want = col.copy()
+    for q in range(n):
+        want[rp[q]:rp[q + 1]] = np.sort(want[rp[q]:rp[q + 1]])
+    assert np.array_equal(back.rowptr, rp) and np.array_equal(back.col, want)
