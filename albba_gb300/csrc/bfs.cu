@@ -34,7 +34,7 @@ namespace alb {
 
 constexpr int kMaxBlock = 1024;
 constexpr uint64_t kBarrierTimeoutNs = 4ull * 1000 * 1000 * 1000;
-constexpr unsigned kBarFailed = 0x80000000u;  // grid barrier gave up (bar_gen bit 31)
+constexpr unsigned long long kBarFailed = 1ull << 62;  // grid barrier gave up (bit 62 of bar)
 
 // Loads of bitmaps/queues: .nc is safe in standalone kernels (the data was
 // written by an earlier launch); the persistent kernel needs ordinary loads.
@@ -190,26 +190,27 @@ __device__ __forceinline__ void push_edges4(const BfsArgs &a, uint32_t *N, const
 // from -1 to L + 1. Parents still meet by atomicMin over every source one
 // level up. Neither the visited nor the frontier bitmaps are touched: a level
 // that needs them rebuilds them from the levels first (materialize_phase),
-// so a run of such levels costs one grid barrier each.
+// so a run of such levels costs one grid barrier each. The CAS is issued at
+// once, together with the parent read (one round trip): a CAS that finds a
+// level set changes nothing, and its old value tells a target claimed this
+// level (L + 1: still a parent candidate) from one visited before.
 __device__ __forceinline__ void push_edges4_lazy(const BfsArgs &a, int L, const int32_t (&v)[4],
                                                  const uint32_t (&ou)[4], unsigned &bypassed,
                                                  unsigned &claimed) {
-    int32_t lp[4];
-    bool live[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) lp[k] = v[k] >= 0 ? __ldcg(a.level_pos + v[k]) : 0;
+    int32_t old[4];
     uint32_t cur_parent[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        live[k] = v[k] >= 0 && (lp[k] == -1 || lp[k] == L + 1);
-        bypassed += v[k] >= 0 && !live[k];
-        cur_parent[k] = live[k] ? __ldcg(a.parent_pos + v[k]) : 0u;
+        old[k] = v[k] >= 0 ? atomicCAS(a.level_pos + v[k], -1, L + 1) : 0;
+        cur_parent[k] = v[k] >= 0 ? __ldcg(a.parent_pos + v[k]) : 0u;
     }
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        if (!live[k]) continue;
+        const bool live = v[k] >= 0 && (old[k] == -1 || old[k] == L + 1);
+        bypassed += v[k] >= 0 && !live;
+        if (!live) continue;
         if (ou[k] < cur_parent[k]) atomicMin(a.parent_pos + v[k], ou[k]);
-        if (lp[k] == -1 && atomicCAS(a.level_pos + v[k], -1, L + 1) == -1) claimed |= 1u << k;
+        if (old[k] == -1) claimed |= 1u << k;
     }
 }
 
@@ -242,13 +243,23 @@ __device__ __forceinline__ void flush_claims(const BfsArgs &a, int32_t *NQ,
 struct LazyCounts {
     unsigned n = 0;
     unsigned long long mo = 0, mi = 0;
-    __device__ __forceinline__ void add(const BfsArgs &a, const int32_t (&v)[4], unsigned claimed) {
+    int32_t od[4], id[4];
+    // the claimed targets' degrees, requested before the queue append so
+    // that both round trips overlap; add() uses them after it
+    __device__ __forceinline__ void load(const BfsArgs &a, const int32_t (&v)[4], unsigned claimed) {
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-            if (!((claimed >> k) & 1u)) continue;
-            n++;
-            mo += (unsigned long long)__ldg(a.odeg + v[k]);
-            mi += (unsigned long long)__ldg(a.ideg + v[k]);
+            const bool c = (claimed >> k) & 1u;
+            od[k] = c ? __ldg(a.odeg + v[k]) : 0;
+            id[k] = c ? __ldg(a.ideg + v[k]) : 0;
+        }
+    }
+    __device__ __forceinline__ void add(unsigned claimed) {
+        n += __popc(claimed);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            mo += (unsigned long long)od[k];
+            mi += (unsigned long long)id[k];
         }
     }
     __device__ __forceinline__ void flush(const BfsArgs &a, int L) {
@@ -268,11 +279,17 @@ struct LazyCounts {
 // than by scanning the whole next-frontier bitmap.
 __device__ __forceinline__ bool td_append(const BfsArgs &a, int64_t mf) { return mf <= a.nwords; }
 
-// Rows per warp for the short-row pass: as many frontier rows as keep every
-// warp busy (1 when the frontier is small, up to 32 when it is large).
-__device__ __forceinline__ int rows_per_warp(int64_t qlen, int64_t nwarps) {
-    int G = 32;
-    while (G > 1 && (int64_t)(G >> 1) * nwarps >= qlen) G >>= 1;
+// Rows per warp for the short-row pass (a power of two up to 32): at least
+// as many as spread the frontier over the warps available, and, when the
+// frontier is small, as many as fill about one 128-edge step at the mean push
+// degree -- the latency per warp is the same either way, and fewer warps
+// means fewer appends and counter atomics on the level's shared words (each
+// warp's land on the same few addresses, where L2 serialises them).
+__device__ __forceinline__ int rows_per_warp(int64_t qlen, int64_t mf, int64_t nwarps) {
+    const int64_t mean = qlen > 0 ? max((int64_t)1, mf / qlen) : 1;
+    const int64_t per_warp = max((int64_t)128, mf / max(nwarps, (int64_t)1));
+    int G = 1;
+    while (G < 32 && ((int64_t)G * nwarps < qlen || (int64_t)(2 * G) * mean <= per_warp)) G <<= 1;
     return G;
 }
 
@@ -283,7 +300,8 @@ constexpr int kBigShift = 38;
 constexpr unsigned long long kBigMask = (1ull << kBigShift) - 1;
 
 template <bool kPersist>
-__device__ void td_phase(const BfsArgs &a, int L, Range r, bool append, bool lazy = false) {
+__device__ void td_phase(const BfsArgs &a, int L, Range r, int64_t mf, bool append,
+                         bool lazy = false) {
     LazyCounts lc;
     const int32_t *Q = (L & 1) ? a.q1 : a.q0;
     int32_t *NQ = (L & 1) ? a.q0 : a.q1;
@@ -299,7 +317,7 @@ __device__ void td_phase(const BfsArgs &a, int L, Range r, bool append, bool laz
     const int64_t wpb = blockDim.x >> 5;
     const int64_t gw = (int64_t)r.bid * wpb + wib;
     const int64_t nwarps = (int64_t)r.nblk * wpb;
-    const int G = rows_per_warp(qlen, nwarps);
+    const int G = rows_per_warp(qlen, mf, nwarps);
     const int64_t stride = nwarps * G;
     unsigned bypassed = 0;
     for (int64_t cb = gw * G; cb < qlen; cb += stride) {
@@ -350,11 +368,14 @@ __device__ void td_phase(const BfsArgs &a, int L, Range r, bool append, bool laz
             }
             if (lazy) {
                 push_edges4_lazy(a, L, v, ou4, bypassed, claimed);
-                lc.add(a, v, claimed);
+                const unsigned cl = claimed;
+                lc.load(a, v, cl);
+                flush_claims(a, NQ, nq_slot, v, claimed);
+                lc.add(cl);
             } else {
                 push_edges4(a, N, v, ou4, kPersist, bypassed, append, claimed);
+                if (append) flush_claims(a, NQ, nq_slot, v, claimed);
             }
-            if (append || lazy) flush_claims(a, NQ, nq_slot, v, claimed);
         }
         __syncwarp();
     }
@@ -423,11 +444,14 @@ __device__ void td_big_phase(const BfsArgs &a, int L, Range r, bool append, bool
         }
         if (lazy) {
             push_edges4_lazy(a, L, v, ou4, bypassed, claimed);
-            lc.add(a, v, claimed);
+            const unsigned cl = claimed;
+            lc.load(a, v, cl);
+            flush_claims(a, NQ, nq_slot, v, claimed);
+            lc.add(cl);
         } else {
             push_edges4(a, N, v, ou4, kPersist, bypassed, append, claimed);
+            if (append) flush_claims(a, NQ, nq_slot, v, claimed);
         }
-        if (append || lazy) flush_claims(a, NQ, nq_slot, v, claimed);
     }
     if (lazy) lc.flush(a, L);
     add_stat(a, L, kStEdgesBypassed, bypassed);
@@ -512,24 +536,37 @@ __device__ void td_finish_phase(const BfsArgs &a, int L, Range r, bool append) {
 // Rebuilds the bitmaps after a run of lazy levels (see push_edges4_lazy):
 // visited = the initial mask | every position with a level, frontier (of
 // level L) = the positions at level L, next frontier cleared; the words with
-// an unvisited row are counted into acc_active[L % 3]. One thread per
-// position, one ballot per word.
+// an unvisited row are counted into acc_active[L % 3]. A warp takes 32 words
+// (1024 positions) at a time: lane l loads position 32k + l of word k for
+// every k before any ballot, so 32 loads per lane are in flight together,
+// and lane k then writes word k (coalesced stores).
 __device__ void materialize_phase(const BfsArgs &a, int L, Range r) {
     uint32_t *F = (L & 1) ? a.bm1 : a.bm0;
     uint32_t *N = (L & 1) ? a.bm0 : a.bm1;
     const int lane = threadIdx.x & 31;
-    const int64_t tid = (int64_t)r.bid * blockDim.x + threadIdx.x;
-    const int64_t nth = (int64_t)r.nblk * blockDim.x;
-    const int64_t npos = a.nwords * 32;
+    const int64_t wpb = blockDim.x >> 5;
+    const int64_t gw = (int64_t)r.bid * wpb + (threadIdx.x >> 5);
+    const int64_t nwarps = (int64_t)r.nblk * wpb;
     unsigned active = 0;
-    // the loop bound is warp-uniform so that every lane reaches the ballots
-    for (int64_t p0 = tid & ~31ll; p0 < npos; p0 += nth) {
-        const int64_t p = p0 + lane;
-        const int32_t lp = p < a.n ? __ldcg(a.level_pos + p) : -1;
-        const uint32_t vb = __ballot_sync(kFull, lp >= 0);
-        const uint32_t fb = __ballot_sync(kFull, lp == L);
-        if (lane == 0) {
-            const int64_t w = p0 >> 5;
+    for (int64_t w0 = gw * 32; w0 < a.nwords; w0 += nwarps * 32) {
+        int32_t lp[32];
+#pragma unroll
+        for (int k = 0; k < 32; k++) {
+            const int64_t p = (w0 + k) * 32 + lane;
+            lp[k] = p < a.n ? __ldcg(a.level_pos + p) : -1;
+        }
+        uint32_t vb = 0, fb = 0;
+#pragma unroll
+        for (int k = 0; k < 32; k++) {
+            const uint32_t v = __ballot_sync(kFull, lp[k] >= 0);
+            const uint32_t f = __ballot_sync(kFull, lp[k] == L);
+            if (lane == k) {
+                vb = v;
+                fb = f;
+            }
+        }
+        const int64_t w = w0 + lane;
+        if (w < a.nwords) {
             const uint32_t vis = __ldg(a.vinit + w) | vb;
             a.vis[w] = vis;
             F[w] = fb;
@@ -962,8 +999,9 @@ __global__ void k_prep(BfsArgs a) {
 }
 
 __global__ void k_td(BfsArgs a) {
-    td_phase<false>(a, a.ctl->level, Range{(int)blockIdx.x, (int)gridDim.x},
-                    td_append(a, a.ctl->mf));
+    const int64_t mf = a.ctl->mf;
+    td_phase<false>(a, a.ctl->level, Range{(int)blockIdx.x, (int)gridDim.x}, mf,
+                    td_append(a, mf));
 }
 
 __global__ void k_td_big(BfsArgs a) {
@@ -1061,45 +1099,71 @@ __global__ void k_scatter(BfsArgs a, int32_t *level, int32_t *parent) {
 
 // ------------------------------------------------------ persistent kernel
 
-// Grid barrier of the persistent kernel. Its wait is bounded by
-// a.barrier_ns: on expiry it records ALB_ERR_TIMEOUT and every block leaves.
-// (withhold_level: a test hook under which one block skips its arrival at
-// level L's barriers and leaves.)
-__device__ bool grid_sync(const BfsArgs &a, unsigned nblocks, int L) {
+// Grid barrier of the persistent kernel: one 64-bit arrival counter that is
+// never reset. A block's arrival (an acquire-release atomicAdd, which also
+// publishes the block's writes) returns the count before it; the barrier it
+// belongs to ends when the count reaches the next multiple of the block
+// count, so the last arrival itself releases everyone -- no reset, no second
+// word, one round trip on the critical path. Waits are bounded by
+// a.barrier_ns: on expiry the block records ALB_ERR_TIMEOUT and sets bit 62,
+// which puts the count past every target, so every waiter leaves at once and
+// reads the failure from the same word. (withhold_level: a test hook under
+// which one block skips its arrival at level L's barriers and leaves.)
+__device__ __forceinline__ unsigned long long atom_add_acq_rel(unsigned long long *p,
+                                                               unsigned long long v) {
+    unsigned long long old;
+    asm volatile("atom.acq_rel.gpu.global.add.u64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v)
+                 : "memory");
+    return old;
+}
+
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// The level's counters as they stand after a barrier, read by thread 0
+// right after its wait (all five loads in one round trip) and shared with
+// the block by the barrier's closing __syncthreads: nbig[L % 3] (long frontier
+// rows) and the (L + 1) % 3 accumulators that roll() consumes.
+struct LevelSums {
+    unsigned long long nbig, n, mo, mi, full;
+};
+
+__device__ bool grid_sync(const BfsArgs &a, unsigned nblocks, int L, LevelSums *sums = nullptr) {
     BfsCtl *ctl = a.ctl;
     if (a.withhold_level >= 0 && L == a.withhold_level && (int)blockIdx.x == a.withhold_block)
         return false;
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        // the generation word counts barriers in its low 31 bits; bit 31 is
-        // set by a block whose wait ran out, so that every waiter sees a
-        // change and leaves (and the status needs no second load)
-        volatile unsigned *gen = &ctl->bar_gen;
-        const unsigned g0 = *gen;
-        bool ok = !(g0 & kBarFailed);
+        const unsigned long long old = atom_add_acq_rel(&ctl->bar, 1ull);
+        bool ok = !(old & kBarFailed);
         if (ok) {
-            __threadfence();
-            const unsigned arrived = atomicAdd(&ctl->bar_count, 1u);
-            if (arrived == nblocks - 1) {
-                atomicExch(&ctl->bar_count, 0u);
-                __threadfence();
-                atomicAdd(&ctl->bar_gen, 1u);
-            } else {
+            const unsigned long long target = (old / nblocks + 1) * nblocks;
+            if (old + 1 != target) {
                 const uint64_t t0 = globaltimer_ns();
-                unsigned gv;
-                while ((gv = *gen) == g0) {
+                unsigned long long cur;
+                while ((cur = ld_acquire(&ctl->bar)) < target) {
                     if (globaltimer_ns() - t0 > a.barrier_ns) {
                         atomicExch(&ctl->err, ALB_ERR_TIMEOUT);
-                        atomicOr(&ctl->bar_gen, kBarFailed);
-                        gv = kBarFailed;
+                        atomicOr(&ctl->bar, kBarFailed);
+                        cur = kBarFailed;
                         break;
                     }
-                    __nanosleep(64);
                 }
-                ok = !(gv & kBarFailed);
+                ok = !(cur & kBarFailed);
             }
-            __threadfence();
+        }
+        if (ok && sums) {
+            const volatile BfsCtl *g = ctl;
+            const int k = (L + 1) % 3;
+            sums->nbig = g->nbig[L % 3];
+            sums->n = g->acc_n[k];
+            sums->mo = g->acc_mo[k];
+            sums->mi = g->acc_mi[k];
+            sums->full = g->acc_full[k];
         }
         s_ok = ok ? 1 : 0;
     }
@@ -1114,6 +1178,7 @@ constexpr unsigned kPersistBlock = 768;
 __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(BfsArgs a) {
     __shared__ BfsCtl c;
     __shared__ int s_dir;
+    __shared__ LevelSums s_sums;
     const unsigned nb = gridDim.x;
     const Range r{(int)blockIdx.x, (int)gridDim.x};
     if (threadIdx.x == 0) c = *a.ctl;  // written by an earlier launch
@@ -1166,53 +1231,54 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(BfsArgs a) {
             }
             const bool app = td_append(a, c.mf);
             if (ok) {
-                td_phase<true>(a, L, r, app, lazy);
-                ok = grid_sync(a, nb, L);
+                td_phase<true>(a, L, r, c.mf, app, lazy);
+                ok = grid_sync(a, nb, L, &s_sums);
             }
-            if (ok && *(volatile unsigned long long *)&a.ctl->nbig[L % 3]) {
+            if (ok && s_sums.nbig) {
                 td_big_phase<true>(a, L, r, app, lazy);
-                ok = grid_sync(a, nb, L);
+                ok = grid_sync(a, nb, L, &s_sums);
             }
             if (ok && !lazy) {
                 td_finish_phase<true>(a, L, r, app);
-                ok = grid_sync(a, nb, L);
+                ok = grid_sync(a, nb, L, &s_sums);
             }
         } else if (dir == ALB_DIR_BOTTOMUP) {
             if (a.nlong) {
                 bu_long_phase<true, true>(a, L, r);
-                ok = grid_sync(a, nb, L);
-                if (ok && *(volatile unsigned long long *)&a.ctl->nbig[L % 3]) {
+                ok = grid_sync(a, nb, L, &s_sums);
+                if (ok && s_sums.nbig) {
                     bu_long_tail_phase<true, true>(a, L, r);
                     ok = grid_sync(a, nb, L);
                 }
             }
             if (ok) {
                 bu_phase<true, true, true>(a, L, r);
-                ok = grid_sync(a, nb, L);
+                ok = grid_sync(a, nb, L, &s_sums);
             }
         } else {
             if (a.nlong) {
                 bu_long_phase<true, false>(a, L, r);
-                ok = grid_sync(a, nb, L);
-                if (ok && *(volatile unsigned long long *)&a.ctl->nbig[L % 3]) {
+                ok = grid_sync(a, nb, L, &s_sums);
+                if (ok && s_sums.nbig) {
                     bu_long_tail_phase<true, false>(a, L, r);
                     ok = grid_sync(a, nb, L);
                 }
             }
             if (ok) {
                 bu_phase<true, false, false>(a, L, r);
-                ok = grid_sync(a, nb, L);
+                ok = grid_sync(a, nb, L, &s_sums);
             }
         }
         if (!ok) break;
         if (threadIdx.x == 0) {
+            // the level's last barrier read its counters into s_sums
             const int k = (L + 1) % 3;
-            volatile BfsCtl *g = a.ctl;
             if (blockIdx.x == 0 && a.trace && L < c.trace_cap) {
-                a.trace[L].bytes = level_bytes(c, dir, g->acc_n[k], g->acc_bytes[k]);
+                volatile BfsCtl *g = a.ctl;
+                a.trace[L].bytes = level_bytes(c, dir, s_sums.n, g->acc_bytes[k]);
                 write_stats(a.trace[L], *g, k);
             }
-            roll(c, dir, g->acc_n[k], g->acc_mo[k], g->acc_mi[k], g->acc_full[k]);
+            roll(c, dir, s_sums.n, s_sums.mo, s_sums.mi, s_sums.full);
             c.dir = dir;
             if (lazy) c.lazy = 1;
         }

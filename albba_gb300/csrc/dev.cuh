@@ -210,7 +210,7 @@ struct BfsCtl {
     unsigned long long nbig[3];  // rows too long for one warp, per level slot
     unsigned long long work[3];  // bottom-up word counter (grab_words), per level slot
     unsigned long long acc_stat[3][5];  // bypass statistics per level slot (kSt*)
-    unsigned int bar_count, bar_gen;  // persistent-kernel grid barrier
+    unsigned long long bar;  // persistent-kernel grid barrier: arrivals (bit 62: gave up)
     int32_t trace_cap, trace_len;
     int32_t level_cap;       // safety bound on the number of levels
     int32_t branch;          // loop-graph switch branch taken this level
