@@ -20,14 +20,18 @@
 // reference's, bit for bit.
 //
 // Rows longer than kSpLong entries (the hubs of a power-law graph) keep an
-// empty SELL row: one lane walking a hub of 10^5 entries one group at a time
-// would hold its warp -- and the whole launch -- for tens of milliseconds.
-// They are copied in CSR order to a separate list and each is summed by one
-// warp: the lanes fetch the next 32 values and x gathers together (the batch
-// after it already requested) and stage them in shared memory, and every
-// lane then runs the row's fma chain over them in order. The chain itself
-// stays sequential -- its order is what makes y bit-identical -- so a hub
-// costs one dependent fma per entry, but no memory latency per entry.
+// empty SELL row: in a slice a hub's lane waits on one group of x gathers at
+// a time and holds its warp -- and the whole launch -- for tens of
+// milliseconds. They are copied in CSR order to a separate list (longest
+// first, each row padded to 8 entries so that a lane reads its row in
+// aligned 32-byte column and 64-byte value blocks) and summed lane per row
+// by k_spmv_long, which keeps two blocks of x gathers in flight ahead of the
+// fma chain. The chain itself stays sequential -- its order is what makes y
+// bit-identical -- and a dependent fp64 fma costs about 90 cycles on GB300
+// (the fp64 pipe takes as long for one active lane as for 32), so the launch
+// can end no sooner than the longest row's length x that latency; lane per
+// row keeps every other row's chains, 32 per warp instruction, off the fp64
+// pipe's critical path. The long rows run on a side stream beside the slices.
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -39,7 +43,8 @@
 struct alb_sellmat {
     int device = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaStream_t side = nullptr;  // the long rows run beside the slices
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, fork = nullptr, join = nullptr;
     int64_t n = 0, nnz = 0, nslices = 0, stored = 0;
     int32_t sigma = 0;
     int32_t *perm = nullptr;       // position -> row
@@ -50,10 +55,11 @@ struct alb_sellmat {
     double *dx = nullptr, *dy = nullptr;  // staging for host vectors
     int64_t nlong = 0;             // rows longer than kSpLong, summed by a warp each
     int32_t *lrow = nullptr;       // their row ids, longest first
-    int64_t *lptr = nullptr;       // nlong + 1 offsets into lcol / lval
-    int32_t *lcol = nullptr;       // their entries in CSR order
+    int64_t *lptr = nullptr;       // first entry of each in lcol / lval (multiple of 8)
+    int32_t *llen = nullptr;       // their lengths
+    int32_t *lcol = nullptr;       // their entries in CSR order, each row padded to 8
     double *lval = nullptr;
-    unsigned long long *ctr = nullptr;  // k_spmv_long's row counter
+    int32_t max_long = 0;          // the longest row's length
 };
 
 namespace alb {
@@ -172,48 +178,104 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, int64_t nslices, const 
     }
 }
 
-// One warp per long row (the list is longest first, handed out from a
-// counter): batches of 32 entries, lane l fetching entry l of a batch -- its
-// value and x[column] -- one batch ahead; the batch goes to shared memory and
-// every lane then applies its 32 fmas in order, so all lanes carry the same
-// accumulator and lane 0 writes it.
-constexpr int kSpLongBlock = 128;
+// Lane per long row (rows longest first). The first nsolo warps (one per SM,
+// launched first) take one row each, the longest ones, so that the chains
+// that set the launch's length neither wait on 31 other lanes' gathers (a
+// warp's cp.async wait ends when its slowest lane's copies land) nor share an
+// SM with another long chain; the rest go 32 rows of similar length per warp.
+// Entries in blocks of kLb. Each lane streams its row through two
+// shared-memory rings filled by cp.async: column ids kLd blocks ahead of the
+// x gathers that need them, values and x (each gather 8 bytes) kLd blocks
+// ahead of the fmas. The group committed at step t carries block t's values
+// and gathers and block t + kLd's columns, so one wait gives both. With the
+// fma chain at about 90 cycles per entry, each load has kLd x kLb entries'
+// worth of chain time to land. Ring layout: lane-fastest, so that the 32
+// lanes' accesses fall in different banks.
+constexpr int kSpLongBlock = 32;
+constexpr int kLb = 8;
+constexpr int kLd = 8;
 
-__global__ void __launch_bounds__(kSpLongBlock) k_spmv_long(
-    int64_t nlong, const int32_t *lrow, const int64_t *lptr, const int32_t *lcol,
-    const double *lval, const double *x, double *y, unsigned long long *ctr) {
-    __shared__ double s_v[kSpLongBlock / 32][32], s_x[kSpLongBlock / 32][32];
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+__global__ void __launch_bounds__(kSpLongBlock) k_spmv_long(int64_t nlong, int64_t nsolo,
+                                                         const int32_t *lrow, const int64_t *lptr,
+                                                         const int32_t *llen, const int32_t *lcol,
+                                                         const double *lval, const double *x,
+                                                         double *y) {
+    __shared__ double2 s_v[kSpLongBlock / 32][kLd][kLb / 2][32];
+    __shared__ double s_x[kSpLongBlock / 32][kLd][kLb][32];
+    __shared__ int4 s_c[kSpLongBlock / 32][kLd][kLb / 4][32];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    for (;;) {
-        unsigned long long i = 0;
-        if (lane == 0) i = atomicAdd(ctr, 1ull);
-        i = __shfl_sync(kFull, i, 0);
-        if ((int64_t)i >= nlong) break;
-        const int64_t b = lptr[i], e = lptr[i + 1];
-        double acc = 0.0;
-        // batch k holds entries b + 32k .. b + 32k + 31
-        double v = 0.0, xv = 0.0;
-        if (b + lane < e) {
-            v = __ldcs(lval + b + lane);
-            xv = __ldg(x + __ldcs(lcol + b + lane));
+    const int64_t wg = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t i = wg < nsolo ? (lane == 0 ? wg : nlong) : nsolo + (wg - nsolo) * 32 + lane;
+    const int64_t b = i < nlong ? lptr[i] : 0;
+    const int64_t e = i < nlong ? b + llen[i] : 0;
+    const int64_t nblk = (e - b + kLb - 1) / kLb;
+    // values and x of block t (columns c); columns of block t + kLd
+    auto issue = [&](int64_t t, const int32_t (&c)[kLb]) {
+        const int slot = (int)(t % kLd);
+        if (t < nblk) {
+            const int64_t s0 = b + t * kLb;
+            const double2 *src = reinterpret_cast<const double2 *>(lval + s0);
+#pragma unroll
+            for (int h = 0; h < kLb / 2; h++) cp_async16(&s_v[wib][slot][h][lane], src + h);
+#pragma unroll
+            for (int k = 0; k < kLb; k++)
+                if (s0 + k < e) cp_async8(&s_x[wib][slot][k][lane], x + c[k]);
         }
-        for (int64_t t = b; t < e; t += 32) {
-            double vn = 0.0, xn = 0.0;
-            if (t + 32 + lane < e) {
-                vn = __ldcs(lval + t + 32 + lane);
-                xn = __ldg(x + __ldcs(lcol + t + 32 + lane));
-            }
-            __syncwarp();
-            s_v[wib][lane] = v;
-            s_x[wib][lane] = xv;
-            __syncwarp();
-            const int cnt = (int)min((int64_t)32, e - t);
-            for (int k = 0; k < cnt; k++) acc = fma(s_v[wib][k], s_x[wib][k], acc);
-            v = vn;
-            xv = xn;
+        if (t + kLd < nblk) {
+            const int4 *src = reinterpret_cast<const int4 *>(lcol + b + (t + kLd) * kLb);
+#pragma unroll
+            for (int h = 0; h < kLb / 4; h++) cp_async16(&s_c[wib][slot][h][lane], src + h);
         }
-        if (lane == 0) y[lrow[i]] = acc;
+        cp_async_commit();
+    };
+    int32_t c[kLb];
+    for (int t = 0; t < kLd; t++) {
+#pragma unroll
+        for (int k = 0; k < kLb; k++) c[k] = 0;
+        if (t < nblk) {
+            const int4 *q = reinterpret_cast<const int4 *>(lcol + b + (int64_t)t * kLb);
+            const int4 u = __ldcs(q), w = __ldcs(q + 1);
+            c[0] = u.x, c[1] = u.y, c[2] = u.z, c[3] = u.w;
+            c[4] = w.x, c[5] = w.y, c[6] = w.z, c[7] = w.w;
+        }
+        issue(t, c);
     }
+    double acc = 0.0;
+    for (int64_t t = 0; t < nblk; t++) {
+        cp_async_wait<kLd - 1>();  // this lane's group t has landed
+        const int slot = (int)(t % kLd);
+        const int64_t rem = e - (b + t * kLb);
+#pragma unroll
+        for (int h = 0; h < kLb / 2; h++) {
+            const double2 v = s_v[wib][slot][h][lane];
+            if (2 * h < rem) acc = fma(v.x, s_x[wib][slot][2 * h][lane], acc);
+            if (2 * h + 1 < rem) acc = fma(v.y, s_x[wib][slot][2 * h + 1][lane], acc);
+        }
+        // block t + kLd's columns (landed with group t), read out before the
+        // slot is refilled; the refill comes after the fmas in program order,
+        // so their shared loads have landed when the copies issue
+        const int4 u = s_c[wib][slot][0][lane], w = s_c[wib][slot][1][lane];
+        c[0] = u.x, c[1] = u.y, c[2] = u.z, c[3] = u.w;
+        c[4] = w.x, c[5] = w.y, c[6] = w.z, c[7] = w.w;
+        asm volatile("" ::"d"(acc), "r"(c[0]), "r"(c[7]) : "memory");
+        issue(t + kLd, c);
+    }
+    cp_async_wait<0>();
+    if (i < nlong) y[lrow[i]] = acc;
 }
 
 __global__ void k_sp_long_flags(int64_t n, const int32_t *len, int32_t *flag) {
@@ -229,13 +291,13 @@ __global__ void k_sp_long_scatter(int64_t n, const int32_t *flag, const int64_t 
 
 // One warp per long row: its entries copied in CSR order.
 __global__ void k_sp_long_fill(int64_t nlong, const int32_t *lrow, const int64_t *lptr,
-                               const int64_t *rp, const int32_t *col, const double *val,
-                               int32_t *lcol, double *lval) {
+                               const int32_t *llen, const int64_t *rp, const int32_t *col,
+                               const double *val, int32_t *lcol, double *lval) {
     const int lane = threadIdx.x & 31;
     const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t i = w0; i < nlong; i += nw) {
-        const int64_t src = rp[lrow[i]], dst = lptr[i], len = lptr[i + 1] - dst;
+        const int64_t src = rp[lrow[i]], dst = lptr[i], len = llen[i];
         for (int64_t k = lane; k < len; k += 32) {
             lcol[dst + k] = col[src + k];
             lval[dst + k] = val[src + k];
@@ -301,7 +363,6 @@ alb_status build(alb_sellmat *m, const int64_t *rowptr, const int32_t *col, cons
             int64_t *p;
             ~Free() { dfree(p); }
         } free_idx{idx};
-        ALB_TRY(dmalloc((void **)&m->ctr, sizeof(unsigned long long), "SpMV counter"));
         int32_t *flags = nullptr;
         ALB_TRY(dmalloc((void **)&flags, sizeof(int32_t) * (size_t)n, "SpMV long flags"));
         struct Free32 {
@@ -329,22 +390,34 @@ alb_status build(alb_sellmat *m, const int64_t *rowptr, const int32_t *col, cons
             for (int64_t i = 0; i < nl; i++) order[(size_t)i] = i;
             std::stable_sort(order.begin(), order.end(),
                              [&](int64_t x, int64_t y) { return hlen[(size_t)x] > hlen[(size_t)y]; });
-            std::vector<int32_t> srow((size_t)nl);
+            std::vector<int32_t> srow((size_t)nl), slen((size_t)nl);
             std::vector<int64_t> sptr((size_t)nl + 1, 0);
             for (int64_t i = 0; i < nl; i++) {
+                const int64_t len = hlen[(size_t)order[(size_t)i]];
                 srow[(size_t)i] = hrow[(size_t)order[(size_t)i]];
-                sptr[(size_t)i + 1] = sptr[(size_t)i] + hlen[(size_t)order[(size_t)i]];
+                slen[(size_t)i] = (int32_t)len;
+                sptr[(size_t)i + 1] = sptr[(size_t)i] + ((len + kLb - 1) / kLb) * kLb;
             }
+            m->max_long = slen[0];
+            ALB_TRY(dmalloc((void **)&m->llen, sizeof(int32_t) * (size_t)nl, "SpMV long lengths"));
             ALB_CK(cudaMemcpyAsync(m->lrow, srow.data(), sizeof(int32_t) * (size_t)nl,
+                                   cudaMemcpyHostToDevice, st));
+            ALB_CK(cudaMemcpyAsync(m->llen, slen.data(), sizeof(int32_t) * (size_t)nl,
                                    cudaMemcpyHostToDevice, st));
             ALB_CK(cudaMemcpyAsync(m->lptr, sptr.data(), sizeof(int64_t) * (size_t)(nl + 1),
                                    cudaMemcpyHostToDevice, st));
+            // padded entries are never summed; zeroed so that the layout is
+            // fixed by the CSR alone
             const int64_t nent = sptr[(size_t)nl];
             ALB_TRY(dmalloc((void **)&m->lcol, sizeof(int32_t) * (size_t)nent, "SpMV long columns"));
             ALB_TRY(dmalloc((void **)&m->lval, sizeof(double) * (size_t)nent, "SpMV long values"));
-            k_sp_long_fill<<<blocks_for(nl * 32, 256), 256, 0, st>>>(nl, m->lrow, m->lptr, d_rp,
-                                                                    d_col, d_val, m->lcol, m->lval);
+            ALB_CK(cudaMemsetAsync(m->lcol, 0, sizeof(int32_t) * (size_t)nent, st));
+            ALB_CK(cudaMemsetAsync(m->lval, 0, sizeof(double) * (size_t)nent, st));
+            k_sp_long_fill<<<blocks_for(nl * 32, 256), 256, 0, st>>>(
+                nl, m->lrow, m->lptr, m->llen, d_rp, d_col, d_val, m->lcol, m->lval);
             ALB_CK(cudaGetLastError());
+            // the host vectors must outlive the copies
+            ALB_CK(cudaStreamSynchronize(st));
         }
         ALB_CK(cudaStreamSynchronize(st));
         return ALB_OK;
@@ -370,10 +443,14 @@ void destroy(alb_sellmat *m) {
     dfree(m->lptr);
     dfree(m->lcol);
     dfree(m->lval);
-    dfree(m->ctr);
+    dfree(m->llen);
+    if (m->side) cudaStreamSynchronize(m->side);
     if (m->ev0) cudaEventDestroy(m->ev0);
     if (m->ev1) cudaEventDestroy(m->ev1);
+    if (m->fork) cudaEventDestroy(m->fork);
+    if (m->join) cudaEventDestroy(m->join);
     if (m->stream) cudaStreamDestroy(m->stream);
+    if (m->side) cudaStreamDestroy(m->side);
     cudaGetLastError();
     if (prev >= 0) cudaSetDevice(prev);
     delete m;
@@ -387,15 +464,23 @@ alb_status launch(alb_sellmat *m, const double *d_x, double *d_y, float *us) {
     const int64_t cap = (int64_t)(per > 0 ? per : 4) * sms;
     const unsigned grid = (unsigned)std::max<int64_t>(1, std::min(want, cap));
     if (us) ALB_CK(cudaEventRecord(m->ev0, m->stream));
+    // the long rows' chains (one dependent fma per entry, the longest row
+    // the critical path) start first, on the side stream, and the slices
+    // run beside them
+    if (m->nlong > 0) {
+        ALB_CK(cudaEventRecord(m->fork, m->stream));
+        ALB_CK(cudaStreamWaitEvent(m->side, m->fork, 0));
+        const int64_t nsolo = std::min<int64_t>(m->nlong, sms);
+        const int64_t warps = nsolo + (m->nlong - nsolo + 31) / 32;
+        k_spmv_long<<<blocks_for(warps * 32, kSpLongBlock), kSpLongBlock, 0, m->side>>>(
+            m->nlong, nsolo, m->lrow, m->lptr, m->llen, m->lcol, m->lval, d_x, d_y);
+        ALB_CK(cudaGetLastError());
+        ALB_CK(cudaEventRecord(m->join, m->side));
+    }
     k_spmv<<<grid, 256, 0, m->stream>>>(m->n, m->nslices, m->perm, m->deg, m->slice_off, m->col,
                                          m->val, d_x, d_y);
-    if (m->nlong > 0) {
-        ALB_CK(cudaMemsetAsync(m->ctr, 0, sizeof(unsigned long long), m->stream));
-        const int64_t warps = std::min<int64_t>(m->nlong, (int64_t)sms * 16);
-        k_spmv_long<<<(unsigned)((warps + 3) / 4), kSpLongBlock, 0, m->stream>>>(
-            m->nlong, m->lrow, m->lptr, m->lcol, m->lval, d_x, d_y, m->ctr);
-    }
     ALB_CK(cudaGetLastError());
+    if (m->nlong > 0) ALB_CK(cudaStreamWaitEvent(m->stream, m->join, 0));
     if (us) {
         ALB_CK(cudaEventRecord(m->ev1, m->stream));
         ALB_CK(cudaEventSynchronize(m->ev1));
@@ -430,6 +515,9 @@ alb_status alb_sellmat_create(int64_t n, const int64_t *rowptr, const int32_t *c
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&m->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&m->ev1);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&m->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&m->join, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         cudaGetLastError();
         destroy(m);

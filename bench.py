@@ -198,12 +198,17 @@ def run_reference(args, rank: int, world: int) -> None:
     comp = {}
     times = []
     edges = 0
+    agree = True
     for i in range(args.warmup + args.steps):
         r = int(roots[i % len(roots)])
         counts, bms = ra.run(r)
         if r not in comp:
             lv, _, _ = oracle.bfs(g.rowptr, g.col, r)
             comp[r] = int(deg[lv >= 0].sum()) // 2
+            # the loop's per-level frontier sizes against the queue BFS's
+            # level sets (the reference's own -v 1 check), outside the timing
+            want = np.bincount(lv[lv >= 0]) if (lv >= 0).any() else np.zeros(0, np.int64)
+            agree = agree and np.array_equal(np.asarray(counts), want)
         if i >= args.warmup:
             times.append(bms)
             edges += comp[r]
@@ -219,6 +224,7 @@ def run_reference(args, rank: int, world: int) -> None:
             "cpu_baseline": {"value": v, "unit": "GTEPS", "cores": threads, "kind": "port",
                              "sample": f"{args.steps} timed roots, one per step, level loop "
                                        f"only, {REF_TASKS} tasks per level"},
+            "frontier_counts_match_oracle": bool(agree),
             "e2e": {"value": v, "unit": "GTEPS", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     ra.close()
