@@ -60,14 +60,16 @@ struct Range {
 // ------------------------------------------------------------ level phases
 
 // Decision (one warp). forced >= 0 overrides the policy (host-driven loop).
-__device__ int decide_warp(const BfsArgs &a, const BfsCtl &c, int forced) {
+// P: the network's parameters (a.mlp, or a shared-memory copy of them).
+__device__ int decide_warp(const BfsArgs &a, const BfsCtl &c, int forced,
+                           const float *P = nullptr) {
     int dir;
     if (forced >= 0) {
         dir = forced;
     } else if (c.policy == ALB_POLICY_LEARNED && a.mlp && a.mlp[kMlpParams] != 0.0f) {
         float f[kMlpIn];
         level_features(c, f);
-        dir = mlp_select_warp(a.mlp, f);
+        dir = mlp_select_warp(P ? P : a.mlp, f);
     } else {
         dir = rule_dir(c);
     }
@@ -379,8 +381,30 @@ __device__ void td_phase(const BfsArgs &a, int L, Range r, int64_t mf, bool appe
         }
         __syncwarp();
     }
-    if (lazy) lc.flush(a, L);
-    add_stat(a, L, kStEdgesBypassed, bypassed);
+    // the level's counters and the bypass statistic, combined in the block
+    // first: one atomic per block and counter instead of one per warp (each
+    // warp's would land on the same few words, where L2 serialises them)
+    __shared__ unsigned long long s_c[4];
+    if (threadIdx.x < 4) s_c[threadIdx.x] = 0;
+    __syncthreads();
+    const unsigned long long cn = warp_sum((unsigned long long)lc.n), cmo = warp_sum(lc.mo),
+                             cmi = warp_sum(lc.mi), cb = warp_sum((unsigned long long)bypassed);
+    if ((threadIdx.x & 31) == 0) {
+        if (cn) atomicAdd(&s_c[0], cn);
+        if (cmo) atomicAdd(&s_c[1], cmo);
+        if (cmi) atomicAdd(&s_c[2], cmi);
+        if (cb) atomicAdd(&s_c[3], cb);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int k = (L + 1) % 3;
+        if (s_c[0]) {
+            atomicAdd(&a.ctl->acc_n[k], s_c[0]);
+            atomicAdd(&a.ctl->acc_mo[k], s_c[1]);
+            atomicAdd(&a.ctl->acc_mi[k], s_c[2]);
+        }
+        if (s_c[3]) atomicAdd(&a.ctl->acc_stat[k][kStEdgesBypassed], s_c[3]);
+    }
 }
 
 // Long frontier rows, kBigChunk edges per chunk, chunks spread over all
@@ -961,6 +985,7 @@ __global__ void k_init_root(BfsArgs a, InitParams ip) {
     c.feat_mean_deg = ip.mean_deg;
     c.feat_skew = ip.skew;
     *a.ctl = c;
+    *a.bar = 0;
 }
 
 __global__ void k_decide(BfsArgs a, int forced, cudaGraphConditionalHandle sw) {
@@ -1138,17 +1163,17 @@ __device__ bool grid_sync(const BfsArgs &a, unsigned nblocks, int L, LevelSums *
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        const unsigned long long old = atom_add_acq_rel(&ctl->bar, 1ull);
+        const unsigned long long old = atom_add_acq_rel(a.bar, 1ull);
         bool ok = !(old & kBarFailed);
         if (ok) {
             const unsigned long long target = (old / nblocks + 1) * nblocks;
             if (old + 1 != target) {
                 const uint64_t t0 = globaltimer_ns();
                 unsigned long long cur;
-                while ((cur = ld_acquire(&ctl->bar)) < target) {
+                while ((cur = ld_acquire(a.bar)) < target) {
                     if (globaltimer_ns() - t0 > a.barrier_ns) {
                         atomicExch(&ctl->err, ALB_ERR_TIMEOUT);
-                        atomicOr(&ctl->bar, kBarFailed);
+                        atomicOr(a.bar, kBarFailed);
                         cur = kBarFailed;
                         break;
                     }
@@ -1179,13 +1204,17 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(BfsArgs a) {
     __shared__ BfsCtl c;
     __shared__ int s_dir;
     __shared__ LevelSums s_sums;
+    // the selector network, read once per launch instead of once per level
+    __shared__ __align__(16) float s_mlp[kMlpParams + 1];
     const unsigned nb = gridDim.x;
     const Range r{(int)blockIdx.x, (int)gridDim.x};
     if (threadIdx.x == 0) c = *a.ctl;  // written by an earlier launch
+    if (a.mlp)
+        for (int i = threadIdx.x; i <= kMlpParams; i += blockDim.x) s_mlp[i] = a.mlp[i];
     __syncthreads();
     while (true) {
         if (threadIdx.x < 32) {
-            const int dir = decide_warp(a, c, -1);
+            const int dir = decide_warp(a, c, -1, s_mlp);
             if (threadIdx.x == 0) {
                 s_dir = dir;
                 if (blockIdx.x == 0) {
@@ -1366,6 +1395,7 @@ alb_status bfs_scratch_alloc(alb_graph *g) {
     ALB_TRY(dmalloc((void **)&b.level_pos, sizeof(int32_t) * n, "levels"));
     ALB_TRY(dmalloc((void **)&b.parent_pos, sizeof(uint32_t) * n, "parents"));
     ALB_TRY(dmalloc((void **)&b.ctl, sizeof(BfsCtl), "level control"));
+    ALB_TRY(dmalloc((void **)&b.bar, 256, "grid barrier"));
     b.trace_cap = (int32_t)std::min<int64_t>(n + 2, 1 << 16);
     ALB_TRY(dmalloc((void **)&b.trace, sizeof(alb_level_rec) * b.trace_cap, "level trace"));
     ALB_CK(cudaMallocHost((void **)&b.h_ctl, sizeof(BfsCtl)));
@@ -1385,6 +1415,7 @@ void bfs_scratch_free(alb_graph *g) {
     dfree(b.out_level);
     dfree(b.out_parent);
     dfree(b.ctl);
+    dfree(b.bar);
     dfree(b.trace);
     if (b.h_ctl) cudaFreeHost(b.h_ctl);
     b = BfsScratch();
@@ -1440,6 +1471,7 @@ BfsArgs make_args(alb_graph *g) {
     a.level_pos = b.level_pos;
     a.parent_pos = b.parent_pos;
     a.ctl = b.ctl;
+    a.bar = b.bar;
     a.trace = b.trace;
     a.mlp = selector_device_params(0);
     const DeviceWaits dw = device_waits(kBarrierTimeoutNs, kBulkWaitNs);

@@ -210,7 +210,6 @@ struct BfsCtl {
     unsigned long long nbig[3];  // rows too long for one warp, per level slot
     unsigned long long work[3];  // bottom-up word counter (grab_words), per level slot
     unsigned long long acc_stat[3][5];  // bypass statistics per level slot (kSt*)
-    unsigned long long bar;  // persistent-kernel grid barrier: arrivals (bit 62: gave up)
     int32_t trace_cap, trace_len;
     int32_t level_cap;       // safety bound on the number of levels
     int32_t branch;          // loop-graph switch branch taken this level
@@ -258,6 +257,8 @@ struct BfsArgs {
     int32_t *level_pos;        // depth by position
     uint32_t *parent_pos;      // parent original id by position
     BfsCtl *ctl;
+    unsigned long long *bar;   // persistent-kernel grid barrier: arrivals (bit 62: gave up),
+                               // its own allocation, apart from the counters' cache lines
     alb_level_rec *trace;
     const float *mlp;          // selector parameters or null
     // bounded waits (DeviceWaits): limits and test hooks

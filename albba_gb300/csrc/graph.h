@@ -96,6 +96,7 @@ struct BfsScratch {
     int32_t *out_level = nullptr, *out_parent = nullptr;  // staging for host outputs
     BfsCtl *ctl = nullptr;
     BfsCtl *h_ctl = nullptr;  // pinned mirror
+    unsigned long long *bar = nullptr;  // persistent-kernel grid barrier
     alb_level_rec *trace = nullptr;
     int32_t trace_cap = 0;
 };

@@ -64,21 +64,22 @@ __host__ __device__ inline int argmin3(const float *o) {
 // all of its parameter loads (its rows of W1 and W2 as 16-byte loads, its
 // biases, its column of W3), so the pass costs one memory round trip rather
 // than one per layer; P must be 16-byte aligned (the parameter blocks are).
+// P may point to global memory or to a shared-memory copy (generic loads).
 __device__ inline int mlp_select_warp(const float *P, const float *x) {
     const int j = threadIdx.x & 31;
     const float4 *w1 = reinterpret_cast<const float4 *>(P + kMlpW1 + j * kMlpIn);
     const float4 *w2 = reinterpret_cast<const float4 *>(P + kMlpW2 + j * kMlpH);
     float4 r1[kMlpIn / 4], r2[kMlpH / 4];
 #pragma unroll
-    for (int i = 0; i < kMlpIn / 4; i++) r1[i] = __ldg(w1 + i);
+    for (int i = 0; i < kMlpIn / 4; i++) r1[i] = w1[i];
 #pragma unroll
-    for (int i = 0; i < kMlpH / 4; i++) r2[i] = __ldg(w2 + i);
-    const float b1 = __ldg(P + kMlpB1 + j), b2 = __ldg(P + kMlpB2 + j);
+    for (int i = 0; i < kMlpH / 4; i++) r2[i] = w2[i];
+    const float b1 = P[kMlpB1 + j], b2 = P[kMlpB2 + j];
     float w3[kMlpOut], b3[kMlpOut];
 #pragma unroll
     for (int k = 0; k < kMlpOut; k++) {
-        w3[k] = __ldg(P + kMlpW3 + k * kMlpH + j);
-        b3[k] = __ldg(P + kMlpB3 + k);
+        w3[k] = P[kMlpW3 + k * kMlpH + j];
+        b3[k] = P[kMlpB3 + k];
     }
     float a = b1;
 #pragma unroll
