@@ -62,7 +62,16 @@ struct MsCtl {
     int64_t push_budget;
     unsigned long long used;  // root bits in use
     int32_t pushed_roots;     // sum of popc(tmask) over the levels
+    int32_t gtrace_on;        // graph loop: record each level in MsArgs::gtrace
 };
+static_assert(sizeof(MsCtl) % 8 == 0, "k_ms_end moves the control block in 8-byte words");
+
+// Level records of the CUDA-graph loop (the benchmarked form), written on the
+// device: start (k_ms_branch) and end (k_ms_end) %globaltimer stamps, the
+// level's algorithmic bytes, its direction, and the frontier and unvisited
+// counts it started from.
+constexpr int kGTraceCap = 1 << 14;
+constexpr int kGTraceW = 8;
 
 // Rows and push degrees of each root's sampled frontier. Kept beside the
 // control block (same allocation) so that k_ms_end's copy of it stays small.
@@ -115,6 +124,7 @@ struct MsArgs {
     MsSample *smp;  // directly after *ctl
     int32_t long_row;  // rows with more sources than this are the long rows
     const float *mlp;
+    long long *gtrace;  // kGTraceCap x kGTraceW level records (MsCtl::gtrace_on)
 };
 
 __device__ __forceinline__ uint32_t *nz_bits(const MsArgs &a, int L) {
@@ -159,6 +169,7 @@ struct MsInit {
     float alpha, beta, mean_deg, skew;
     int64_t n_live, m_in, active0, push_budget;
     int32_t grab;
+    int32_t gtrace;  // record the graph loop's levels
 };
 
 // One block of 64 threads: thread i seeds root i; thread 0 fills the control block.
@@ -225,6 +236,7 @@ __global__ void k_ms_roots(MsArgs a, MsInit in) {
         c.push_budget = in.push_budget;
         c.grab = in.grab;
         c.used = in.nroots >= 64 ? kAll : (1ull << in.nroots) - 1;
+        c.gtrace_on = in.gtrace;
         c.done = c.nf == 0;
         // level 0's direction: the rule of later levels (the learned policy
         // falls back to Beamer here: no level has run yet)
@@ -1213,6 +1225,18 @@ __global__ void k_ms_end(MsArgs a, int dir, cudaGraphConditionalHandle wh) {
             if (dir < 0) dir = c.dir;
             const int k = (c.level + 1) % 3;
             const unsigned long long nn = c.acc_n[k];
+            if (c.gtrace_on && c.level < kGTraceCap) {
+                long long *r = a.gtrace + (int64_t)c.level * kGTraceW;
+                r[1] = (long long)globaltimer_ns();
+                r[2] = dir == ALB_DIR_TOPDOWN
+                           ? (long long)(20 * c.nf + 16 * c.mf + 16 * (int64_t)nn)
+                           : (long long)c.acc_bytes[k] + 8 * a.npad + 8 * a.nwords;
+                r[3] = dir;
+                r[4] = c.nf;
+                r[5] = c.mf;
+                r[6] = c.nu;
+                r[7] = c.mu;
+            }
             c.prev_nf = c.nf;
             c.nf = (int64_t)nn;
             c.mf = (int64_t)c.acc_mo[k];
@@ -1322,6 +1346,8 @@ __global__ void k_ms_end(MsArgs a, int dir, cudaGraphConditionalHandle wh) {
 // Graph loop: the level's branch (none once done).
 __global__ void k_ms_branch(MsArgs a, cudaGraphConditionalHandle sh) {
     const MsCtl *c = a.ctl;
+    if (c->gtrace_on && !c->done && c->level < kGTraceCap)
+        a.gtrace[(int64_t)c->level * kGTraceW] = (long long)globaltimer_ns();
     cudaGraphSetConditional(sh, c->done ? (unsigned)kBrCount : (unsigned)c->branch);
 }
 
@@ -1505,6 +1531,7 @@ struct MsScratch {
     int64_t *big_base = nullptr;
     MsCtl *ctl = nullptr, *h_ctl = nullptr;
     int32_t *out = nullptr;
+    long long *gtrace = nullptr;  // the graph loop's level records
     // CUDA-graph level loop (built for one block size)
     cudaGraph_t lg = nullptr;
     cudaGraphExec_t lexec = nullptr;
@@ -1533,6 +1560,7 @@ void ms_scratch_free(alb_graph *g) {
     dfree(m.big_base);
     dfree(m.ctl);
     dfree(m.out);
+    dfree(m.gtrace);
     if (m.h_ctl) cudaFreeHost(m.h_ctl);
     if (m.lexec) cudaGraphExecDestroy(m.lexec);
     if (m.lg) cudaGraphDestroy(m.lg);
@@ -1582,6 +1610,8 @@ alb_status ms_alloc(alb_graph *g, MsScratch &m) {
     ALB_TRY(dmalloc((void **)&m.big, sizeof(int32_t) * npad, "msbfs long-row list"));
     ALB_TRY(dmalloc((void **)&m.big_base, sizeof(int64_t) * npad, "msbfs long-row chunk bases"));
     ALB_TRY(dmalloc((void **)&m.ctl, sizeof(MsCtl) + sizeof(MsSample), "msbfs control"));
+    ALB_TRY(dmalloc((void **)&m.gtrace, sizeof(long long) * kGTraceCap * kGTraceW,
+                    "msbfs level records"));
     ALB_CK(cudaMallocHost((void **)&m.h_ctl, sizeof(MsCtl)));
     m.ready = true;
     return ALB_OK;
@@ -1622,6 +1652,7 @@ MsArgs ms_args(alb_graph *g, MsScratch &m) {
     a.big_base = m.big_base;
     a.ctl = m.ctl;
     a.smp = reinterpret_cast<MsSample *>(m.ctl + 1);
+    a.gtrace = m.gtrace;
     return a;
 }
 
@@ -1804,6 +1835,10 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
     }
     const int32_t level_cap = (int32_t)std::min<int64_t>(g->n + 1, INT32_MAX - 1);
     in.level_cap = level_cap;
+    // a traced run of the graph loop records its levels on the device, so
+    // the trace times the benchmarked form itself
+    const bool gtrace = trace && !prof && o.loop == ALB_LOOP_GRAPH;
+    in.gtrace = gtrace ? 1 : 0;
     const uint64_t unused = nroots >= 64 ? 0ull : ~((1ull << nroots) - 1);
     ALB_CK(cudaEventRecord(g->ev0, stream));
     k_ms_init<<<wide, 256, 0, stream>>>(a, unused);
@@ -1828,7 +1863,7 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
         launches++;
         return ALB_OK;
     };
-    if (o.loop == ALB_LOOP_GRAPH && !trace && !prof) {
+    if (o.loop == ALB_LOOP_GRAPH && (!trace || gtrace) && !prof) {
         // device-driven level loop: the host only steps in for flushes
         if (!m.lexec || m.lblock != block) ALB_TRY(build_ms_graph(g, m, a, block));
         while (true) {
@@ -1841,6 +1876,30 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
         }
         // per level: branch, sample and end kernels plus the branch's step kernels
         launches += (int64_t)h->levels_td * 9 + (int64_t)h->levels_bu * 10;
+        if (gtrace) {
+            const int nl = std::min<int>(h->level, kGTraceCap);
+            std::vector<long long> rec((size_t)nl * kGTraceW);
+            if (nl > 0)
+                ALB_CK(cudaMemcpyAsync(rec.data(), m.gtrace, sizeof(long long) * rec.size(),
+                                       cudaMemcpyDeviceToHost, stream));
+            ALB_CK(cudaStreamSynchronize(stream));
+            trace->clear();
+            for (int L = 0; L < nl; L++) {
+                const long long *r = rec.data() + (size_t)L * kGTraceW;
+                alb_level_rec t;
+                std::memset(&t, 0, sizeof(t));
+                t.level = L;
+                t.dir = (int32_t)r[3];
+                t.nf = r[4];
+                t.mf = r[5];
+                t.nu = r[6];
+                t.mu = r[7];
+                t.t_ns = r[0];
+                t.step_us = (float)((r[1] - r[0]) / 1e3);
+                t.bytes = r[2];
+                trace->push_back(t);
+            }
+        }
     } else {
         ALB_CK(cudaMemcpyAsync(h, a.ctl, sizeof(MsCtl), cudaMemcpyDeviceToHost, stream));
         ALB_CK(cudaStreamSynchronize(stream));
