@@ -1250,7 +1250,10 @@ __global__ void k_ms_end(MsArgs a, int dir, cudaGraphConditionalHandle wh) {
             c.dir = dir;
             if (dir == ALB_DIR_TOPDOWN) c.levels_td++; else c.levels_bu++;
             c.level++;
-            c.launches += 1;
+            // kernels of this level in the graph loop: branch, sample and end,
+            // plus the branch's steps (six top-down; seven bottom-up, four in
+            // kBrBU, which has no push)
+            c.launches += 3 + (c.branch == kBrTD ? 6 : c.branch == kBrBU ? 4 : 7);
             if (nn == 0) c.done = 1;
             if (!c.done && c.level >= c.level_cap) {  // cannot happen in a BFS: refuse
                 c.done = 1;
@@ -1761,10 +1764,18 @@ alb_status build_ms_graph(alb_graph *g, MsScratch &m, MsArgs &a, int block) {
         }
         return ALB_OK;
     };
-    auto bu = [&](int br, const void *slices, bool early) -> alb_status {
+    // push: the branch can be the first bottom-up level after a top-down one,
+    // the only level whose tmask roots are pushed (kBrBU never is: it is the
+    // unfiltered branch of later levels, so its three push launches, which
+    // would return at once, are left out)
+    auto bu = [&](int br, const void *slices, bool early, bool push) -> alb_status {
         const void *hd = early ? (const void *)k_ms_bu_long<true> : (const void *)k_ms_bu_long<false>;
         const void *tl = early ? (const void *)k_ms_bu_long_tail<true>
                                : (const void *)k_ms_bu_long_tail<false>;
+        if (!push)
+            return chain(sp.conditional.phGraph_out[br],
+                         {{res(slices, kMsBuBlock), aj}, {res(hd, block), ajf},
+                          {res(tl, block), ajf}, {res((const void *)k_ms_bu_long_fin, block), aj}});
         return chain(sp.conditional.phGraph_out[br],
                      {{res(slices, kMsBuBlock), aj}, {res(hd, block), ajf}, {res(tl, block), ajf},
                       {res((const void *)k_ms_bu_long_fin, block), aj}, {tq, aj},
@@ -1779,11 +1790,11 @@ alb_status build_ms_graph(alb_graph *g, MsScratch &m, MsArgs &a, int block) {
                   {{cmp, ac0}, {zero, aj}, {res((const void *)k_ms_td<false>, block), aj},
                    {res((const void *)k_ms_td_big<false>, block), aj}, {cmp, ac1},
                    {res((const void *)k_ms_td_finish, block), aj}}));
-    ALB_TRY(bu(kBrBUFilt, (const void *)k_ms_bu<true, true, true>, true));
-    ALB_TRY(bu(kBrBU, (const void *)k_ms_bu<true, true, false>, true));
-    ALB_TRY(bu(kBrBUWide, (const void *)k_ms_bu<true, true, false, true>, true));
-    ALB_TRY(bu(kBrBUNBFilt, (const void *)k_ms_bu<false, false, true>, false));
-    ALB_TRY(bu(kBrBUNB, (const void *)k_ms_bu<false, false, false>, false));
+    ALB_TRY(bu(kBrBUFilt, (const void *)k_ms_bu<true, true, true>, true, true));
+    ALB_TRY(bu(kBrBU, (const void *)k_ms_bu<true, true, false>, true, false));
+    ALB_TRY(bu(kBrBUWide, (const void *)k_ms_bu<true, true, false, true>, true, true));
+    ALB_TRY(bu(kBrBUNBFilt, (const void *)k_ms_bu<false, false, true>, false, true));
+    ALB_TRY(bu(kBrBUNB, (const void *)k_ms_bu<false, false, false>, false, true));
     int dneg = -1;
     void *eargs[] = {&a, &dneg, &wh};
     cudaGraphNode_t nsample, nend;
@@ -1874,8 +1885,8 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
             if (h->done || !h->need_flush) break;
             ALB_TRY(flush());
         }
-        // per level: branch, sample and end kernels plus the branch's step kernels
-        launches += (int64_t)h->levels_td * 9 + (int64_t)h->levels_bu * 10;
+        // per level: counted by k_ms_end from the branch the level took
+        launches += h->launches;
         if (gtrace) {
             const int nl = std::min<int>(h->level, kGTraceCap);
             std::vector<long long> rec((size_t)nl * kGTraceW);
@@ -1972,7 +1983,7 @@ alb_status msbfs_impl(alb_graph *g, const int32_t *roots, int32_t nroots, const 
                     launch_resident(k_ms_bu_long_fin, block, g->num_sms, stream, a, j);
                     launches += 4;
                 }
-                if (d != ALB_DIR_TOPDOWN) {  // push of the roots in tmask
+                if (d != ALB_DIR_TOPDOWN && h->prev_dir == ALB_DIR_TOPDOWN) {  // push of the roots in tmask
                     k_ms_tq<<<wide, block, 0, stream>>>(a, j);
                     launch_resident(k_ms_td<true>, block, g->num_sms, stream, a, j);
                     launch_resident(k_ms_td_big<true>, block, g->num_sms, stream, a, j);
