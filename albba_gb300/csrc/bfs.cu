@@ -301,16 +301,17 @@ __device__ __forceinline__ int rows_per_warp(int64_t qlen, int64_t mf, int64_t n
 constexpr int kBigShift = 38;
 constexpr unsigned long long kBigMask = (1ull << kBigShift) - 1;
 
+// qknown >= 0: the queue's length, already read by the caller.
 template <bool kPersist>
 __device__ void td_phase(const BfsArgs &a, int L, Range r, int64_t mf, bool append,
-                         bool lazy = false) {
+                         bool lazy = false, int64_t qknown = -1) {
     LazyCounts lc;
     const int32_t *Q = (L & 1) ? a.q1 : a.q0;
     int32_t *NQ = (L & 1) ? a.q0 : a.q1;
     unsigned long long *nq_slot = &a.ctl->qn[(L + 1) % 3];
     unsigned claimed = 0;
     uint32_t *N = (L & 1) ? a.bm0 : a.bm1;
-    const int64_t qlen = (int64_t)ld_state<kPersist>(&a.ctl->qn[L % 3]);
+    const int64_t qlen = qknown >= 0 ? qknown : (int64_t)ld_state<kPersist>(&a.ctl->qn[L % 3]);
     unsigned long long *big_slot = &a.ctl->nbig[L % 3];
     __shared__ int64_t s_ex[kMaxBlock / 32][32];
     __shared__ int64_t s_st[kMaxBlock / 32][32];
@@ -1154,6 +1155,7 @@ __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long lon
 // rows) and the (L + 1) % 3 accumulators that roll() consumes.
 struct LevelSums {
     unsigned long long nbig, n, mo, mi, full;
+    unsigned long long qn;  // qn[(L + 1) % 3]: the next level's queue, when it was built
 };
 
 __device__ bool grid_sync(const BfsArgs &a, unsigned nblocks, int L, LevelSums *sums = nullptr) {
@@ -1189,6 +1191,7 @@ __device__ bool grid_sync(const BfsArgs &a, unsigned nblocks, int L, LevelSums *
             sums->mo = g->acc_mo[k];
             sums->mi = g->acc_mi[k];
             sums->full = g->acc_full[k];
+            sums->qn = g->qn[k];
         }
         s_ok = ok ? 1 : 0;
     }
@@ -1204,11 +1207,17 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(BfsArgs a) {
     __shared__ BfsCtl c;
     __shared__ int s_dir;
     __shared__ LevelSums s_sums;
+    // the current level's queue length when the last level's closing barrier
+    // read it (-1: read it from the control block)
+    __shared__ int64_t s_qlen;
     // the selector network, read once per launch instead of once per level
     __shared__ __align__(16) float s_mlp[kMlpParams + 1];
     const unsigned nb = gridDim.x;
     const Range r{(int)blockIdx.x, (int)gridDim.x};
-    if (threadIdx.x == 0) c = *a.ctl;  // written by an earlier launch
+    if (threadIdx.x == 0) {
+        c = *a.ctl;  // written by an earlier launch
+        s_qlen = -1;
+    }
     if (a.mlp)
         for (int i = threadIdx.x; i <= kMlpParams; i += blockDim.x) s_mlp[i] = a.mlp[i];
     __syncthreads();
@@ -1254,13 +1263,15 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(BfsArgs a) {
         if (!ok) {
             // a barrier gave up: every block leaves below
         } else if (dir == ALB_DIR_TOPDOWN) {
+            int64_t qk = s_qlen;
             if (!c.q_valid || c.n_dirty) {
                 prep_phase<true>(a, L, !c.q_valid, c.n_dirty != 0, r);
                 ok = grid_sync(a, nb, L);
+                qk = -1;  // the queue was rebuilt
             }
             const bool app = td_append(a, c.mf);
             if (ok) {
-                td_phase<true>(a, L, r, c.mf, app, lazy);
+                td_phase<true>(a, L, r, c.mf, app, lazy, qk);
                 ok = grid_sync(a, nb, L, &s_sums);
             }
             if (ok && s_sums.nbig) {
@@ -1310,6 +1321,8 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(BfsArgs a) {
             roll(c, dir, s_sums.n, s_sums.mo, s_sums.mi, s_sums.full);
             c.dir = dir;
             if (lazy) c.lazy = 1;
+            // a top-down level built the next queue before its last barrier
+            s_qlen = dir == ALB_DIR_TOPDOWN ? (int64_t)s_sums.qn : -1;
         }
         __syncthreads();
         if (c.done) break;
