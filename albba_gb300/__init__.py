@@ -482,10 +482,16 @@ class Graph:
                                   C.byref(st)))
         return st
 
-    def msbfs64(self, roots, opts: BfsOpts | None = None) -> tuple[np.ndarray, Stats]:
-        """Levels from up to 64 roots at once: array (n, 64), column i = roots[i]."""
+    def msbfs64(self, roots, opts: BfsOpts | None = None,
+                out: np.ndarray | None = None) -> tuple[np.ndarray, Stats]:
+        """Levels from up to 64 roots at once: array (n, 64), column i = roots[i].
+        out: a C-contiguous int32 (n, 64) host array to fill (page-locked
+        memory is written by the device directly)."""
         r = np.ascontiguousarray(roots, dtype=np.int32)
-        out = np.empty((self.n, 64), np.int32)
+        if out is None:
+            out = np.empty((self.n, 64), np.int32)
+        elif out.dtype != np.int32 or out.shape != (self.n, 64) or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous int32 array of shape (n, 64)")
         st = Stats()
         o = opts or bfs_opts()
         check(_lib.alb_msbfs64(self._h, r.ctypes.data, r.shape[0], C.byref(o), out.ctypes.data,

@@ -80,6 +80,12 @@ def cmd_scales(a):
 
 
 def cmd_loops(a):
+    """Level-loop overhead on high-diameter and low-diameter graphs: every
+    loop driver, sigma in {1, 256, 4096}, the Beamer rule and the learned
+    selector (when its weights are installed)."""
+    from albba_gb300 import selector
+    loaded = selector.install()
+    policies = ["beamer"] + (["learned"] if loaded.get("plain") else [])
     graphs = [("grid4096", lambda: ab.gen_grid(4096, 4096, 0.1, 1e-4, seed=3)),
               ("er2^24", lambda: ab.gen_er(1 << 24, 8.0, seed=3))]
     for name, mk in graphs:
@@ -88,15 +94,17 @@ def cmd_loops(a):
         with ab.Graph(g, flags=ab.CSR_SYMMETRIC | ab.CSR_SORTED) as dg:
             for sigma in (1, 256, 4096):
                 bms = dg.sell_build(32, sigma)
-                for loop in ("host", "graph", "persistent"):
-                    opts = ab.bfs_opts("beamer", loop)
-                    plain_runs(dg, roots[:1], opts)
-                    hm, ms = plain_runs(dg, roots, opts)
-                    st = dg.bfs_device(int(roots[0]), None, None, opts)
-                    emit({"config": "loops", "graph": name, "sigma": sigma, "loop": loop,
-                          "levels": st.num_levels, "ms_median": statistics.median(ms),
-                          "us_per_level": 1000 * statistics.median(ms) / st.num_levels,
-                          "gteps_hmean": hm, "roots": len(roots), "sell_build_ms": bms})
+                for pol in policies:
+                    for loop in ("host", "graph", "persistent"):
+                        opts = ab.bfs_opts(pol, loop)
+                        plain_runs(dg, roots[:1], opts)
+                        hm, ms = plain_runs(dg, roots, opts)
+                        st = dg.bfs_device(int(roots[0]), None, None, opts)
+                        emit({"config": "loops", "graph": name, "sigma": sigma, "policy": pol,
+                              "loop": loop, "levels": st.num_levels,
+                              "ms_median": statistics.median(ms),
+                              "us_per_level": 1000 * statistics.median(ms) / st.num_levels,
+                              "gteps_hmean": hm, "roots": len(roots), "sell_build_ms": bms})
         del g
 
 

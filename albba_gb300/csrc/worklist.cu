@@ -11,7 +11,10 @@
 // graph stay in HBM, built by alb_sell_build with that graph's own C, sigma
 // and long-row threshold. Direction: Beamer alpha/beta per graph.
 // Output: level arrays (original ids), one per item, concatenated in the
-// order items were added.
+// order items were added. Graphs whose three bitmaps do not fit in one CTA's
+// shared memory are not refused: their items run one by one on the
+// device-driven single-root path (alb_bfs_device, CUDA-graph level loop,
+// the entry's alpha and beta) into the same output, before the launch.
 #include <algorithm>
 #include <cstring>
 #include <new>
@@ -54,7 +57,6 @@ __global__ void k_worklist(const WlGraph *graphs, const WlItem *items, int32_t n
     extern __shared__ uint32_t sm[];
     __shared__ int s_item;
     __shared__ WlCounters s_acc;
-    __shared__ int s_dir;
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const int nw = blockDim.x >> 5;
@@ -96,10 +98,7 @@ __global__ void k_worklist(const WlGraph *graphs, const WlItem *items, int32_t n
             else
                 dir = (nf >= prev_nf || (double)nf > (double)g.n / g.beta) ? ALB_DIR_BOTTOMUP
                                                                            : ALB_DIR_TOPDOWN;
-            if (threadIdx.x == 0) {
-                s_acc.n = s_acc.mo = s_acc.mi = 0;
-                s_dir = dir;
-            }
+            if (threadIdx.x == 0) s_acc.n = s_acc.mo = s_acc.mi = 0;
             __syncthreads();
             unsigned long long cn = 0, cmo = 0, cmi = 0;
             if (dir == ALB_DIR_BOTTOMUP) {
@@ -283,14 +282,40 @@ alb_status alb_worklist_run_device(alb_worklist *w, int32_t block, int32_t *d_le
         return fail(ALB_ERR_UNSUPPORTED, "alb_worklist_run: block must be 128, 256, 512 or 1024");
     alb_graph *g0 = w->entries[0].g;
     ALB_CK(cudaSetDevice(g0->device));
+    int max_smem = 0;
+    ALB_CK(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, g0->device));
+    // a graph fits the kernel when its three bitmaps and 1 KB of other
+    // shared state fit in one CTA
+    auto fits = [&](const Sell &s) {
+        return sizeof(uint32_t) * 3 * (size_t)s.nwords + 1024 <= (size_t)max_smem;
+    };
     std::vector<WlGraph> hg;
     std::vector<WlItem> hi;
     std::vector<int64_t> cost;
-    int64_t nwords_max = 0, off = 0, edges = 0, reached_cap = 0;
+    int64_t nwords_max = 0, off = 0;
+    float big_ms = 0.f;
+    int64_t big_kernels = 0;
     for (size_t gi = 0; gi < w->entries.size(); gi++) {
         const auto &e = w->entries[gi];
         const Sell &s = e.g->sell;
         if (!s.built) return fail(ALB_ERR_STATE, "alb_worklist_run: a graph lost its SELL build");
+        if (!fits(s)) {
+            // too large for one CTA's shared memory: the single-root path
+            alb_bfs_opts o;
+            alb_bfs_opts_default(&o);
+            o.policy = ALB_POLICY_BEAMER;
+            o.loop = ALB_LOOP_GRAPH;
+            o.alpha = e.alpha;
+            o.beta = e.beta;
+            for (int32_t r : e.roots) {
+                alb_stats bs;
+                ALB_TRY(alb_bfs_device(e.g, r, &o, d_levels + off, nullptr, &bs));
+                big_ms += bs.ms;
+                big_kernels += bs.kernels;
+                off += e.g->n;
+            }
+            continue;
+        }
         WlGraph d;
         std::memset(&d, 0, sizeof(d));
         d.n = e.g->n;
@@ -316,21 +341,22 @@ alb_status alb_worklist_run_device(alb_worklist *w, int32_t block, int32_t *d_le
         d.beta = e.beta;
         hg.push_back(d);
         nwords_max = std::max(nwords_max, s.nwords);
+        // the kernel's graph index is the position in hg
         for (int32_t r : e.roots) {
-            hi.push_back({(int32_t)gi, r, off});
+            hi.push_back({(int32_t)hg.size() - 1, r, off});
             cost.push_back(e.g->nnz_in);
             off += e.g->n;
         }
-        (void)edges;
-        (void)reached_cap;
+    }
+    if (hi.empty()) {  // every graph took the single-root path
+        if (st) {
+            std::memset(st, 0, sizeof(*st));
+            st->ms = big_ms;
+            st->kernels = big_kernels;
+        }
+        return ALB_OK;
     }
     const size_t smem = sizeof(uint32_t) * 3 * (size_t)nwords_max;
-    int max_smem = 0;
-    ALB_CK(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, g0->device));
-    if (smem + 1024 > (size_t)max_smem)
-        return fail(ALB_ERR_UNSUPPORTED,
-                    "alb_worklist_run: largest graph needs %zu bytes of shared memory (max %d)",
-                    smem, max_smem);
     // longest items first
     std::vector<int32_t> order(hi.size());
     std::iota(order.begin(), order.end(), 0);
@@ -372,8 +398,8 @@ alb_status alb_worklist_run_device(alb_worklist *w, int32_t block, int32_t *d_le
         ALB_CK(cudaEventElapsedTime(&ms, g0->ev0, g0->ev1));
         if (st) {
             std::memset(st, 0, sizeof(*st));
-            st->ms = ms;
-            st->kernels = 1;
+            st->ms = ms + big_ms;
+            st->kernels = 1 + big_kernels;
         }
         return ALB_OK;
     }();

@@ -263,8 +263,10 @@ alb_status alb_msbfs64_device(alb_graph *g, const int32_t *roots, int32_t nroots
  * visited bitmaps in shared memory, popping the next item from a global
  * counter (longest graphs first). Graphs keep their own SELL build (C, sigma,
  * long rows) and Beamer thresholds. Levels only (no parents). A graph added
- * to a work list must outlive the list's runs and must fit the shared-memory
- * budget (3 bits per vertex: up to about 600K vertices). */
+ * to a work list must outlive the list's runs. A graph whose bitmaps exceed
+ * one CTA's shared memory (3 bits per vertex: above about 600K vertices)
+ * runs its items one by one on the single-root path (alb_bfs_device,
+ * CUDA-graph loop, the entry's alpha and beta) into the same output. */
 typedef struct alb_worklist alb_worklist;
 alb_status alb_worklist_create(alb_worklist **out);
 void alb_worklist_destroy(alb_worklist *w);
@@ -274,7 +276,9 @@ alb_status alb_worklist_add(alb_worklist *w, alb_graph *g, const int32_t *roots,
 alb_status alb_worklist_size(const alb_worklist *w, int64_t *level_entries, int32_t *items);
 /* levels: host buffer of alb_worklist_size entries; item k (in the order
  * added, roots in order) occupies n_g consecutive entries, original ids.
- * block: threads per CTA (128, 256, 512 or 1024). stats.ms = kernel time. */
+ * block: threads per CTA (128, 256, 512 or 1024). stats.ms = kernel time
+ * plus the single-root runs of graphs too large for the kernel; stats.kernels
+ * counts the kernel and those runs' launches. */
 alb_status alb_worklist_run(alb_worklist *w, int32_t block, int32_t *levels, alb_stats *st);
 alb_status alb_worklist_run_device(alb_worklist *w, int32_t block, int32_t *d_levels,
                                    alb_stats *st);

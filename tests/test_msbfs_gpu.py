@@ -145,3 +145,18 @@ def test_full_scale_against_single_root():
         out = d.cpu().numpy()
     for i in (0, 37):
         assert np.array_equal(out[:, i], oracle.bfs(g.rowptr, g.col, int(roots[i]))[0])
+
+
+def test_host_levels_page_locked_and_pageable(rmat16_dev):
+    # page-locked output is written by the expansion across the host link;
+    # pageable output goes through a device buffer and a copy: same levels
+    import torch
+    g, roots, dg = rmat16_dev
+    pinned = torch.full((g.n, 64), -7, dtype=torch.int32, pin_memory=True).numpy()
+    a, _ = dg.msbfs64(roots, out=pinned)
+    b, _ = dg.msbfs64(roots)
+    want = oracle_levels(g, roots)
+    k = len(roots)
+    assert a is pinned
+    assert np.array_equal(a[:, :k], want) and np.array_equal(b[:, :k], want)
+    assert np.array_equal(a, b)

@@ -47,6 +47,26 @@ def test_worklist_uneven_graphs_bit_exact():
             assert np.array_equal(lv, ref), (gi, root, block)
 
 
+def test_worklist_carries_a_graph_too_large_for_shared_memory():
+    """A graph whose three bitmaps exceed one CTA's shared memory (RMAT s20:
+    3 x 128 KB) runs its items on the single-root path, into the same output
+    and order, beside small graphs that run in the persistent kernel."""
+    wl = ab.Worklist()
+    csrs = []
+    for i, (sc, ef) in enumerate([(10, 8), (20, 8), (12, 16)]):
+        g = ab.gen_rmat(sc, ef, seed=300 + i)
+        dg = ab.Graph(g)
+        dg.sell_build(32, 256)
+        wl.add(dg, g.pick_roots(3, seed=i))
+        csrs.append(g)
+    levels, st = wl.run(256)
+    assert st.ms > 0 and st.kernels > 1
+    for lv, (gi, root, n) in zip(levels, wl.layout):
+        g = csrs[gi]
+        ref, _, _ = oracle.bfs(g.rowptr, g.col, root)
+        assert np.array_equal(lv, ref), (gi, root)
+
+
 def test_worklist_rejects_bad_input():
     wl = ab.Worklist()
     g = ab.gen_rmat(8, 8, seed=1)
