@@ -128,7 +128,12 @@ __global__ void k_sp_fill(int64_t n, int64_t npad, const int32_t *perm, const in
 // Warp per slice, lane per row. The next group's columns and values are
 // requested before this group's x gathers are used, so each lane keeps the
 // stream and the gathers in flight together.
-__global__ void __launch_bounds__(256) k_spmv(int64_t n, int64_t nslices, const int32_t *perm,
+// 512 threads a block (32 K registers): such a block does not fit on an SM
+// beside a solo long-row CTA (k_spmv_long<true>), which keeps the slices off
+// the longest chains' SMs.
+constexpr int kSpBlock = 512;
+
+__global__ void __launch_bounds__(kSpBlock) k_spmv(int64_t n, int64_t nslices, const int32_t *perm,
                                               const int32_t *deg, const int64_t *slice_off,
                                               const int32_t *col, const double *val,
                                               const double *x, double *y) {
@@ -178,11 +183,14 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, int64_t nslices, const 
     }
 }
 
-// Lane per long row (rows longest first). The first nsolo warps (one per SM,
-// launched first) take one row each, the longest ones, so that the chains
-// that set the launch's length neither wait on 31 other lanes' gathers (a
-// warp's cp.async wait ends when its slowest lane's copies land) nor share an
-// SM with another long chain; the rest go 32 rows of similar length per warp.
+// Lane per long row (rows longest first). kSolo: the launch's longest rows,
+// one per CTA of 1024 threads of which one lane works: the CTA holds most of
+// its SM's registers until the row ends, so no slices block shares the SM
+// and its fp64 pipe with the chain that sets the SpMV's length (measured: a
+// slices kernel beside the longest chain slowed it from 8.0 to about 10 ms at
+// RMAT s22), and the chain waits on no other lane's gathers (a warp's
+// cp.async wait ends when its slowest lane's copies land). The other long
+// rows go 32 of similar length per warp.
 // Entries in blocks of kLb. Each lane streams its row through two
 // shared-memory rings filled by cp.async: column ids kLd blocks ahead of the
 // x gathers that need them, values and x (each gather 8 bytes) kLd blocks
@@ -191,7 +199,7 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t n, int64_t nslices, const 
 // fma chain at about 90 cycles per entry, each load has kLd x kLb entries'
 // worth of chain time to land. Ring layout: lane-fastest, so that the 32
 // lanes' accesses fall in different banks.
-constexpr int kSpLongBlock = 32;
+constexpr int kSpLongBlock = 32;  // one warp per CTA
 constexpr int kLb = 8;
 constexpr int kLd = 8;
 
@@ -209,17 +217,23 @@ __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-__global__ void __launch_bounds__(kSpLongBlock) k_spmv_long(int64_t nlong, int64_t nsolo,
-                                                         const int32_t *lrow, const int64_t *lptr,
-                                                         const int32_t *llen, const int32_t *lcol,
-                                                         const double *lval, const double *x,
-                                                         double *y) {
-    __shared__ double2 s_v[kSpLongBlock / 32][kLd][kLb / 2][32];
-    __shared__ double s_x[kSpLongBlock / 32][kLd][kLb][32];
-    __shared__ int4 s_c[kSpLongBlock / 32][kLd][kLb / 4][32];
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int64_t wg = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t i = wg < nsolo ? (lane == 0 ? wg : nlong) : nsolo + (wg - nsolo) * 32 + lane;
+constexpr int kSoloThreads = 1024;
+constexpr int64_t kSoloRows = 8;  // rows on CTAs of their own
+
+template <bool kSolo>
+__global__ void __launch_bounds__(kSolo ? kSoloThreads : kSpLongBlock)
+    k_spmv_long(int64_t nlong, int64_t first, const int32_t *lrow, const int64_t *lptr,
+                const int32_t *llen, const int32_t *lcol, const double *lval, const double *x,
+                double *y) {
+    __shared__ double2 s_v[1][kLd][kLb / 2][32];
+    __shared__ double s_x[1][kLd][kLb][32];
+    __shared__ int4 s_c[1][kLd][kLb / 4][32];
+    // kSolo: warp 0 of CTA b takes row first + b on lane 0 (the other warps
+    // leave at once); otherwise warp w takes rows first + 32 w + lane
+    if (kSolo && threadIdx.x >= 32) return;
+    const int lane = threadIdx.x & 31, wib = 0;
+    const int64_t i = kSolo ? (lane == 0 ? first + blockIdx.x : nlong)
+                            : first + (int64_t)blockIdx.x * 32 + lane;
     const int64_t b = i < nlong ? lptr[i] : 0;
     const int64_t e = i < nlong ? b + llen[i] : 0;
     const int64_t nblk = (e - b + kLb - 1) / kLb;
@@ -458,26 +472,29 @@ void destroy(alb_sellmat *m) {
 
 alb_status launch(alb_sellmat *m, const double *d_x, double *d_y, float *us) {
     int per = 0, sms = 0;
-    ALB_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_spmv, 256, 0));
+    ALB_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_spmv, kSpBlock, 0));
     ALB_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device));
-    const int64_t want = (m->nslices + 7) / 8;
-    const int64_t cap = (int64_t)(per > 0 ? per : 4) * sms;
+    const int64_t want = (m->nslices + 15) / 16;  // 16 warps a block, one slice each
+    const int64_t cap = (int64_t)(per > 0 ? per : 2) * sms;
     const unsigned grid = (unsigned)std::max<int64_t>(1, std::min(want, cap));
     if (us) ALB_CK(cudaEventRecord(m->ev0, m->stream));
     // the long rows' chains (one dependent fma per entry, the longest row
-    // the critical path) start first, on the side stream, and the slices
-    // run beside them
+    // the critical path) start first, and the slices run beside them
     if (m->nlong > 0) {
         ALB_CK(cudaEventRecord(m->fork, m->stream));
         ALB_CK(cudaStreamWaitEvent(m->side, m->fork, 0));
-        const int64_t nsolo = std::min<int64_t>(m->nlong, sms);
-        const int64_t warps = nsolo + (m->nlong - nsolo + 31) / 32;
-        k_spmv_long<<<blocks_for(warps * 32, kSpLongBlock), kSpLongBlock, 0, m->side>>>(
-            m->nlong, nsolo, m->lrow, m->lptr, m->llen, m->lcol, m->lval, d_x, d_y);
+        // the few longest rows on CTAs of their own (side stream); the other
+        // long rows, then the slices, on the main stream beside them
+        const int64_t nsolo = std::min<int64_t>(m->nlong, kSoloRows);
+        k_spmv_long<true><<<(unsigned)nsolo, kSoloThreads, 0, m->side>>>(
+            m->nlong, 0, m->lrow, m->lptr, m->llen, m->lcol, m->lval, d_x, d_y);
         ALB_CK(cudaGetLastError());
         ALB_CK(cudaEventRecord(m->join, m->side));
+        if (m->nlong > nsolo)
+            k_spmv_long<false><<<blocks_for(m->nlong - nsolo, 32), kSpLongBlock, 0, m->stream>>>(
+                m->nlong, nsolo, m->lrow, m->lptr, m->llen, m->lcol, m->lval, d_x, d_y);
     }
-    k_spmv<<<grid, 256, 0, m->stream>>>(m->n, m->nslices, m->perm, m->deg, m->slice_off, m->col,
+    k_spmv<<<grid, kSpBlock, 0, m->stream>>>(m->n, m->nslices, m->perm, m->deg, m->slice_off, m->col,
                                          m->val, d_x, d_y);
     ALB_CK(cudaGetLastError());
     if (m->nlong > 0) ALB_CK(cudaStreamWaitEvent(m->stream, m->join, 0));

@@ -518,10 +518,13 @@ def e2e_batched(args, g, roots, ab, torch, opts, steps: int = 5) -> dict:
         step()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    marks = []
     for _ in range(steps):
-        step()
+        step()  # returns after the levels are in host memory
+        marks.append(time.perf_counter())
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
+    per_step = [(b - a) * 1e3 for a, b in zip([t0] + marks[:-1], marks)]
     # phase split of one more step, right away (wall clock, a synchronize
     # after each call)
     ph = {}
@@ -550,6 +553,7 @@ def e2e_batched(args, g, roots, ab, torch, opts, steps: int = 5) -> dict:
     floor_ms = h2d / fl["h2d_gbs"] / 1e6 + d2h / fl["d2h_gbs"] / 1e6
     return {"value": steps * edges / dt / 1e9, "unit": "GTEPS", "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h, "steps": steps, "ms_per_step": dt / steps * 1e3,
+            "step_ms": [round(x, 2) for x in per_step],
             "phases": {k: round(v, 2) for k, v in ph.items()},
             "copy_floor": {"h2d_gbs": round(fl["h2d_gbs"], 1), "d2h_gbs": round(fl["d2h_gbs"], 1),
                            "ms_per_step": round(floor_ms, 2),
