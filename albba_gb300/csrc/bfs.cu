@@ -620,6 +620,7 @@ __device__ __forceinline__ uint32_t ld_front(const uint32_t *F, int32_t w) {
 // Words per run of the bottom-up pull (a warp's unit of work from the
 // level's counter): one visited word per lane.
 constexpr int64_t kBuRun = 32;
+constexpr int kBuWords = 2;  // words a warp scans at a time
 
 template <bool kPersist, bool kBypass, bool kEarly, bool kSmemF = false>
 __device__ void bu_phase(const BfsArgs &a, int L, Range r, const uint32_t *Fs = nullptr) {
@@ -633,6 +634,7 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r, const uint32_t *Fs = 
     unsigned long long cmo = 0, cmi = 0, bytes = 0;
     unsigned n_wbyp = 0, n_rows = 0, n_grp = 0, n_gtot = 0;
     const uint64_t pol = l2_evict_first();
+    constexpr int kW = kPersist ? 1 : kBuWords;
     // Words come in runs of kBuRun from the level's counter. Lane l holds the
     // visited mask of word l of the run (one coalesced load, the next run's
     // requested one run ahead; only the warp that takes a word writes its
@@ -669,75 +671,119 @@ __device__ void bu_phase(const BfsArgs &a, int L, Range r, const uint32_t *Fs = 
             nxt = grab();
             vnxt = run_vis(nxt);
         }
+      // kW words at a time (kBuWords; one in the persistent kernel, whose
+      // 80-register budget more would overflow): lane l scans row l of each,
+      // their geometry, first column groups and frontier words requested
+      // together, so that each lane keeps that many times the loads in flight
+      // (a word costs a few dependent round trips whatever its rows' lengths).
       while (todo) {
-        const int q = __ffs(todo) - 1;
-        todo &= todo - 1;
-        const int64_t w = base_w + q;
-        const uint32_t vis = __shfl_sync(kFull, vrun, q);
-        const int32_t p = (int32_t)(w * 32 + lane);
-        // rows past n are preset visited; clamp their slice index
-        const int64_t s = (int64_t)(p < a.n ? p : a.n - 1) >> log2C;
-        const int32_t wd = __ldg(a.width + s);
-        const int64_t so = __ldg(a.slice_off + s);
-        bool active = !((vis >> lane) & 1u);
-        const int32_t ng = active ? (wd + 3) >> 2 : 0;
-        n_rows += ng > 0;
-        n_gtot += ng;
-        const int4 *cp = a.col4 + (so >> 2) + (p & (C - 1));
-        int32_t found = -1;
-        // group j+1 is requested before group j's frontier tests, so each lane
-        // keeps one column load in flight while it waits on the bitmap
-        int4 c = make_int4(p, p, p, p);
-        if (active && ng > 0) c = ld_stream(cp, pol);
+        int qs[kW];
+        int nr = 0;  // words taken (warp-uniform)
+#pragma unroll
+        for (int t = 0; t < kW; t++) {
+            qs[t] = todo ? __ffs(todo) - 1 : qs[0];
+            nr += todo != 0;
+            todo &= todo - 1;
+        }
+        int64_t w[kW];
+        uint32_t vis[kW];
+        int32_t p[kW], ng[kW], found[kW];
+        bool active[kW], long_cand[kW];
+        const int4 *cp[kW];
+        int4 c[kW];
+#pragma unroll
+        for (int t = 0; t < kW; t++) {
+            w[t] = base_w + qs[t];
+            vis[t] = __shfl_sync(kFull, vrun, qs[t]);
+            p[t] = (int32_t)(w[t] * 32 + lane);
+            found[t] = -1;
+        }
+        int32_t wd[kW];
+        int64_t so[kW];
+#pragma unroll
+        for (int t = 0; t < kW; t++) {
+            // rows past n are preset visited; clamp their slice index
+            const int64_t sl = (int64_t)(p[t] < a.n ? p[t] : a.n - 1) >> log2C;
+            wd[t] = t < nr ? __ldg(a.width + sl) : 0;
+            so[t] = t < nr ? __ldg(a.slice_off + sl) : 0;
+        }
+#pragma unroll
+        for (int t = 0; t < kW; t++) {
+            active[t] = t < nr && !((vis[t] >> lane) & 1u);
+            ng[t] = active[t] ? (wd[t] + 3) >> 2 : 0;
+            n_rows += ng[t] > 0;
+            n_gtot += ng[t];
+            cp[t] = a.col4 + (so[t] >> 2) + (p[t] & (C - 1));
+            // group j+1 is requested before group j's frontier tests, so each
+            // lane keeps column loads in flight while it waits on the bitmap
+            c[t] = make_int4(p[t], p[t], p[t], p[t]);
+            if (active[t] && ng[t] > 0) c[t] = ld_stream(cp[t], pol);
+        }
         // an unvisited row whose first entry is padding is a long row (rows
         // without sources start visited): the long-row pass has run already
-        const bool long_cand = active && c.x == p;
-        for (int32_t j = 0;; j++) {
-            active = active && (j < ng);
-            if (!__any_sync(kFull, active)) break;
-            if (!active) continue;
-            bytes += 32;  // four columns and the four frontier words they select
-            n_grp++;
-            int4 nx = make_int4(p, p, p, p);
-            if (j + 1 < ng) nx = ld_stream(cp + (int64_t)(j + 1) * C, pol);
-            ALB_CHECK_ID4(c, a.nwords * 32, p, &a.ctl->err);
-            const uint32_t f0 = ld_front<kSmemF, kPersist>(F, c.x >> 5);
-            const uint32_t f1 = ld_front<kSmemF, kPersist>(F, c.y >> 5);
-            const uint32_t f2 = ld_front<kSmemF, kPersist>(F, c.z >> 5);
-            const uint32_t f3 = ld_front<kSmemF, kPersist>(F, c.w >> 5);
-            const int32_t cc[4] = {c.x, c.y, c.z, c.w};
-            const uint32_t ff[4] = {f0, f1, f2, f3};
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
-                if (!active) break;
-                if (kEarly && cc[k] == p) {
-                    active = false;  // padding: end of row
-                } else if ((ff[k] >> (cc[k] & 31)) & 1u) {
-                    if (found < 0) found = cc[k];
-                    if (kEarly) active = false;
+        for (int t = 0; t < kW; t++) long_cand[t] = active[t] && c[t].x == p[t];
+        for (int32_t j = 0;; j++) {
+            bool any = false;
+#pragma unroll
+            for (int t = 0; t < kW; t++) {
+                active[t] = active[t] && (j < ng[t]);
+                any = any || active[t];
+            }
+            if (!__any_sync(kFull, any)) break;
+            int4 nx[kW];
+            uint32_t ff[kW][4];
+#pragma unroll
+            for (int t = 0; t < kW; t++) {
+                nx[t] = make_int4(p[t], p[t], p[t], p[t]);
+                if (!active[t]) continue;
+                bytes += 32;  // four columns and the four frontier words they select
+                n_grp++;
+                if (j + 1 < ng[t]) nx[t] = ld_stream(cp[t] + (int64_t)(j + 1) * C, pol);
+                ALB_CHECK_ID4(c[t], a.nwords * 32, p[t], &a.ctl->err);
+                ff[t][0] = ld_front<kSmemF, kPersist>(F, c[t].x >> 5);
+                ff[t][1] = ld_front<kSmemF, kPersist>(F, c[t].y >> 5);
+                ff[t][2] = ld_front<kSmemF, kPersist>(F, c[t].z >> 5);
+                ff[t][3] = ld_front<kSmemF, kPersist>(F, c[t].w >> 5);
+            }
+#pragma unroll
+            for (int t = 0; t < kW; t++) {
+                if (!active[t]) continue;
+                const int32_t cc[4] = {c[t].x, c[t].y, c[t].z, c[t].w};
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    if (!active[t]) break;
+                    if (kEarly && cc[k] == p[t]) {
+                        active[t] = false;  // padding: end of row
+                    } else if ((ff[t][k] >> (cc[k] & 31)) & 1u) {
+                        if (found[t] < 0) found[t] = cc[k];
+                        if (kEarly) active[t] = false;
+                    }
+                }
+                c[t] = nx[t];
+            }
+        }
+        for (int t = 0; t < nr; t++) {
+            bool reached = found[t] >= 0;
+            bool by_long = false;
+            if (long_cand[t] && !reached && a.nlong)
+                by_long = reached = ld_state<kPersist>(a.parent_pos + p[t]) != kFull;
+            const unsigned nm = __ballot_sync(kFull, reached);
+            if (lane == 0) {
+                N[w[t]] = nm;
+                if (nm) {
+                    a.vis[w[t]] = vis[t] | nm;
+                    full += (vis[t] != kFull && (vis[t] | nm) == kFull);
                 }
             }
-            c = nx;
-        }
-        bool reached = found >= 0;
-        bool by_long = false;
-        if (long_cand && !reached && a.nlong)
-            by_long = reached = ld_state<kPersist>(a.parent_pos + p) != kFull;
-        const unsigned nm = __ballot_sync(kFull, reached);
-        if (lane == 0) {
-            N[w] = nm;
-            if (nm) {
-                a.vis[w] = vis | nm;
-                full += (vis != kFull && (vis | nm) == kFull);
+            if (reached) {
+                a.level_pos[p[t]] = lvl;
+                if (!by_long) a.parent_pos[p[t]] = (uint32_t)__ldg(a.perm + found[t]);
+                bytes += 20;  // level, parent, the parent's id, two degrees
+                cn++;
+                cmo += (unsigned long long)__ldg(a.odeg + p[t]);
+                cmi += (unsigned long long)__ldg(a.ideg + p[t]);
             }
-        }
-        if (reached) {
-            a.level_pos[p] = lvl;
-            if (!by_long) a.parent_pos[p] = (uint32_t)__ldg(a.perm + found);
-            bytes += 20;  // level, parent, the parent's id, two degrees
-            cn++;
-            cmo += (unsigned long long)__ldg(a.odeg + p);
-            cmi += (unsigned long long)__ldg(a.ideg + p);
         }
       }
     }
@@ -1041,11 +1087,12 @@ __global__ void k_td_finish(BfsArgs a) {
 }
 
 // The slice pass runs with kBuBlock threads whatever the loop's block size:
-// the bound holds it at 48 registers (5 blocks, 40 warps per SM).
+// the bound holds it at 64 registers (4 blocks, 32 warps per SM; it scans
+// two words at a time).
 constexpr unsigned kBuBlock = 256;
 
 template <bool kBypass, bool kEarly>
-__global__ void __launch_bounds__(kBuBlock, 5) k_bu(BfsArgs a) {
+__global__ void __launch_bounds__(kBuBlock, 4) k_bu(BfsArgs a) {
     bu_phase<false, kBypass, kEarly>(a, a.ctl->level, Range{(int)blockIdx.x, (int)gridDim.x});
 }
 

@@ -485,7 +485,7 @@ def copy_floor(torch, nbytes: int = 1 << 30) -> dict:
     return out
 
 
-def e2e_batched(args, g, roots, ab, torch, opts, steps: int = 5) -> dict:
+def e2e_batched(args, g, roots, ab, torch, opts, steps: int = 10) -> dict:
     """Host CSR in, host levels out, through the C ABI: alb_graph_create +
     alb_sell_build + alb_msbfs64 (n x 64 int32 levels copied back)."""
     # page-locked host buffers: the graph the caller hands over and the levels
