@@ -653,13 +653,24 @@ __global__ void k_fill_chunks(int64_t nchunks, const int32_t *crow, const int32_
         const int64_t lo = slo[i], hi = shi[i];
         const int64_t o = by_pos ? obase[p] : obase[i];
         const int64_t o2 = out2 ? obase2[p] : 0;
-        for (int64_t j = s0 + lane; j < s1; j += 32) {
-            const int32_t c = ld_hint(col + j, pstream);
-            if (c != v) {
+        // four entries per lane per step: their column loads, then their
+        // four inv gathers, are issued before any is used
+        for (int64_t j0 = s0 + lane; j0 < s1; j0 += 128) {
+            int32_t c[4], q[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int64_t j = j0 + 32 * u;
+                c[u] = j < s1 ? ld_hint(col + j, pstream) : v;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) q[u] = c[u] != v ? __ldg(inv + c[u]) : 0;
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int64_t j = j0 + 32 * u;
+                if (c[u] == v) continue;  // a self-loop, or past the chunk
                 const int64_t at = (j - b) - (min(max(j, lo), hi) - lo);
-                const int32_t q = __ldg(inv + c);
-                __stcs(out + o + at, q);
-                if (out2) __stcs(out2 + o2 + at, q);
+                __stcs(out + o + at, q[u]);
+                if (out2) __stcs(out2 + o2 + at, q[u]);
             }
         }
     }
