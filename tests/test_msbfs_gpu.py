@@ -78,6 +78,13 @@ def test_many_levels_flush_snapshots():
         dg.sell_build(32, 1)
         lv, st = check(g, dg, np.array([0, 150, 299, 7], np.int32))
         assert st.num_levels > 64
+        # the same into page-locked host memory, which the expansion writes
+        # directly (its later flushes included)
+        import torch
+        roots = np.array([0, 150, 299, 7], np.int32)
+        pinned = torch.full((n, 64), -7, dtype=torch.int32, pin_memory=True).numpy()
+        lv2, _ = dg.msbfs64(roots, out=pinned)
+        assert lv2 is pinned and np.array_equal(lv2, lv)
 
 
 def test_device_output_and_trace(rmat16_dev):
