@@ -245,8 +245,12 @@ alb_status alb_level_trace(const alb_graph *g, int32_t cap, alb_level_rec *out,
 /* Bit-parallel BFS from up to 64 roots at once (one uint64 frontier/visited
  * word per vertex, one traversal of the matrix per level for all roots).
  * levels (host, n * 64 int32) is vertex-major: levels[v * 64 + i] = depth of
- * v from roots[i], -1 if unreached (and for i >= nroots). The level loop is
- * host-driven (one small device-to-host read per level); the direction of
+ * v from roots[i], -1 if unreached (and for i >= nroots); page-locked host
+ * memory is written by the device directly, other host memory through a
+ * device buffer and one copy. The level loop is a CUDA graph that decides
+ * and launches every level on the device (ALB_LOOP_GRAPH, the default; the
+ * host steps in only when the 32-level snapshot store fills) or host-driven
+ * (ALB_LOOP_HOST: one small device-to-host read per level); the direction of
  * each level is decided on the device (policy as for alb_bfs; the learned
  * policy uses selector 1). stats: reached = (vertex, root) pairs reached,
  * edges = sum over roots of push-side entries in the root's component. */
