@@ -352,7 +352,10 @@ alb_status alb_spmspv_merge(alb_graph *g, const int32_t *x, int64_t nx, const ui
  * vfmadd chain -- so y is bit-identical to the reference's for the same CSR.
  * Rows are ordered by length inside sigma windows (1..16384) as in the
  * reference; slices hold 32 rows, entries 4-interleaved (int32 columns,
- * fp64 values), diagonal and repeated entries kept as given. */
+ * fp64 values), diagonal and repeated entries kept as given. Rows longer
+ * than 512 entries are summed one lane each from a separate list (the eight
+ * longest on SMs of their own): the in-order chain of fused multiply-adds
+ * makes a launch last at least as long as its longest row's chain. */
 typedef struct alb_sellmat alb_sellmat;
 alb_status alb_sellmat_create(int64_t n, const int64_t *rowptr, const int32_t *col,
                               const double *values, int32_t sigma, alb_sellmat **out);
